@@ -1,0 +1,100 @@
+"""Loaders for the ORACLE libraries (test and measurement infrastructure).
+
+Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline /
+reference legs use this module: it runs the CPU restatement in
+``oracle/unbind_port.cpp`` (liboracle.so) or the reference's own Unbind
+compiled into ``oracle/_ref/``.  The product path (``hbtg.gpu``) never
+imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+from .abi import CallBuffers, Inputs, Params
+
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+ORACLE_DIR = os.path.join(REPO, "oracle")
+
+_libs = {}
+
+
+def _build_module():
+    if ORACLE_DIR not in sys.path:
+        sys.path.insert(0, ORACLE_DIR)
+    import build_oracle  # noqa: E402
+    return build_oracle
+
+
+def port_lib():
+    if "port" not in _libs:
+        path = _build_module().build_port()
+        lib = C.CDLL(path)
+        lib.oracle_unbind_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        lib.oracle_unbind_batch.restype = C.c_int
+        lib.oracle_last_interactions.restype = C.c_int64
+        lib.oracle_last_cells.restype = C.c_int64
+        for fn in (lib.oracle_tree_potential, lib.oracle_direct_potential):
+            fn.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                           C.c_void_p]
+            fn.restype = C.c_int
+        _libs["port"] = lib
+    return _libs["port"]
+
+
+def reference_lib(variant):
+    """The reference's own Unbind ('dmo' or 'hydro'); None when it was not built."""
+    key = "ref_" + variant
+    if key not in _libs:
+        path = os.path.join(ORACLE_DIR, "_ref", "libref_%s.so" % variant)
+        if not os.path.exists(path):
+            mod = _build_module()
+            if mod.reference_available():
+                mod.build_reference()
+        if not os.path.exists(path):
+            return None
+        lib = C.CDLL(path)
+        lib.ref_unbind_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
+        lib.ref_unbind_batch.restype = C.c_int
+        _libs[key] = lib
+    return _libs[key]
+
+
+def run_port(inp: Inputs, params: Params, nthreads=0, inner_parallel=False, want_potential=False):
+    buf = CallBuffers(inp, want_energy=True, want_potential=want_potential)
+    rc = port_lib().oracle_unbind_batch(C.byref(params), C.byref(buf.c), nthreads, int(inner_parallel))
+    if rc != 0:
+        raise RuntimeError("oracle_unbind_batch returned %d" % rc)
+    return buf.out
+
+
+def run_reference(inp: Inputs, params: Params, nthreads=0, inner_parallel=False, want_potential=False):
+    variant = "dmo" if params.dm_only else "hydro"
+    if not params.dm_only and not params.thermal:
+        raise ValueError("the reference oracle is built with UNBIND_WITH_THERMAL_ENERGY for hydro inputs")
+    lib = reference_lib(variant)
+    if lib is None:
+        raise FileNotFoundError("reference oracle not built (reference sources absent)")
+    buf = CallBuffers(inp, want_energy=True, want_potential=want_potential)
+    rc = lib.ref_unbind_batch(C.byref(params), C.byref(buf.c), nthreads, int(inner_parallel))
+    if rc != 0:
+        raise RuntimeError("ref_unbind_batch returned %d" % rc)
+    return buf.out
+
+
+def tree_potential(params, src_pos, src_mass, tgt_pos, tgt_mass=None, direct=False):
+    lib = port_lib()
+    src_pos = np.ascontiguousarray(src_pos, np.float32)
+    src_mass = np.ascontiguousarray(src_mass, np.float32)
+    tgt_pos = np.ascontiguousarray(tgt_pos, np.float32)
+    tm = None if tgt_mass is None else np.ascontiguousarray(tgt_mass, np.float32)
+    out = np.zeros(len(tgt_pos), np.float64)
+    fn = lib.oracle_direct_potential if direct else lib.oracle_tree_potential
+    rc = fn(C.byref(params), len(src_pos), src_pos.ctypes.data, src_mass.ctypes.data, len(tgt_pos),
+            tgt_pos.ctypes.data, None if tm is None else tm.ctypes.data, out.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("oracle potential returned %d" % rc)
+    return out

@@ -1,0 +1,181 @@
+/*
+ * hbt_unbind_gpu.h — C ABI of the GB300 unbinding library (libhbtg.so).
+ *
+ * Drop-in for HBT-HERONS' iterative gravitational unbinding:
+ *   void Subhalo_t::Unbind(const Snapshot_t &epoch)          src/subhalo.h:152,
+ *                                                            src/subhalo_unbind.cpp:463-808
+ *   void SubhaloSnapshot_t::RefineParticles(MpiWorker_t &)   src/subhalo.h:343,
+ *                                                            src/subhalo_unbind.cpp:855-919
+ * One call unbinds a batch of independent subhaloes (a batch of one is
+ * Subhalo_t::Unbind; the field/new-subhalo loops of RefineParticles are a
+ * batch of many).  Plain pointers and sizes only; no C++ types cross it.
+ *
+ * Conventions
+ *  - Every function returns an hbtg_status (0 = OK).  Nothing throws across
+ *    the ABI and the device never traps: per-subhalo problems are reported
+ *    in batch->status.
+ *  - The caller owns every array.  The handle owns the device arena.
+ *  - One handle per host thread.  hbtg_unbind_batch is synchronous.
+ */
+#ifndef HBT_UNBIND_GPU_H
+#define HBT_UNBIND_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HBTG_TYPE_MAX 6 /* ParticleType_t::TypeMax, src/datatypes.h:206-215 */
+#define HBTG_KIN_STRIDE 5  /* SpecificSelfPotentialEnergy, SpecificSelfKineticEnergy, SpecificAngularMomentum[3] */
+#define HBTG_CORE_STRIDE 8 /* CoreComovingPosition[3], CorePhysicalVelocity[3], CoreComovingSigmaR, CorePhysicalSigmaV */
+
+/* Return codes of every entry point. */
+enum hbtg_status
+{
+  HBTG_OK = 0,
+  HBTG_ERR_INVALID = 1,     /* bad argument or inconsistent batch description */
+  HBTG_ERR_NOMEM = 2,       /* device or pinned-host allocation failed */
+  HBTG_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  HBTG_ERR_MAX_ITER = 4,    /* some subhalo reached params.max_iterations (see batch->status) */
+  HBTG_ERR_UNSUPPORTED = 5, /* parameter combination not implemented on this path */
+  HBTG_ERR_NO_DEVICE = 6    /* no CUDA device, or the device is not sm_103 */
+};
+
+/* Per-subhalo outcome written to hbtg_batch.status. */
+enum hbtg_sub_status
+{
+  HBTG_SUB_CONVERGED = 0, /* Nbound >= Nlast*BoundMassPrecision reached (src/subhalo_unbind.cpp:690) */
+  HBTG_SUB_DISRUPTED = 1, /* Nbound < MinNumPartOfSub or too few tracers (src/subhalo_unbind.cpp:647) */
+  HBTG_SUB_EMPTY = 2,     /* no particles: the orphan early return (src/subhalo_unbind.cpp:472-489) */
+  HBTG_SUB_MAX_ITER = 3   /* stopped at params.max_iterations; outputs hold the last iterate */
+};
+
+/* The HBTConfig / PhysicalConst / Cosmology values Subhalo_t::Unbind reads
+ * (src/config_parser.h:22-201, src/snapshot.h:18-48).  Where the reference
+ * stores a value as HBTReal (float), the library rounds it to float first. */
+typedef struct hbtg_params
+{
+  double box_size;             /* BoxSize */
+  int32_t periodic;            /* PeriodicBoundaryOn */
+  double softening;            /* HBTConfig.GetCurrentSoftening(a) (src/config_parser.cpp:641-649) */
+  double tree_node_resolution; /* TreeNodeResolution = 0.1*SofteningHalo (src/config_parser.cpp:210) */
+  double open_angle;           /* TreeNodeOpenAngle (theta) */
+  double bound_mass_precision; /* BoundMassPrecision */
+  int64_t min_num_part;        /* MinNumPartOfSub */
+  int64_t min_num_tracer;      /* MinNumTracerPartOfSub */
+  int32_t tracer_type_mask;    /* TracerParticleBitMask */
+  int32_t no_subsample_mask;   /* DoNotSubsampleParticleBitMask */
+  int64_t max_sample_size;     /* MaxSampleSizeOfPotentialEstimate (0 = no subsampling) */
+  int32_t refine_most_bound;   /* RefineMostBoundParticle */
+  double refine_fraction;      /* BoundFractionCenterRefinement */
+  int32_t upscale_per_type;    /* PotentialEstimateUpscaleMassesPerType */
+  int64_t sub_core_size_min;   /* SubCoreSizeMin */
+  double sub_core_size_factor; /* SubCoreSizeFactor */
+  int32_t dm_only;             /* 1 = DM_ONLY build semantics: types ignored, every particle a tracer */
+  int32_t thermal;             /* 1 = UNBIND_WITH_THERMAL_ENERGY: E += InternalEnergy */
+  double G;                    /* PhysicalConst::G */
+  double scale_factor;         /* epoch.Cosmology.ScaleFactor */
+  double hubble;               /* epoch.Cosmology.Hz */
+  int32_t max_iterations;      /* bound on the unbinding loop (no counterpart in the reference) */
+  int32_t mode;                /* 0 = reference tree geometry (parity); other values reserved */
+  int64_t seed;                /* seeds the tie-break of sub-resolution cells (reference: drand48) */
+} hbtg_params;
+
+/* A batch of subhaloes in CSR layout: subhalo s owns particles
+ * [offsets[s], offsets[s+1]) of every per-particle array.  Local index k of
+ * subhalo s means global row offsets[s]+k.
+ *
+ * Inputs mirror Particle_t (src/snapshot.h:62-106) as structure-of-arrays;
+ * in/out fields mirror the Subhalo_t members Unbind reads and writes
+ * (src/subhalo.h:26-216). */
+typedef struct hbtg_batch
+{
+  int64_t n_sub;
+  const int64_t *offsets; /* [n_sub+1], offsets[0] = 0, non-decreasing */
+  const float *pos;       /* [3N] ComovingPosition, xyz interleaved */
+  const float *vel;       /* [3N] PhysicalVelocity */
+  const float *mass;      /* [N]  Mass */
+  const float *u;         /* [N]  InternalEnergy, or NULL (read only if params.thermal) */
+  const int64_t *id;      /* [N]  Id */
+  const uint8_t *type;    /* [N]  Type (0..5), or NULL = every particle TypeDM */
+
+  float *ref_pos;       /* [3 n_sub] in: initial ComovingAveragePosition; out: final frame */
+  float *ref_vel;       /* [3 n_sub] in: initial PhysicalAverageVelocity; out: final frame */
+  float *mostbound_pos; /* [3 n_sub] in/out: ComovingMostBoundPosition */
+  float *mostbound_vel; /* [3 n_sub] in/out: PhysicalMostBoundVelocity */
+  int64_t *most_bound_id; /* [n_sub] in/out: MostBoundParticleId (kept when not resolved) */
+
+  int64_t *order;       /* [N] out: order[offsets[s]+k] = input local index of the particle now at position k */
+  int64_t *nbound;      /* [n_sub] out: Nbound */
+  float *mbound;        /* [n_sub] out: Mbound */
+  int64_t *nbound_type; /* [6 n_sub] out: NboundType, or NULL */
+  float *mbound_type;   /* [6 n_sub] out: MboundType, or NULL */
+  int64_t *tracer_index; /* [n_sub] out: TracerIndex */
+  float *kinematics;    /* [5 n_sub] out, or NULL (HBTG_KIN_STRIDE) */
+  float *core;          /* [8 n_sub] out, or NULL (HBTG_CORE_STRIDE) */
+  float *energy;        /* [N] out, or NULL: ParticleBindingEnergies at positions k < nbound */
+  float *potential;     /* [N] out, or NULL: ParticlePotentialEnergies at positions k < nbound */
+  int32_t *iterations;  /* [n_sub] out: unbinding iterations (NumberUnbindingIterations) */
+  int32_t *status;      /* [n_sub] out: enum hbtg_sub_status */
+} hbtg_batch;
+
+/* Counters of the last call, for measurement. */
+typedef struct hbtg_stats
+{
+  int64_t n_sub;
+  int64_t n_particles;
+  int64_t total_bound;        /* sum of nbound */
+  int64_t global_iterations;  /* lock-step iterations of the batch */
+  int64_t interactions;       /* node/particle interactions evaluated by the tree walks (if counted) */
+  int64_t tree_nodes;         /* internal nodes built, summed over iterations */
+  double ms_total;            /* wall time of the device part of the last call (CUDA events) */
+  double ms_walk;             /* summed tree-walk kernel time (CUDA events) */
+  int64_t walk_launches;
+  int64_t kernel_launches;    /* kernels launched by the last call */
+  int64_t h2d_bytes, d2h_bytes;
+} hbtg_stats;
+
+typedef struct hbtg_handle hbtg_handle;
+
+/* Creates a handle bound to CUDA device `device`.  Checks that the device is
+ * compute capability 10.3.  Replaces nothing in the reference (its trees are
+ * stack objects, src/subhalo_unbind.cpp:517-518). */
+int hbtg_create(hbtg_handle **handle, int device);
+
+/* Frees the device arena and the handle. */
+int hbtg_destroy(hbtg_handle *handle);
+
+/* Unbinds every subhalo of `batch`; all pointers are HOST pointers.  Copies
+ * inputs to the device, runs, copies outputs back, synchronises.
+ * Replaces: Subhalo_t::Unbind (src/subhalo_unbind.cpp:463) for n_sub = 1, and
+ * the OpenMP loops of SubhaloSnapshot_t::RefineParticles
+ * (src/subhalo_unbind.cpp:888-903) for a batch. */
+int hbtg_unbind_batch(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch);
+
+/* Same as hbtg_unbind_batch but every array pointer in `batch` is a DEVICE
+ * pointer, except `offsets`, which is a host array; work is queued on
+ * `cuda_stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns after the stream is synchronised. */
+int hbtg_unbind_batch_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch, void *cuda_stream);
+
+/* Fills `stats` with the counters of the last call on this handle. */
+int hbtg_get_stats(const hbtg_handle *handle, hbtg_stats *stats);
+
+/* Enables (1) or disables (0) the interaction counter of the tree walk
+ * (slower; used to compute the roofline's algorithmic flops). */
+int hbtg_set_count_interactions(hbtg_handle *handle, int enable);
+
+/* Static description of a return code. */
+const char *hbtg_status_string(int status);
+
+/* Fills `params` with the reference defaults (src/config_parser.h:98-172)
+ * and a=1, Hz=0, G=43.0071 (src/config_parser.cpp:200 with default units). */
+void hbtg_default_params(hbtg_params *params);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HBT_UNBIND_GPU_H */

@@ -1,0 +1,234 @@
+/*
+ * ref_driver.cpp — TEST INFRASTRUCTURE (oracle).  Runs the reference's own,
+ * unmodified Subhalo_t::Unbind (src/subhalo_unbind.cpp:463-808) over a batch
+ * described by the library's C ABI (include/hbt_unbind_gpu.h), so that the
+ * reference itself can produce golden outputs and the CPU baseline.
+ *
+ * Built by oracle/build_oracle.py from the reference sources where they lie
+ * (no source is copied) into oracle/_ref/libref_{dmo,hydro}.so, against the
+ * single-rank stub headers in oracle/stub/.  Never linked into the product.
+ *
+ * The fake epoch follows the reference's own mocking idiom: a Snapshot_t
+ * subclass that only carries Cosmology (unit_tests/test_neighbour_search.cpp:13-60).
+ * Batching follows SubhaloSnapshot_t::RefineParticles (src/subhalo_unbind.cpp:888-903):
+ * an OpenMP dynamic,1 loop over subhaloes with nested parallelism off
+ * (HBT.cpp:26), so the per-particle loops inside Unbind run serially.
+ * inner_parallel=1 instead calls Unbind serially over subhaloes with its inner
+ * OpenMP loops enabled (the single-subhalo case).
+ */
+#include <cstdlib>
+#include <omp.h>
+#include <vector>
+
+#include "config_parser.h"
+#include "snapshot.h"
+#include "subhalo.h"
+
+#include "hbt_unbind_gpu.h"
+
+namespace
+{
+class EpochSnapshot_t : public Snapshot_t
+{
+  HBTxyz dummy{{0.f, 0.f, 0.f}};
+
+public:
+  EpochSnapshot_t(double a, double hz)
+  {
+    Cosmology.ScaleFactor = a;
+    Cosmology.Hz = hz;
+    Cosmology.OmegaM0 = 0.3;
+    Cosmology.OmegaLambda0 = 0.7;
+    SnapshotIndex = 1;
+    SnapshotId = 1;
+  }
+  HBTInt size() const override { return 0; }
+  const HBTxyz &GetComovingPosition(const HBTInt) const override { return dummy; }
+  const HBTxyz GetPhysicalVelocity(const HBTInt) const override { return dummy; }
+  HBTReal GetMass(const HBTInt) const override { return 0; }
+};
+
+void set_config(const hbtg_params *p, const hbtg_batch *b)
+{
+  HBTConfig.BoxSize = p->box_size;
+  HBTConfig.BoxHalf = HBTConfig.BoxSize / 2.;
+  HBTConfig.PeriodicBoundaryOn = p->periodic != 0;
+  HBTConfig.SofteningHalo = p->softening;
+  HBTConfig.MaxPhysicalSofteningHalo = -1;
+  HBTConfig.TreeNodeResolution = p->tree_node_resolution;
+  HBTConfig.TreeNodeResolutionHalf = HBTConfig.TreeNodeResolution / 2.;
+  HBTConfig.TreeNodeOpenAngle = p->open_angle;
+  HBTConfig.TreeNodeOpenAngleSquare = HBTConfig.TreeNodeOpenAngle * HBTConfig.TreeNodeOpenAngle;
+  HBTConfig.BoundMassPrecision = p->bound_mass_precision;
+  HBTConfig.MinNumPartOfSub = (int)p->min_num_part;
+  HBTConfig.MinNumTracerPartOfSub = (int)p->min_num_tracer;
+  HBTConfig.TracerParticleBitMask = p->tracer_type_mask;
+  HBTConfig.DoNotSubsampleParticleBitMask = p->no_subsample_mask;
+  HBTConfig.MaxSampleSizeOfPotentialEstimate = p->max_sample_size;
+  HBTConfig.RefineMostBoundParticle = p->refine_most_bound != 0;
+  HBTConfig.BoundFractionCenterRefinement = p->refine_fraction;
+  HBTConfig.PotentialEstimateUpscaleMassesPerType = p->upscale_per_type != 0;
+  HBTConfig.SubCoreSizeMin = p->sub_core_size_min;
+  HBTConfig.SubCoreSizeFactor = p->sub_core_size_factor;
+  HBTConfig.SaveBoundParticleBindingEnergies = b->energy != nullptr;
+  HBTConfig.SaveBoundParticlePotentialEnergies = b->potential != nullptr;
+  PhysicalConst::G = p->G;
+}
+
+void load_subhalo(const hbtg_params *p, const hbtg_batch *b, int64_t s, Subhalo_t &sub)
+{
+  const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+  sub.Particles.resize(n);
+  for (int64_t k = 0; k < n; k++)
+  {
+    Particle_t &q = sub.Particles[k];
+    const int64_t g = off + k;
+    q.Id = b->id[g];
+    for (int d = 0; d < 3; d++)
+    {
+      q.ComovingPosition[d] = b->pos[3 * g + d];
+      q.PhysicalVelocity[d] = b->vel[3 * g + d];
+    }
+    q.Mass = b->mass[g];
+#ifndef DM_ONLY
+#ifdef HAS_THERMAL_ENERGY
+    q.InternalEnergy = b->u ? b->u[g] : 0.f;
+#endif
+    q.Type = static_cast<ParticleType_t>(b->type ? b->type[g] : 1);
+#endif
+    q.HostId = k; /* carries the input index through the permutation */
+  }
+  sub.Nbound = n;
+  for (int d = 0; d < 3; d++)
+  {
+    sub.ComovingAveragePosition[d] = b->ref_pos[3 * s + d];
+    sub.PhysicalAverageVelocity[d] = b->ref_vel[3 * s + d];
+    sub.ComovingMostBoundPosition[d] = b->mostbound_pos[3 * s + d];
+    sub.PhysicalMostBoundVelocity[d] = b->mostbound_vel[3 * s + d];
+  }
+  sub.MostBoundParticleId = b->most_bound_id[s];
+  /* members the empty-subhalo early return leaves untouched start at zero */
+  sub.SpecificSelfPotentialEnergy = sub.SpecificSelfKineticEnergy = 0.f;
+  for (int d = 0; d < 3; d++)
+    sub.SpecificAngularMomentum[d] = 0.f;
+  sub.SnapshotOfBirth = 0;
+  sub.TrackId = s;
+}
+
+void store_subhalo(const hbtg_batch *b, int64_t s, Subhalo_t &sub)
+{
+  const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+  for (int64_t k = 0; k < n; k++)
+    b->order[off + k] = sub.Particles[k].HostId;
+  b->nbound[s] = sub.Nbound;
+  b->mbound[s] = sub.Mbound;
+#ifndef DM_ONLY
+  for (int t = 0; t < HBTG_TYPE_MAX; t++)
+  {
+    if (b->nbound_type)
+      b->nbound_type[HBTG_TYPE_MAX * s + t] = sub.NboundType[t];
+    if (b->mbound_type)
+      b->mbound_type[HBTG_TYPE_MAX * s + t] = sub.MboundType[t];
+  }
+#else
+  for (int t = 0; t < HBTG_TYPE_MAX; t++)
+  {
+    if (b->nbound_type)
+      b->nbound_type[HBTG_TYPE_MAX * s + t] = (t == 1) ? sub.Nbound : 0;
+    if (b->mbound_type)
+      b->mbound_type[HBTG_TYPE_MAX * s + t] = 0.f;
+  }
+#endif
+  b->tracer_index[s] = sub.TracerIndex;
+  b->most_bound_id[s] = sub.MostBoundParticleId;
+  for (int d = 0; d < 3; d++)
+  {
+    b->ref_pos[3 * s + d] = sub.ComovingAveragePosition[d];
+    b->ref_vel[3 * s + d] = sub.PhysicalAverageVelocity[d];
+    b->mostbound_pos[3 * s + d] = sub.ComovingMostBoundPosition[d];
+    b->mostbound_vel[3 * s + d] = sub.PhysicalMostBoundVelocity[d];
+  }
+  if (b->kinematics)
+  {
+    float *k = b->kinematics + HBTG_KIN_STRIDE * s;
+    k[0] = sub.SpecificSelfPotentialEnergy;
+    k[1] = sub.SpecificSelfKineticEnergy;
+    k[2] = sub.SpecificAngularMomentum[0];
+    k[3] = sub.SpecificAngularMomentum[1];
+    k[4] = sub.SpecificAngularMomentum[2];
+  }
+  if (b->core)
+  {
+    float *c = b->core + HBTG_CORE_STRIDE * s;
+    for (int d = 0; d < 3; d++)
+    {
+      c[d] = sub.CoreComovingPosition[d];
+      c[3 + d] = sub.CorePhysicalVelocity[d];
+    }
+    c[6] = sub.CoreComovingSigmaR;
+    c[7] = sub.CorePhysicalSigmaV;
+  }
+  if (b->energy)
+    for (int64_t k = 0; k < (int64_t)sub.ParticleBindingEnergies.size(); k++)
+      b->energy[off + k] = sub.ParticleBindingEnergies[k];
+  if (b->potential)
+    for (int64_t k = 0; k < (int64_t)sub.ParticlePotentialEnergies.size(); k++)
+      b->potential[off + k] = sub.ParticlePotentialEnergies[k];
+#ifdef MEASURE_UNBINDING_TIME
+  b->iterations[s] = sub.NumberUnbindingIterations;
+#else
+  b->iterations[s] = -1;
+#endif
+  if (n == 0)
+    b->status[s] = HBTG_SUB_EMPTY;
+  else if (sub.SnapshotOfDeath == 1)
+    b->status[s] = HBTG_SUB_DISRUPTED;
+  else
+    b->status[s] = HBTG_SUB_CONVERGED;
+}
+
+void unbind_one(const hbtg_params *p, hbtg_batch *b, const EpochSnapshot_t &epoch, int64_t s)
+{
+  Subhalo_t sub;
+  load_subhalo(p, b, s, sub);
+  sub.Unbind(epoch);
+  store_subhalo(b, s, sub);
+}
+} // namespace
+
+extern "C" int ref_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthreads, int inner_parallel)
+{
+  if (!p || !b || b->n_sub < 0)
+    return HBTG_ERR_INVALID;
+  set_config(p, b);
+  EpochSnapshot_t epoch(p->scale_factor, p->hubble);
+  srand48(p->seed);
+  if (nthreads <= 0)
+    nthreads = omp_get_max_threads();
+  if (inner_parallel)
+  {
+    omp_set_max_active_levels(1);
+    omp_set_num_threads(nthreads);
+    for (int64_t s = 0; s < b->n_sub; s++)
+      unbind_one(p, b, epoch, s);
+  }
+  else
+  {
+    omp_set_max_active_levels(1);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int64_t s = 0; s < b->n_sub; s++)
+      unbind_one(p, b, epoch, s);
+  }
+  return HBTG_OK;
+}
+
+extern "C" const char *ref_variant()
+{
+#ifdef DM_ONLY
+  return "reference Subhalo_t::Unbind, DM_ONLY";
+#elif defined(UNBIND_WITH_THERMAL_ENERGY)
+  return "reference Subhalo_t::Unbind, hydro, UNBIND_WITH_THERMAL_ENERGY";
+#else
+  return "reference Subhalo_t::Unbind, hydro";
+#endif
+}

@@ -1,0 +1,841 @@
+/*
+ * unbind_port.cpp — TEST INFRASTRUCTURE (oracle) and CPU baseline.
+ *
+ * The project's own CPU restatement of HBT-HERONS' iterative unbinding, used
+ * (a) as the checker of the GPU path in tests, smoke() and bench.py, and
+ * (b) as the timed CPU baseline on machines where the reference sources are
+ * absent.  It is NOT part of the product: libhbtg.so never calls it.
+ *
+ * It restates, with the same float/double rounding so that its results are
+ * bit-identical to the reference built with the same flags:
+ *   Subhalo_t::Unbind                     src/subhalo_unbind.cpp:463-808
+ *   EnergySnapshot_t (masses, CoM frame,  src/subhalo_unbind.cpp:46-393
+ *     AverageKinematics, GetPotentialEnergy)
+ *   RemoveUnboundParticles                src/subhalo_unbind.cpp:35-44
+ *   OctTree_t::Build                      src/oct_tree.tpp:12-142
+ *   GravityTree_t::UpdateInternalNodes    src/gravity_tree.cpp:18-80
+ *   GravityTree_t::EvaluatePotential      src/gravity_tree.cpp:82-166
+ *   GravityTree_t::BindingEnergy          src/gravity_tree.cpp:168-178
+ *   Snapshot_t::RelativeVelocity          src/snapshot.h:135-148
+ *   Subhalo_t::CountParticleTypes         src/subhalo.cpp:311-393
+ *   Subhalo_t::GetCorePhaseSpaceProperties src/subhalo_merge.cpp:94-181
+ * Potential subsampling (MaxSampleSizeOfPotentialEstimate > 0) is not
+ * restated; such calls return HBTG_ERR_UNSUPPORTED.
+ *
+ * Build with -ffp-contract=off (oracle/build_oracle.py) so that no multiply-
+ * add is fused: the reference is built the same way for comparison.
+ */
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstdlib>
+#include <omp.h>
+#include <vector>
+
+#include "hbt_unbind_gpu.h"
+
+namespace
+{
+
+/* HBTConfig values as the reference stores them (HBTReal = float). */
+struct Cfg
+{
+  float box, half;
+  bool periodic;
+  float soft;
+  float res, res_half;
+  float theta2;
+  float bmp;
+  int64_t min_part, min_tracer;
+  int tracer_mask, nosub_mask;
+  int64_t core_min;
+  float core_factor;
+  bool dm_only, thermal, want_energy, want_potential;
+  float G, a, hz;
+  int max_iter;
+};
+
+inline double wrap_d(double x, const Cfg &c)
+{
+  return x > (double)c.half ? x - (double)c.box : (x < -(double)c.half ? x + (double)c.box : x);
+}
+inline float wrap_f(float x, const Cfg &c)
+{
+  return x > c.half ? x - c.box : (x < -c.half ? x + c.box : x);
+}
+
+/* One particle of a subhalo, as the reference's Particle_t (src/snapshot.h:62-106). */
+struct Part
+{
+  int64_t id;
+  float x[3];
+  float v[3];
+  float m;
+  float u;
+  int type;
+  int64_t input_index;
+};
+
+struct Entry /* ParticleEnergy_t, src/subhalo_unbind.cpp:12-16 */
+{
+  float E;
+  int64_t p;
+};
+
+inline bool is_tracer(const Part &q, const Cfg &c) { return c.dm_only || (((1 << q.type) & c.tracer_mask) != 0); }
+
+/* RelativeVelocity (src/snapshot.h:135-148), all float. */
+inline void rel_vel(const float *x, const float *v, const float *rx, const float *rv, const Cfg &c, float *dv)
+{
+  const float hz_a = c.hz * c.a;
+  for (int j = 0; j < 3; j++)
+  {
+    float dx = x[j] - rx[j];
+    if (c.periodic)
+      dx = wrap_f(dx, c);
+    dv[j] = v[j] - rv[j];
+    dv[j] += hz_a * dx;
+  }
+}
+inline float norm2_f(const float *d) { return d[0] * d[0] + d[1] * d[1] + d[2] * d[2]; }
+
+/* ------------------------------------------------------------------------
+ * Octree with the reference's insertion build and threaded walk.
+ * Items 0..n-1 are the sources (particles), items >= n are cells.
+ * ---------------------------------------------------------------------- */
+class Tree
+{
+  struct Cell
+  {
+    int64_t son[8];
+    float s[3];
+    float len, mass;
+    int64_t sibling, nextnode;
+  };
+  std::vector<Cell> cells;
+  std::vector<int64_t> next_of;
+  const float *const *xs = nullptr; /* per source: pointer to float[3] */
+  const float *ms = nullptr;        /* per source mass */
+  int64_t n = 0;
+  const Cfg *cfg = nullptr;
+
+  Cell &cell(int64_t id) { return cells[id - n]; }
+
+  void finalize(int64_t no, int64_t sib, double len)
+  {
+    int64_t sons[8];
+    for (int j = 0; j < 8; j++)
+      sons[j] = cell(no).son[j];
+    cell(no).len = (float)len;
+    cell(no).sibling = sib;
+    int first = 0;
+    while (sons[first] < 0)
+      first++;
+    cell(no).nextnode = sons[first];
+    double mass = 0., com[3] = {0., 0., 0.};
+    for (int j = first; j < 8; j++)
+    {
+      const int64_t it = sons[j];
+      if (it < 0)
+        continue;
+      int64_t nxt = sib;
+      for (int k = j + 1; k < 8; k++)
+        if (sons[k] >= 0)
+        {
+          nxt = sons[k];
+          break;
+        }
+      if (it < n)
+      {
+        const double mm = ms[it];
+        mass += mm;
+        for (int d = 0; d < 3; d++)
+          com[d] += xs[it][d] * mm;
+        next_of[it] = nxt;
+      }
+      else
+      {
+        finalize(it, nxt, len >= (double)cfg->res ? len / 2. : len);
+        const double mm = cell(it).mass;
+        mass += mm;
+        for (int d = 0; d < 3; d++)
+          com[d] += cell(it).s[d] * mm;
+      }
+    }
+    cell(no).mass = (float)mass;
+    for (int d = 0; d < 3; d++)
+      cell(no).s[d] = (float)(com[d] / mass);
+  }
+
+public:
+  /* OctTree_t::Build (src/oct_tree.tpp:12-142) followed by
+   * UpdateInternalNodes (src/gravity_tree.cpp:50-80). */
+  void build(int64_t np, const float *const *x, const float *m, const Cfg &c)
+  {
+    n = np;
+    xs = x;
+    ms = m;
+    cfg = &c;
+    cells.clear();
+    cells.reserve(std::max<int64_t>(10, np));
+    next_of.assign(np, -1);
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++)
+      lo[d] = hi[d] = x[0][d];
+    for (int64_t i = 1; i < np; i++)
+      for (int d = 0; d < 3; d++)
+      {
+        const double v = x[i][d];
+        if (v > hi[d])
+          hi[d] = v;
+        else if (v < lo[d])
+          lo[d] = v;
+      }
+    double side = hi[0] - lo[0];
+    for (int d = 1; d < 3; d++)
+      if (hi[d] - lo[d] > side)
+        side = hi[d] - lo[d];
+    double centre0[3];
+    for (int d = 0; d < 3; d++)
+      centre0[d] = 0.5 * (hi[d] + lo[d]);
+    const double half0 = 0.5 * side;
+    auto new_cell = [&]() {
+      Cell cc;
+      for (int j = 0; j < 8; j++)
+        cc.son[j] = -1;
+      cells.push_back(cc);
+      return n + (int64_t)cells.size() - 1;
+    };
+    new_cell(); /* root = n */
+    for (int64_t i = 0; i < np; i++)
+    {
+      int64_t node = n;
+      double half = half0, ctr[3] = {centre0[0], centre0[1], centre0[2]};
+      for (;;)
+      {
+        half *= 0.5;
+        int sub = 0;
+        for (int d = 0; d < 3; d++)
+        {
+          if ((double)x[i][d] > ctr[d])
+          {
+            ctr[d] += half;
+            sub += 1 << d;
+          }
+          else
+            ctr[d] -= half;
+        }
+        const int64_t occ = cell(node).son[sub];
+        if (occ < 0)
+        {
+          cell(node).son[sub] = i;
+          break;
+        }
+        if (occ < n)
+        {
+          const int64_t fresh = new_cell();
+          cell(node).son[sub] = fresh;
+          node = fresh;
+          int sub2;
+          if (half < (double)c.res_half)
+          {
+            sub2 = (int)(8.0 * drand48());
+            if (sub2 >= 8)
+              sub2 = 7;
+          }
+          else
+          {
+            sub2 = 0;
+            for (int d = 0; d < 3; d++)
+              if ((double)x[occ][d] > ctr[d])
+                sub2 += 1 << d;
+          }
+          cell(node).son[sub2] = occ;
+        }
+        else
+          node = occ;
+      }
+    }
+    finalize(n, -1, side);
+  }
+
+  int64_t num_cells() const { return (int64_t)cells.size(); }
+
+  /* GravityTree_t::EvaluatePotential (src/gravity_tree.cpp:82-166). */
+  double potential(const float *tp, float target_mass, int64_t *interactions) const
+  {
+    const Cfg &c = *cfg;
+    const double h = 2.8 * (double)c.soft, h_inv = 1.0 / h;
+    double pot = (double)(target_mass / c.soft);
+    const double px = tp[0], py = tp[1], pz = tp[2];
+    int64_t no = n, count = 0;
+    while (no >= 0)
+    {
+      double dx, dy, dz, mass, r2;
+      if (no < n)
+      {
+        dx = xs[no][0] - px;
+        dy = xs[no][1] - py;
+        dz = xs[no][2] - pz;
+        if (c.periodic)
+        {
+          dx = wrap_d(dx, c);
+          dy = wrap_d(dy, c);
+          dz = wrap_d(dz, c);
+        }
+        mass = ms[no];
+        no = next_of[no];
+        r2 = dx * dx + dy * dy + dz * dz;
+      }
+      else
+      {
+        const Cell &q = cells[no - n];
+        dx = q.s[0] - px;
+        dy = q.s[1] - py;
+        dz = q.s[2] - pz;
+        if (c.periodic)
+        {
+          dx = wrap_d(dx, c);
+          dy = wrap_d(dy, c);
+          dz = wrap_d(dz, c);
+        }
+        mass = q.mass;
+        r2 = dx * dx + dy * dy + dz * dz;
+        const float len2 = q.len * q.len;
+        if ((double)len2 > r2 * (double)c.theta2)
+        {
+          no = q.nextnode;
+          continue;
+        }
+        no = q.sibling;
+      }
+      count++;
+      const double r = std::sqrt(r2);
+      if (r >= h)
+        pot -= mass / r;
+      else
+      {
+        const double u = r * h_inv;
+        double wp;
+        if (u < 0.5)
+          wp = -2.8 + u * u * (5.333333333333 + u * u * (6.4 * u - 9.6));
+        else
+          wp = -3.2 + 0.066666666667 / u + u * u * (10.666666666667 + u * (-16.0 + u * (9.6 - 2.133333333333 * u)));
+        pot += mass * h_inv * wp;
+      }
+    }
+    if (interactions)
+      *interactions += count;
+    return pot * (double)c.G / (double)c.a;
+  }
+};
+
+std::atomic<int64_t> g_interactions{0};
+std::atomic<int64_t> g_cells{0};
+
+/* Subhalo_t::Unbind restated for one subhalo of the batch. */
+void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_parallel)
+{
+  const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+  float ref_pos[3], ref_vel[3], mb_pos[3], mb_vel[3];
+  for (int d = 0; d < 3; d++)
+  {
+    ref_pos[d] = b->ref_pos[3 * s + d];
+    ref_vel[d] = b->ref_vel[3 * s + d];
+    mb_pos[d] = b->mostbound_pos[3 * s + d];
+    mb_vel[d] = b->mostbound_vel[3 * s + d];
+  }
+  int64_t most_bound_id = b->most_bound_id[s];
+  int64_t nbound = 0, nbound_type[HBTG_TYPE_MAX] = {0};
+  float mbound = 0.f, mbound_type[HBTG_TYPE_MAX] = {0.f};
+  int64_t tracer_index = 0;
+  float kin[HBTG_KIN_STRIDE] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float core[HBTG_CORE_STRIDE] = {0.f};
+  int iterations = 0;
+  int status = HBTG_SUB_CONVERGED;
+
+  std::vector<Part> P(n);
+  for (int64_t k = 0; k < n; k++)
+  {
+    const int64_t g = off + k;
+    Part &q = P[k];
+    q.id = b->id[g];
+    for (int d = 0; d < 3; d++)
+    {
+      q.x[d] = b->pos[3 * g + d];
+      q.v[d] = b->vel[3 * g + d];
+    }
+    q.m = b->mass[g];
+    q.u = (c.thermal && b->u) ? b->u[g] : 0.f;
+    q.type = c.dm_only ? 1 : (b->type ? b->type[g] : 1);
+    q.input_index = k;
+  }
+
+  auto finish_core = [&](int64_t nb) {
+    /* GetCorePhaseSpaceProperties (src/subhalo_merge.cpp:94-181) */
+    if (nb == 0)
+    {
+      for (int d = 0; d < 3; d++)
+      {
+        core[d] = mb_pos[d];
+        core[3 + d] = mb_vel[d];
+      }
+      core[6] = core[7] = 0.f;
+      return;
+    }
+    int64_t used = 0;
+    double msum = 0, ps[3] = {0, 0, 0}, ps2[3] = {0, 0, 0}, vs[3] = {0, 0, 0}, vs2[3] = {0, 0, 0};
+    const int64_t core_size = std::max((int64_t)((float)nb * c.core_factor), c.core_min);
+    double origin[3] = {0, 0, 0};
+    if (c.periodic)
+      for (int d = 0; d < 3; d++)
+        origin[d] = P[0].x[d];
+    for (int pass = 0; pass < 2 && used != core_size; pass++)
+    {
+      for (int i = 0; i < (int)nb; i++)
+      {
+        const bool t = is_tracer(P[i], c);
+        if ((t && pass == 0) || (!t && pass == 1))
+        {
+          used++;
+          const float m = P[i].m;
+          msum += m;
+          for (int d = 0; d < 3; d++)
+          {
+            double dx = P[i].x[d];
+            if (c.periodic)
+              dx = wrap_d(dx - origin[d], c);
+            ps[d] += m * dx;
+            ps2[d] += m * dx * dx;
+            const double dv = P[i].v[d];
+            vs[d] += m * dv;
+            vs2[d] += m * dv * dv;
+          }
+        }
+        if (used == core_size)
+          break;
+      }
+    }
+    for (int d = 0; d < 3; d++)
+    {
+      ps[d] /= msum;
+      ps2[d] /= msum;
+      float cp = (float)ps[d];
+      if (c.periodic)
+        cp += origin[d];
+      core[d] = cp;
+      ps2[d] -= ps[d] * ps[d];
+      vs[d] /= msum;
+      vs2[d] /= msum;
+      core[3 + d] = (float)vs[d];
+      vs2[d] -= vs[d] * vs[d];
+    }
+    core[6] = (float)std::sqrt(ps2[0] + ps2[1] + ps2[2]);
+    core[7] = (float)std::sqrt(vs2[0] + vs2[1] + vs2[2]);
+  };
+
+  std::vector<Entry> E(n);
+  int64_t interactions = 0;
+
+  if (n == 0)
+  {
+    status = HBTG_SUB_EMPTY;
+    tracer_index = -1; /* the reference returns before SetTracerIndex (src/subhalo_unbind.cpp:472-489) */
+    finish_core(0);
+  }
+  else
+  {
+    for (int64_t i = 0; i < n; i++)
+      E[i].p = i;
+    nbound = n;
+    int64_t nlast = n;
+    bool correction = false;
+    float old_pos[3] = {0, 0, 0}, old_vel[3] = {0, 0, 0};
+    Tree tree;
+    std::vector<const float *> src_x;
+    std::vector<float> src_m;
+    auto gather_sources = [&](int64_t first, int64_t count) {
+      src_x.resize(count);
+      src_m.resize(count);
+      for (int64_t i = 0; i < count; i++)
+      {
+        src_x[i] = P[E[first + i].p].x;
+        src_m[i] = P[E[first + i].p].m;
+      }
+    };
+    for (;;)
+    {
+      iterations++;
+      if (correction)
+      {
+        float dV[3];
+        rel_vel(old_pos, old_vel, ref_pos, ref_vel, c, dV);
+        const float dK = (float)(0.5 * norm2_f(dV));
+        gather_sources(nbound, nlast - nbound);
+        tree.build(nlast - nbound, src_x.data(), src_m.data(), c);
+        g_cells += tree.num_cells();
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : interactions) if (inner_parallel)
+        for (int64_t i = 0; i < nbound; i++)
+        {
+          const Part &q = P[E[i].p];
+          float ov[3];
+          rel_vel(q.x, q.v, old_pos, old_vel, c, ov);
+          const float dot = ov[0] * dV[0] + ov[1] * dV[1] + ov[2] * dV[2];
+          const double phi = tree.potential(q.x, 0.f, &interactions);
+          E[i].E = (float)((double)E[i].E + ((double)(dot + dK) - phi));
+        }
+        nlast = nbound;
+      }
+      else
+      {
+        nlast = nbound;
+        gather_sources(0, nlast);
+        tree.build(nlast, src_x.data(), src_m.data(), c);
+        g_cells += tree.num_cells();
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : interactions) if (inner_parallel)
+        for (int64_t i = 0; i < nlast; i++)
+        {
+          const Part &q = P[E[i].p];
+          const double phi = tree.potential(q.x, q.m, &interactions);
+          float dv[3];
+          rel_vel(q.x, q.v, ref_pos, ref_vel, c, dv);
+          float e = (float)((double)norm2_f(dv) * 0.5 + phi);
+          if (c.thermal)
+            e += q.u;
+          E[i].E = e;
+        }
+      }
+      /* RemoveUnboundParticles: stable partition on E < 0 */
+      {
+        std::vector<Entry> tmp;
+        tmp.reserve(nlast);
+        for (int64_t i = 0; i < nlast; i++)
+          if (E[i].E < 0)
+            tmp.push_back(E[i]);
+        const int64_t nb = (int64_t)tmp.size();
+        for (int64_t i = 0; i < nlast; i++)
+          if (!(E[i].E < 0))
+            tmp.push_back(E[i]);
+        std::copy(tmp.begin(), tmp.end(), E.begin());
+        nbound = nb;
+      }
+      int64_t tracers = 0;
+      if (c.dm_only)
+        tracers = nbound;
+      else
+        for (int64_t i = 0; i < nbound; i++)
+        {
+          if (is_tracer(P[E[i].p], c))
+            tracers++;
+          if (tracers >= c.min_tracer)
+            break;
+        }
+      if (nbound < c.min_part || tracers < c.min_tracer)
+      {
+        for (int d = 0; d < 3; d++)
+        {
+          ref_pos[d] = mb_pos[d];
+          ref_vel[d] = mb_vel[d];
+        }
+        nbound = 0;
+        mbound = 0.f;
+        status = HBTG_SUB_DISRUPTED;
+        break;
+      }
+      std::sort(E.begin() + nbound, E.begin() + nlast, [](const Entry &a, const Entry &q) { return a.E < q.E; });
+      const int64_t ndiff = nlast - nbound;
+      if (ndiff < nbound)
+      {
+        correction = true;
+        for (int d = 0; d < 3; d++)
+        {
+          old_pos[d] = ref_pos[d];
+          old_vel[d] = ref_vel[d];
+        }
+      }
+      /* CentreOfMassReferenceFrame (src/subhalo_unbind.cpp:151-198) */
+      {
+        double M = 0, wx[3] = {0, 0, 0}, wv[3] = {0, 0, 0}, origin[3] = {0, 0, 0};
+        if (c.periodic)
+          for (int d = 0; d < 3; d++)
+            origin[d] = P[E[0].p].x[d];
+        for (int64_t i = 0; i < nbound; i++)
+        {
+          const Part &q = P[E[i].p];
+          const float m = q.m;
+          M += m;
+          for (int d = 0; d < 3; d++)
+          {
+            wx[d] += c.periodic ? wrap_d(q.x[d] - origin[d], c) * m : (double)(q.x[d] * m);
+            wv[d] += q.v[d] * m;
+          }
+        }
+        for (int d = 0; d < 3; d++)
+        {
+          wx[d] /= M;
+          wv[d] /= M;
+        }
+        if (c.periodic)
+          for (int d = 0; d < 3; d++)
+            wx[d] += origin[d];
+        for (int d = 0; d < 3; d++)
+        {
+          ref_pos[d] = (float)wx[d];
+          ref_vel[d] = (float)wv[d];
+        }
+        mbound = (float)M;
+      }
+      if ((float)nbound >= (float)nlast * c.bmp)
+      {
+        std::sort(E.begin(), E.begin() + nbound, [](const Entry &a, const Entry &q) { return a.E < q.E; });
+        std::vector<Part> Q(n);
+        for (int64_t i = 0; i < n; i++)
+        {
+          Q[i] = P[E[i].p];
+          E[i].p = i;
+        }
+        P.swap(Q);
+        for (int d = 0; d < 3; d++)
+        {
+          mb_pos[d] = P[0].x[d];
+          mb_vel[d] = P[0].v[d];
+        }
+        break;
+      }
+      if (iterations >= c.max_iter)
+      {
+        status = HBTG_SUB_MAX_ITER;
+        break;
+      }
+    }
+    /* AverageKinematics (src/subhalo_unbind.cpp:200-249) */
+    if (nbound > 1)
+    {
+      double Et = 0, K = 0, L0 = 0, L1 = 0, L2 = 0, M = 0;
+      for (int64_t i = 0; i < nbound; i++)
+      {
+        const Part &q = P[E[i].p];
+        const float m = q.m;
+        Et += E[i].E * m;
+        if (c.thermal)
+          Et -= q.u * m;
+        double dx[3], dv[3];
+        for (int j = 0; j < 3; j++)
+        {
+          dx[j] = q.x[j] - ref_pos[j];
+          if (c.periodic)
+            dx[j] = wrap_d(dx[j], c);
+          dx[j] *= c.a;
+          dv[j] = q.v[j] - ref_vel[j] + c.hz * dx[j];
+          K += dv[j] * dv[j] * m;
+        }
+        L0 += (dx[1] * dv[2] - dx[2] * dv[1]) * m;
+        L1 += (dx[2] * dv[0] - dx[0] * dv[2]) * m;
+        L2 += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
+        M += m;
+      }
+      Et /= M;
+      K *= 0.5 / M;
+      kin[0] = (float)(Et - K);
+      kin[1] = (float)K;
+      kin[2] = (float)(L0 / M);
+      kin[3] = (float)(L1 / M);
+      kin[4] = (float)(L2 / M);
+    }
+    /* CountParticleTypes (src/subhalo.cpp:311-393) */
+    int64_t first_tracer = -1;
+    for (int64_t i = 0; i < nbound; i++)
+    {
+      const Part &q = P[i];
+      nbound_type[q.type]++;
+      mbound_type[q.type] += q.m;
+      if (first_tracer < 0 && is_tracer(q, c))
+        first_tracer = i;
+    }
+    tracer_index = (c.dm_only || first_tracer < 0) ? 0 : first_tracer;
+    if (status == HBTG_SUB_CONVERGED || status == HBTG_SUB_MAX_ITER)
+      most_bound_id = P[tracer_index].id;
+    finish_core(nbound);
+  }
+
+  /* outputs */
+  for (int64_t k = 0; k < n; k++)
+    b->order[off + k] = P[k].input_index;
+  b->nbound[s] = nbound;
+  b->mbound[s] = mbound;
+  for (int t = 0; t < HBTG_TYPE_MAX; t++)
+  {
+    if (b->nbound_type)
+      b->nbound_type[HBTG_TYPE_MAX * s + t] = nbound_type[t];
+    if (b->mbound_type)
+      b->mbound_type[HBTG_TYPE_MAX * s + t] = c.dm_only ? 0.f : mbound_type[t];
+  }
+  b->tracer_index[s] = tracer_index;
+  b->most_bound_id[s] = most_bound_id;
+  for (int d = 0; d < 3; d++)
+  {
+    b->ref_pos[3 * s + d] = ref_pos[d];
+    b->ref_vel[3 * s + d] = ref_vel[d];
+    b->mostbound_pos[3 * s + d] = mb_pos[d];
+    b->mostbound_vel[3 * s + d] = mb_vel[d];
+  }
+  if (b->kinematics)
+    for (int j = 0; j < HBTG_KIN_STRIDE; j++)
+      b->kinematics[HBTG_KIN_STRIDE * s + j] = kin[j];
+  if (b->core)
+    for (int j = 0; j < HBTG_CORE_STRIDE; j++)
+      b->core[HBTG_CORE_STRIDE * s + j] = core[j];
+  if (b->energy)
+    for (int64_t k = 0; k < nbound; k++)
+      b->energy[off + k] = E[k].E;
+  if (b->potential)
+    for (int64_t k = 0; k < nbound; k++)
+    {
+      /* GetPotentialEnergy (src/subhalo_unbind.cpp:114-135) */
+      const Part &q = P[k];
+      float e = E[k].E;
+      if (c.thermal)
+        e -= q.u;
+      for (int j = 0; j < 3; j++)
+      {
+        double dx = q.x[j] - ref_pos[j];
+        if (c.periodic)
+          dx = wrap_d(dx, c);
+        dx *= c.a;
+        const double dv = q.v[j] - ref_vel[j] + c.hz * dx;
+        e -= 0.5 * dv * dv;
+      }
+      b->potential[off + k] = e;
+    }
+  b->iterations[s] = iterations;
+  b->status[s] = status;
+  g_interactions += interactions;
+}
+
+Cfg make_cfg(const hbtg_params *p, const hbtg_batch *b)
+{
+  Cfg c;
+  c.box = (float)p->box_size;
+  c.half = (float)((double)c.box / 2.);
+  c.periodic = p->periodic != 0;
+  c.soft = (float)p->softening;
+  c.res = (float)p->tree_node_resolution;
+  c.res_half = (float)((double)c.res / 2.);
+  const float theta = (float)p->open_angle;
+  c.theta2 = theta * theta;
+  c.bmp = (float)p->bound_mass_precision;
+  c.min_part = (int)p->min_num_part;
+  c.min_tracer = (int)p->min_num_tracer;
+  c.tracer_mask = p->tracer_type_mask;
+  c.nosub_mask = p->no_subsample_mask;
+  c.core_min = p->sub_core_size_min;
+  c.core_factor = (float)p->sub_core_size_factor;
+  c.dm_only = p->dm_only != 0;
+  c.thermal = p->thermal != 0;
+  c.want_energy = b && b->energy;
+  c.want_potential = b && b->potential;
+  c.G = (float)p->G;
+  c.a = (float)p->scale_factor;
+  c.hz = (float)p->hubble;
+  c.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
+  return c;
+}
+
+} // namespace
+
+/* Batch entry with the library's contract.  nthreads <= 0 = all cores.
+ * inner_parallel = 0: OpenMP dynamic,1 over subhaloes (RefineParticles);
+ * inner_parallel = 1: subhaloes in turn, the energy loops parallel inside. */
+extern "C" int oracle_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthreads, int inner_parallel)
+{
+  if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
+    return HBTG_ERR_INVALID;
+  if (p->max_sample_size > 0)
+    return HBTG_ERR_UNSUPPORTED;
+  for (int64_t s = 0; s < b->n_sub; s++)
+    if (b->offsets[s + 1] < b->offsets[s])
+      return HBTG_ERR_INVALID;
+  const Cfg c = make_cfg(p, b);
+  srand48(p->seed);
+  g_interactions = 0;
+  g_cells = 0;
+  if (nthreads <= 0)
+    nthreads = omp_get_max_threads();
+  if (inner_parallel)
+  {
+    omp_set_num_threads(nthreads);
+    for (int64_t s = 0; s < b->n_sub; s++)
+      unbind_one(c, b, s, true);
+  }
+  else
+  {
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int64_t s = 0; s < b->n_sub; s++)
+      unbind_one(c, b, s, false);
+  }
+  return HBTG_OK;
+}
+
+/* Interactions (accepted nodes + particles) evaluated by the last batch. */
+extern "C" int64_t oracle_last_interactions() { return g_interactions.load(); }
+extern "C" int64_t oracle_last_cells() { return g_cells.load(); }
+
+/* Tree potential of `ns` sources at `nt` targets (specific, times G/a, as
+ * EvaluatePotential).  target_mass may be NULL (no self term removed). */
+extern "C" int oracle_tree_potential(const hbtg_params *p, int64_t ns, const float *src_pos, const float *src_mass,
+                                     int64_t nt, const float *tgt_pos, const float *tgt_mass, double *out)
+{
+  if (ns <= 0)
+    return HBTG_ERR_INVALID;
+  const Cfg c = make_cfg(p, nullptr);
+  std::vector<const float *> xs(ns);
+  for (int64_t i = 0; i < ns; i++)
+    xs[i] = src_pos + 3 * i;
+  Tree t;
+  srand48(p->seed);
+  t.build(ns, xs.data(), src_mass, c);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < nt; i++)
+    out[i] = t.potential(tgt_pos + 3 * i, tgt_mass ? tgt_mass[i] : 0.f, nullptr);
+  return HBTG_OK;
+}
+
+/* FP64 direct-sum potential with the same softening kernel and periodic
+ * wrap (no tree): the precision oracle for the FP32 walk. */
+extern "C" int oracle_direct_potential(const hbtg_params *p, int64_t ns, const float *src_pos, const float *src_mass,
+                                       int64_t nt, const float *tgt_pos, const float *tgt_mass, double *out)
+{
+  const Cfg c = make_cfg(p, nullptr);
+  const double h = 2.8 * (double)c.soft, h_inv = 1.0 / h;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t i = 0; i < nt; i++)
+  {
+    double pot = tgt_mass ? (double)(tgt_mass[i] / c.soft) : 0.0;
+    for (int64_t j = 0; j < ns; j++)
+    {
+      double d[3];
+      for (int k = 0; k < 3; k++)
+      {
+        d[k] = (double)src_pos[3 * j + k] - (double)tgt_pos[3 * i + k];
+        if (c.periodic)
+          d[k] = wrap_d(d[k], c);
+      }
+      const double r = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      const double m = src_mass[j];
+      if (r >= h)
+        pot -= m / r;
+      else
+      {
+        const double u = r * h_inv;
+        const double wp = u < 0.5 ? -2.8 + u * u * (5.333333333333 + u * u * (6.4 * u - 9.6))
+                                  : -3.2 + 0.066666666667 / u +
+                                      u * u * (10.666666666667 + u * (-16.0 + u * (9.6 - 2.133333333333 * u)));
+        pot += m * h_inv * wp;
+      }
+    }
+    out[i] = pot * (double)c.G / (double)c.a;
+  }
+  return HBTG_OK;
+}
