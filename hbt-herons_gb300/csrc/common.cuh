@@ -1,0 +1,71 @@
+// common.cuh - shared device types and helpers of the GB300 unbinding library.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hbtg
+{
+
+constexpr int kWarp = 32;
+
+// Float <-> order-preserving uint32 (used by min/max atomics and radix keys).
+__device__ __forceinline__ uint32_t float_to_ordered(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(uint32_t u)
+{
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Index of the segment holding packed item `idx`: the last s with off[s] <= idx,
+// for a non-decreasing offset array of n+1 entries.
+template <typename T>
+__device__ __forceinline__ int find_segment(const T *__restrict__ off, int n, T idx)
+{
+  int lo = 0, hi = n; // answer in [lo, hi)
+  while (hi - lo > 1)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= idx)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+// Reference NEAREST macro (src/config_parser.h:218-219) in float.
+__device__ __forceinline__ float nearest_f(float x, float half, float box)
+{
+  return x > half ? x - box : (x < -half ? x + box : x);
+}
+__device__ __forceinline__ double nearest_d(double x, double half, double box)
+{
+  return x > half ? x - box : (x < -half ? x + box : x);
+}
+
+// One node of a packed octree in depth-first preorder.  Leaves are the
+// particles themselves (crit = 0 so they are never opened).  A node's first
+// child is the next record; `skip` is the index just past its subtree.
+struct __align__(16) NodeRec
+{
+  float4 xyzm; // centre of mass and mass
+  float crit;  // open the node when r^2 < crit  (crit = len^2 / theta^2)
+  int skip;    // first record after this subtree
+  int pad0, pad1;
+};
+
+// Per-subhalo status while iterating.
+enum SubState : int
+{
+  kActive = 0,
+  kConverged = 1,
+  kDisrupted = 2,
+  kEmpty = 3,
+  kMaxIter = 4
+};
+
+} // namespace hbtg

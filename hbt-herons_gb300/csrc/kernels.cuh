@@ -1,0 +1,989 @@
+// kernels.cuh - device kernels of the batched unbinding iteration.
+//
+// Every subhalo of the batch is a segment of the particle arrays.  All
+// subhaloes that are still iterating advance together: each lock-step
+// iteration runs the same kernel sequence over the "active" segments, packed
+// by device-side exclusive scans of per-subhalo counts (src_off, chunk_off,
+// part_off, ...).  A packed item j is mapped back to its subhalo by a binary
+// search over the packed offsets.
+//
+// Reference correspondence (HBT-HERONS):
+//   k_bbox/k_root   bounding cube of the tree        src/oct_tree.tpp:27-47
+//   k_keys          insertion descent, as key digits src/oct_tree.tpp:52-92
+//   k_tree_*        octree + multipoles              src/oct_tree.tpp:52-136, src/gravity_tree.cpp:25-80
+//   k_walk          EvaluatePotential                src/gravity_tree.cpp:82-166
+//   k_energy        BindingEnergy + correction loop  src/gravity_tree.cpp:168-178, src/subhalo_unbind.cpp:563-621
+//   k_part_*        RemoveUnboundParticles           src/subhalo_unbind.cpp:35-44, 626
+//   k_after_part    tracer count, disruption, CorrectionLoop flag  src/subhalo_unbind.cpp:630-683
+//   k_com/k_control CentreOfMassReferenceFrame, convergence        src/subhalo_unbind.cpp:151-198, 687-690
+//   k_epilogue      AverageKinematics, CountParticleTypes, GetCorePhaseSpaceProperties,
+//                   binding/potential energies      src/subhalo_unbind.cpp:200-249,764-802,
+//                                                   src/subhalo.cpp:311-393, src/subhalo_merge.cpp:94-181
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "primitives.cuh"
+
+namespace hbtg
+{
+
+// Values of HBTConfig / Cosmology as the reference stores them (HBTReal = float).
+struct KParams
+{
+  float box, half;
+  int periodic;
+  float soft;     // GetCurrentSoftening(a)
+  float h, h_inv; // 2.8 * soft and its inverse (spline support)
+  float res;      // TreeNodeResolution
+  float theta2;   // TreeNodeOpenAngleSquare
+  float bmp;      // BoundMassPrecision
+  int min_part, min_tracer;
+  int tracer_mask;
+  int dm_only, thermal;
+  float G_over_a, a, hz;
+  int max_iter;
+  long long core_min;
+  float core_factor;
+  int count_interactions;
+};
+
+// Device views of the batch state.
+struct DevState
+{
+  int S;
+  long long N;
+  const long long *off; // [S+1]
+  // particles
+  float4 *pm; // x, y, z, mass
+  float4 *vu; // vx, vy, vz, internal energy
+  uint8_t *ty; // bits 0-2 type, bit 3 tracer
+  int *seg_of; // subhalo of each particle
+  int *ord, *ord_tmp; // current energy order: global particle index at each position
+  float *Ep;  // binding energy per particle
+  float *pot; // tree potential per particle (G/a applied)
+  const long long *id;
+  // subhaloes
+  int *n_s, *nbound, *nlast, *state, *corr, *iter, *wrap, *tracers, *nb_new;
+  float *ref_pos, *ref_vel, *old_pos, *old_vel, *mb_pos, *mb_vel, *mbound;
+  long long *mb_id;
+  // per-iteration plan
+  int *src_begin, *src_cnt, *src_off, *tgt_cnt, *chunk_cnt, *chunk_off, *part_cnt, *part_off;
+  int *tail_cnt, *tail_off, *fin_cnt, *fin_off;
+  unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
+  double *root;            // [4S] centre xyz, side length
+  double *com;             // [7S] M, sum m dx, sum m v
+  // packed arrays
+  unsigned long long *key, *key_alt;
+  uint32_t *val, *val_alt, *k32, *k32_alt;
+  int *cnt, *X, *flags, *F;
+  D4 *P;
+  NodeRec *nodes;
+  unsigned long long *interactions;
+};
+
+__device__ __forceinline__ int lcp_levels(unsigned long long a, unsigned long long b)
+{
+  // keys hold 21 levels of 3 bits in bits 62..0; bit 63 is zero
+  return (a == b) ? 21 : (__clzll(a ^ b) - 1) / 3;
+}
+
+__device__ __forceinline__ bool is_tracer_bits(uint8_t t) { return (t & 8u) != 0; }
+
+// ---------------------------------------------------------------------------
+// Set-up
+// ---------------------------------------------------------------------------
+__global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, const float *__restrict__ vel,
+                         const float *__restrict__ mass, const float *__restrict__ u, const uint8_t *__restrict__ type)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
+  {
+    D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
+    D.vu[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], (K.thermal && u) ? u[i] : 0.f);
+    int t = K.dm_only ? 1 : (type ? (int)type[i] : 1);
+    t = t < 0 ? 0 : (t > 5 ? 5 : t);
+    const bool tr = K.dm_only || ((1 << t) & K.tracer_mask);
+    D.ty[i] = (uint8_t)(t | (tr ? 8 : 0));
+    const int s = find_segment<long long>(D.off, D.S, i);
+    D.seg_of[i] = s;
+    D.ord[i] = (int)i;
+  }
+}
+
+__global__ void k_init_subs(DevState D)
+{
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < D.S; s += gridDim.x * blockDim.x)
+  {
+    const int n = (int)(D.off[s + 1] - D.off[s]);
+    D.n_s[s] = n;
+    D.nbound[s] = n;
+    D.nlast[s] = n;
+    D.state[s] = n > 0 ? kActive : kEmpty;
+    D.corr[s] = 0;
+    D.iter[s] = 0;
+    D.wrap[s] = 0;
+    D.tracers[s] = 0;
+    D.mbound[s] = 0.f;
+  }
+}
+
+// Per-iteration plan: ranges of tree sources, walk targets and partition.
+__global__ void k_plan(DevState D)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > D.S)
+    return;
+  if (s == D.S)
+  { // trailing zero so that the exclusive scans yield the totals
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = 0;
+    return;
+  }
+  if (D.state[s] != kActive)
+  {
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tgt_cnt[s] = 0;
+    return;
+  }
+  D.iter[s] += 1;
+  int tgt;
+  if (!D.corr[s])
+  {
+    D.nlast[s] = D.nbound[s];
+    D.src_begin[s] = 0;
+    D.src_cnt[s] = D.nlast[s];
+    tgt = D.nlast[s];
+  }
+  else
+  {
+    D.src_begin[s] = D.nbound[s];
+    D.src_cnt[s] = D.nlast[s] - D.nbound[s];
+    tgt = D.nbound[s];
+    D.nlast[s] = D.nbound[s];
+  }
+  D.tgt_cnt[s] = tgt;
+  D.chunk_cnt[s] = (tgt + kWarp - 1) / kWarp;
+  D.part_cnt[s] = D.nlast[s];
+  D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
+  D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
+  D.tracers[s] = 0;
+}
+
+// ---------------------------------------------------------------------------
+// Tree build
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int src_particle(const DevState &D, int s, int j)
+{
+  const int k = D.src_begin[s] + (j - D.src_off[s]);
+  return D.ord[D.off[s] + k];
+}
+
+__global__ void k_bbox(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j < total;
+  const int s = valid ? find_segment<int>(D.src_off, D.S, j) : -1;
+  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  if (valid)
+  {
+    const float4 x = D.pm[src_particle(D, s, j)];
+    lo[0] = hi[0] = float_to_ordered(x.x);
+    lo[1] = hi[1] = float_to_ordered(x.y);
+    lo[2] = hi[2] = float_to_ordered(x.z);
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, s);
+  const int leader = __ffs(peers) - 1;
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+  {
+    lo[d] = __reduce_min_sync(peers, lo[d]);
+    hi[d] = __reduce_max_sync(peers, hi[d]);
+  }
+  if (valid && (int)(threadIdx.x & 31) == leader)
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      atomicMin(&D.bb_lo[3 * s + d], lo[d]);
+      atomicMax(&D.bb_hi[3 * s + d], hi[d]);
+    }
+}
+
+// Root cube (src/oct_tree.tpp:44-65): centre of the box, side = largest extent.
+__global__ void k_root(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || D.state[s] != kActive || D.src_cnt[s] == 0)
+    return;
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++)
+  {
+    lo[d] = ordered_to_float(D.bb_lo[3 * s + d]);
+    hi[d] = ordered_to_float(D.bb_hi[3 * s + d]);
+  }
+  double len = hi[0] - lo[0];
+  for (int d = 1; d < 3; d++)
+    if (hi[d] - lo[d] > len)
+      len = hi[d] - lo[d];
+  for (int d = 0; d < 3; d++)
+    D.root[4 * s + d] = 0.5 * (hi[d] + lo[d]);
+  D.root[4 * s + 3] = len;
+  if (D.iter[s] == 1 && !D.corr[s]) // first iteration: the sources are every particle
+    D.wrap[s] = K.periodic && (len > (double)K.half);
+}
+
+// The reference inserts each particle by descending from the root cube,
+// halving the half-size and moving the centre by +-half per axis in double
+// (src/oct_tree.tpp:70-92).  The 3-bit child indices of that descent, root
+// first, form the key, so sorting by key orders particles as the reference
+// walk visits them.
+__device__ __forceinline__ unsigned long long descent_key(float4 x, const double *root)
+{
+  double c0 = root[0], c1 = root[1], c2 = root[2];
+  double half = 0.5 * root[3];
+  const double x0 = x.x, x1 = x.y, x2 = x.z;
+  unsigned long long key = 0;
+#pragma unroll 1
+  for (int l = 0; l < 21; l++)
+  {
+    half *= 0.5;
+    unsigned dgt = 0;
+    if (x0 > c0) { c0 += half; dgt |= 1u; } else c0 -= half;
+    if (x1 > c1) { c1 += half; dgt |= 2u; } else c1 -= half;
+    if (x2 > c2) { c2 += half; dgt |= 4u; } else c2 -= half;
+    key = (key << 3) | dgt;
+  }
+  return key;
+}
+
+__global__ void k_keys(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  const int p = src_particle(D, s, j);
+  D.key[j] = descent_key(D.pm[p], D.root + 4 * s);
+  D.val[j] = (uint32_t)p;
+}
+
+// After sorting on the key, a stable sort on the subhalo restores the packing.
+__global__ void k_segkeys(const uint32_t *__restrict__ val, const int *__restrict__ seg_of, uint32_t *__restrict__ k32,
+                          int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < total)
+    k32[j] = (uint32_t)seg_of[val[j]];
+}
+
+__global__ void k_keys_again(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int p = (int)D.val[j];
+  D.key[j] = descent_key(D.pm[p], D.root + 4 * D.seg_of[p]);
+}
+
+// Number of tree cells whose first particle (in key order) is item j:
+// levels lo..hi, where lo is one past the common prefix with the previous key
+// and hi the common prefix with the next key (a cell needs two particles).
+__device__ __forceinline__ void cell_levels(const DevState &D, int j, int i, int m, int &lo, int &hi)
+{
+  const unsigned long long k = D.key[j];
+  lo = (i == 0) ? 0 : lcp_levels(D.key[j - 1], k) + 1;
+  if (i == m - 1)
+    hi = (i == 0) ? 0 : -1; // a lone particle still gets the root cell
+  else
+    hi = lcp_levels(k, D.key[j + 1]);
+}
+
+__global__ void k_tree_count(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > total)
+    return;
+  if (j == total)
+  {
+    D.cnt[j] = 0;
+    return;
+  }
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  const int i = j - D.src_off[s], m = D.src_cnt[s];
+  int lo, hi;
+  cell_levels(D, j, i, m, lo, hi);
+  D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
+}
+
+// Double prefix sums of mass and mass-weighted offset from the root centre.
+__global__ void k_prefix_prep(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int p = (int)D.val[j];
+  const double *r = D.root + 4 * D.seg_of[p];
+  const float4 x = D.pm[p];
+  const double m = x.w;
+  D.P[j] = D4{m, m * ((double)x.x - r[0]), m * ((double)x.y - r[1]), m * ((double)x.z - r[2])};
+}
+
+// Writes the particle leaf and the cells that start at item j, in preorder.
+// Record index: leaf of item j = j + X[j] + cnt[j]; cell (j, level lo+t) =
+// j + X[j] + t.  A cell's subtree ends after the leaf of its last particle.
+__global__ void k_tree_emit(DevState D, KParams K, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  const int seg0 = D.src_off[s], i = j - seg0, m = D.src_cnt[s], seg_end = seg0 + m;
+  int lo, hi;
+  cell_levels(D, j, i, m, lo, hi);
+  const int c = hi >= lo ? hi - lo + 1 : 0;
+  const int base = j + D.X[j];
+  const int p = (int)D.val[j];
+  const float4 x = D.pm[p];
+  NodeRec leaf;
+  leaf.xyzm = x;
+  leaf.crit = 0.f;
+  leaf.skip = base + c + 1;
+  leaf.pad0 = leaf.pad1 = 0;
+  D.nodes[base + c] = leaf;
+  if (c == 0)
+    return;
+  const double *r = D.root + 4 * s;
+  const unsigned long long kj = D.key[j];
+  const D4 before = (j > 0) ? D.P[j - 1] : D4{0., 0., 0., 0.};
+  for (int t = 0; t < c; t++)
+  {
+    const int L = lo + t;
+    // last item whose first L digits equal those of item j
+    int b;
+    if (L == 0)
+      b = seg_end - 1;
+    else
+    {
+      const int shift = 63 - 3 * L;
+      const unsigned long long pref = kj >> shift;
+      int a = j, e = seg_end; // invariant: key[a] has the prefix; answer in [a, e)
+      while (e - a > 1)
+      {
+        const int mid = (a + e) >> 1;
+        if ((D.key[mid] >> shift) == pref)
+          a = mid;
+        else
+          e = mid;
+      }
+      b = a;
+    }
+    const D4 after = D.P[b];
+    const double mass = after.m - before.m;
+    // side length: halved per level while not below the resolution (src/gravity_tree.cpp:38-42)
+    double len = r[3];
+    for (int l = 0; l < L; l++)
+      len = (len >= (double)K.res) ? 0.5 * len : len;
+    const float lenf = (float)len;
+    const float len2 = lenf * lenf;
+    NodeRec nd;
+    nd.xyzm = make_float4((float)(r[0] + (after.x - before.x) / mass), (float)(r[1] + (after.y - before.y) / mass),
+                          (float)(r[2] + (after.z - before.z) / mass), (float)mass);
+    nd.crit = __fdiv_rn(len2, K.theta2);
+    nd.skip = b + D.X[b] + D.cnt[b] + 1;
+    nd.pad0 = nd.pad1 = 0;
+    D.nodes[base + t] = nd;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tree walk: one warp evaluates 32 targets of one subhalo.  The warp visits
+// nodes in preorder; each lane applies the reference opening test for its own
+// target.  A lane that accepts a node skips its subtree (it stays idle until
+// the warp reaches the node's skip index); the warp descends when any lane
+// opens, else jumps to the skip index.  FP32 with Kahan-compensated sums.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float spline_w(float u)
+{
+  // Gadget cubic-spline potential kernel, src/gravity_tree.cpp:154-160
+  return (u < 0.5f) ? -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f))
+                    : -3.2f + 0.066666666667f / u +
+                        u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
+}
+
+template <bool Wrap>
+__device__ __forceinline__ void walk_warp(const NodeRec *__restrict__ nodes, int root, float4 x, bool valid,
+                                          float self_mass, const KParams &K, float &out, unsigned long long &cnt)
+{
+  float sum = valid ? self_mass / K.soft : 0.f, comp = 0.f;
+  const int end = nodes[root].skip;
+  int idx = root, my_skip = valid ? root : 0x7fffffff;
+  const float h2 = K.h * K.h;
+  while (idx < end)
+  {
+    const float4 n = __ldg(&nodes[idx].xyzm);
+    const int2 cs = __ldg(reinterpret_cast<const int2 *>(&nodes[idx].crit));
+    const bool active = idx >= my_skip;
+    float dx = n.x - x.x, dy = n.y - x.y, dz = n.z - x.z;
+    if (Wrap)
+    {
+      dx = nearest_f(dx, K.half, K.box);
+      dy = nearest_f(dy, K.half, K.box);
+      dz = nearest_f(dz, K.half, K.box);
+    }
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const bool open = active && (r2 < __int_as_float(cs.x));
+    if (active && !open)
+    {
+      float term;
+      if (r2 >= h2)
+        term = -n.w * rsqrtf(r2);
+      else
+      {
+        const float r = sqrtf(r2);
+        term = n.w * K.h_inv * spline_w(r * K.h_inv);
+      }
+      const float y = term - comp;
+      const float t = sum + y;
+      comp = (t - sum) - y;
+      sum = t;
+      my_skip = cs.y;
+      cnt++;
+    }
+    idx = __any_sync(0xffffffffu, open) ? idx + 1 : max(cs.y, idx + 1); // strictly increasing
+  }
+  out = sum - comp;
+}
+
+__global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_chunks)
+{
+  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  unsigned long long cnt = 0;
+  for (int c = warp_global; c < total_chunks; c += nwarps)
+  {
+    const int s = find_segment<int>(D.chunk_off, D.S, c);
+    const int t = (c - D.chunk_off[s]) * kWarp + lane;
+    const bool valid = t < D.tgt_cnt[s];
+    const bool corr = D.corr[s] != 0;
+    int p = 0;
+    if (valid)
+      p = corr ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t];
+    const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int root = D.src_off[s] + D.X[D.src_off[s]];
+    float phi = 0.f;
+    if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
+      ;
+    else if (D.wrap[s])
+      walk_warp<true>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+    else
+      walk_warp<false>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+    if (valid)
+      D.pot[p] = phi * K.G_over_a;
+  }
+  if (K.count_interactions)
+  {
+    for (int o = 16; o > 0; o >>= 1)
+      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if (lane == 0)
+      atomicAdd(D.interactions, cnt);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Energies, partition, frame
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rel_vel(float3 x, float3 v, const float *rp, const float *rv, const KParams &K, float *dv)
+{
+  // Snapshot_t::RelativeVelocity (src/snapshot.h:135-148), float
+  const float hz_a = K.hz * K.a;
+  const float xs[3] = {x.x, x.y, x.z}, vs[3] = {v.x, v.y, v.z};
+  for (int d = 0; d < 3; d++)
+  {
+    float dx = __fsub_rn(xs[d], rp[d]);
+    if (K.periodic)
+      dx = nearest_f(dx, K.half, K.box);
+    dv[d] = __fadd_rn(__fsub_rn(vs[d], rv[d]), __fmul_rn(hz_a, dx));
+  }
+}
+__device__ __forceinline__ float norm2_rn(const float *d)
+{
+  return __fadd_rn(__fadd_rn(__fmul_rn(d[0], d[0]), __fmul_rn(d[1], d[1])), __fmul_rn(d[2], d[2]));
+}
+
+__global__ void k_energy(DevState D, KParams K, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  const int k = j - D.part_off[s];
+  const int p = D.ord[D.off[s] + k];
+  const float4 x = D.pm[p], v = D.vu[p];
+  const float3 x3 = make_float3(x.x, x.y, x.z), v3 = make_float3(v.x, v.y, v.z);
+  if (!D.corr[s])
+  {
+    float dv[3];
+    rel_vel(x3, v3, D.ref_pos + 3 * s, D.ref_vel + 3 * s, K, dv);
+    float e = __fadd_rn(__fmul_rn(0.5f, norm2_rn(dv)), D.pot[p]);
+    if (K.thermal)
+      e = __fadd_rn(e, v.w);
+    D.Ep[p] = e;
+  }
+  else
+  {
+    float dV[3], ov[3];
+    const float op[3] = {D.old_pos[3 * s], D.old_pos[3 * s + 1], D.old_pos[3 * s + 2]};
+    const float ovl[3] = {D.old_vel[3 * s], D.old_vel[3 * s + 1], D.old_vel[3 * s + 2]};
+    rel_vel(make_float3(op[0], op[1], op[2]), make_float3(ovl[0], ovl[1], ovl[2]), D.ref_pos + 3 * s,
+            D.ref_vel + 3 * s, K, dV);
+    const float dK = (float)(0.5 * (double)norm2_rn(dV));
+    rel_vel(x3, v3, op, ovl, K, ov);
+    const float dot = __fadd_rn(__fadd_rn(__fmul_rn(ov[0], dV[0]), __fmul_rn(ov[1], dV[1])), __fmul_rn(ov[2], dV[2]));
+    D.Ep[p] = __fadd_rn(D.Ep[p], __fsub_rn(__fadd_rn(dot, dK), D.pot[p]));
+  }
+}
+
+__global__ void k_part_flags(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > total)
+    return;
+  if (j == total)
+  {
+    D.flags[j] = 0;
+    return;
+  }
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  const int k = j - D.part_off[s];
+  D.flags[j] = D.Ep[D.ord[D.off[s] + k]] < 0.f ? 1 : 0;
+}
+
+__global__ void k_part_count(DevState D)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || D.part_cnt[s] == 0)
+    return;
+  D.nb_new[s] = D.F[D.part_off[s + 1]] - D.F[D.part_off[s]];
+}
+
+// Stable partition: bound particles first, each group in its previous order.
+__global__ void k_part_scatter(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j < total;
+  int s = -1, tracer = 0;
+  if (valid)
+  {
+    s = find_segment<int>(D.part_off, D.S, j);
+    const int k = j - D.part_off[s];
+    const int rb = D.F[j] - D.F[D.part_off[s]];
+    const bool bound = D.flags[j] != 0;
+    const int dest = bound ? rb : D.nb_new[s] + (k - rb);
+    const int p = D.ord[D.off[s] + k];
+    D.ord_tmp[D.off[s] + dest] = p;
+    tracer = (bound && is_tracer_bits(D.ty[p])) ? 1 : 0;
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, s);
+  const int tot = __reduce_add_sync(peers, tracer);
+  if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1 && tot)
+    atomicAdd(&D.tracers[s], tot);
+}
+
+__global__ void k_part_copy(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  const long long g = D.off[s] + (j - D.part_off[s]);
+  D.ord[g] = D.ord_tmp[g];
+}
+
+// Disruption test and CorrectionLoop flag (src/subhalo_unbind.cpp:630-683).
+__global__ void k_after_part(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > D.S)
+    return;
+  if (s == D.S)
+  {
+    D.tail_cnt[s] = 0;
+    return;
+  }
+  D.tail_cnt[s] = 0;
+  if (D.state[s] != kActive)
+    return;
+  const int nb = D.nb_new[s];
+  D.nbound[s] = nb;
+  const int tracers = K.dm_only ? nb : D.tracers[s];
+  if (nb < K.min_part || tracers < K.min_tracer)
+  {
+    for (int d = 0; d < 3; d++)
+    {
+      D.ref_pos[3 * s + d] = D.mb_pos[3 * s + d];
+      D.ref_vel[3 * s + d] = D.mb_vel[3 * s + d];
+    }
+    D.nbound[s] = 0;
+    D.mbound[s] = 0.f;
+    D.state[s] = kDisrupted;
+    return;
+  }
+  const int ndiff = D.nlast[s] - nb;
+  D.tail_cnt[s] = ndiff;
+  if (ndiff < nb)
+  {
+    D.corr[s] = 1;
+    for (int d = 0; d < 3; d++)
+    {
+      D.old_pos[3 * s + d] = D.ref_pos[3 * s + d];
+      D.old_vel[3 * s + d] = D.ref_vel[3 * s + d];
+    }
+  }
+  for (int q = 0; q < 7; q++)
+    D.com[7 * s + q] = 0.;
+}
+
+// Keys for sorting ranges by energy: ordered float, value = particle.
+// mode 0: the unbound tail [nbound, nbound + tail_cnt); mode 1: [0, nbound).
+__global__ void k_energy_keys(DevState D, const int *__restrict__ offs, int total, int mode)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(offs, D.S, j);
+  const int k = (mode == 0 ? D.nbound[s] : 0) + (j - offs[s]);
+  const int p = D.ord[D.off[s] + k];
+  D.k32[j] = float_to_ordered(D.Ep[p]);
+  D.val[j] = (uint32_t)p;
+}
+
+__global__ void k_energy_write(DevState D, const uint32_t *__restrict__ sorted_val, const int *__restrict__ offs,
+                               int total, int mode)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(offs, D.S, j);
+  const int k = (mode == 0 ? D.nbound[s] : 0) + (j - offs[s]);
+  D.ord[D.off[s] + k] = (int)sorted_val[j];
+}
+
+// FP64 centre-of-mass sums over the bound set, wrapped about its first particle.
+__global__ void k_com(DevState D, KParams K, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = j < total;
+  int s = -1;
+  double acc[7] = {0., 0., 0., 0., 0., 0., 0.};
+  if (valid)
+  {
+    s = find_segment<int>(D.fin_off, D.S, j);
+    const int k = j - D.fin_off[s];
+    const int p = D.ord[D.off[s] + k];
+    const float4 x = D.pm[p], v = D.vu[p];
+    const float4 o = D.pm[D.ord[D.off[s]]];
+    const float m = x.w;
+    acc[0] = m;
+    if (K.periodic)
+    {
+      acc[1] = nearest_d((double)x.x - (double)o.x, K.half, K.box) * m;
+      acc[2] = nearest_d((double)x.y - (double)o.y, K.half, K.box) * m;
+      acc[3] = nearest_d((double)x.z - (double)o.z, K.half, K.box) * m;
+    }
+    else
+    {
+      acc[1] = __fmul_rn(x.x, m);
+      acc[2] = __fmul_rn(x.y, m);
+      acc[3] = __fmul_rn(x.z, m);
+    }
+    acc[4] = __fmul_rn(v.x, m);
+    acc[5] = __fmul_rn(v.y, m);
+    acc[6] = __fmul_rn(v.z, m);
+  }
+  const unsigned peers = __match_any_sync(0xffffffffu, s);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  // segmented warp reduction: add values of higher peers into the leader
+#pragma unroll
+  for (int q = 0; q < 7; q++)
+  {
+    double v = acc[q];
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const double w = __shfl_down_sync(0xffffffffu, v, o);
+      const int src = lane + o;
+      if (src < 32 && ((peers >> src) & 1u))
+        v += w;
+    }
+    acc[q] = v;
+  }
+  if (valid && lane == leader)
+    for (int q = 0; q < 7; q++)
+      atomicAdd(&D.com[7 * s + q], acc[q]);
+}
+
+// New frame, bound mass and convergence test (src/subhalo_unbind.cpp:687-690).
+__global__ void k_control(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || D.state[s] != kActive)
+    return;
+  const double *c = D.com + 7 * s;
+  const double M = c[0];
+  const float4 o = D.pm[D.ord[D.off[s]]];
+  const double org[3] = {o.x, o.y, o.z};
+  for (int d = 0; d < 3; d++)
+  {
+    double px = c[1 + d] / M;
+    if (K.periodic)
+      px += org[d];
+    D.ref_pos[3 * s + d] = (float)px;
+    D.ref_vel[3 * s + d] = (float)(c[4 + d] / M);
+  }
+  D.mbound[s] = (float)M;
+  const int nb = D.nbound[s];
+  if ((float)nb >= __fmul_rn((float)D.nlast[s], K.bmp))
+    D.state[s] = kConverged;
+  else if (D.iter[s] >= K.max_iter)
+    D.state[s] = kMaxIter;
+}
+
+__global__ void k_plan_counts(DevState D, int mode)
+{
+  // mode 0: fin_cnt = nbound of active subhaloes (frame sums)
+  // mode 1: fin_cnt = nbound of converged / stopped subhaloes (final sort)
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > D.S)
+    return;
+  if (s == D.S)
+  {
+    D.fin_cnt[s] = 0;
+    return;
+  }
+  const int st = D.state[s];
+  const bool take = mode == 0 ? (st == kActive) : (st == kConverged || st == kMaxIter);
+  D.fin_cnt[s] = take ? D.nbound[s] : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Epilogue: one block per subhalo.
+// ---------------------------------------------------------------------------
+struct OutPtrs
+{
+  long long *order, *nbound, *nbound_type, *tracer_index, *most_bound_id;
+  float *mbound, *mbound_type, *kinematics, *core, *energy, *potential;
+  int *iterations, *status;
+};
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T *sh)
+{
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0)
+    sh[w] = v;
+  __syncthreads();
+  T t = 0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+      t += sh[i];
+  return t; // valid in thread 0
+}
+
+__global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs O)
+{
+  __shared__ double sh[8];
+  __shared__ int s_type_n[6];
+  __shared__ double s_type_m[6];
+  __shared__ int s_first_tracer;
+  for (int s = blockIdx.x; s < D.S; s += gridDim.x)
+  {
+    const int st = D.state[s];
+    const long long off = D.off[s];
+    const int n = D.n_s[s];
+    const int nb = (st == kConverged || st == kMaxIter) ? D.nbound[s] : 0;
+    if (threadIdx.x < 6)
+    {
+      s_type_n[threadIdx.x] = 0;
+      s_type_m[threadIdx.x] = 0.;
+    }
+    if (threadIdx.x == 0)
+      s_first_tracer = 0x7fffffff;
+    __syncthreads();
+    // order
+    for (int k = threadIdx.x; k < n; k += blockDim.x)
+      O.order[off + k] = (st == kConverged || st == kMaxIter) ? (long long)D.ord[off + k] - off : (long long)k;
+    // per-particle outputs and sums over the bound set
+    double Et = 0., Kk = 0., L0 = 0., L1 = 0., L2 = 0., Ms = 0.;
+    const float *rp = D.ref_pos + 3 * s, *rv = D.ref_vel + 3 * s;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x)
+    {
+      const int p = D.ord[off + k];
+      const float4 x = D.pm[p], v = D.vu[p];
+      const float e = D.Ep[p];
+      if (O.energy)
+        O.energy[off + k] = e;
+      const float m = x.w;
+      Et += (double)__fmul_rn(e, m);
+      if (K.thermal)
+        Et -= (double)__fmul_rn(v.w, m);
+      const float xs[3] = {x.x, x.y, x.z}, vs[3] = {v.x, v.y, v.z};
+      double dx[3], dv[3];
+      float pe = K.thermal ? __fsub_rn(e, v.w) : e;
+      for (int d = 0; d < 3; d++)
+      {
+        dx[d] = (double)__fsub_rn(xs[d], rp[d]);
+        if (K.periodic)
+          dx[d] = nearest_d(dx[d], K.half, K.box);
+        dx[d] *= (double)K.a;
+        dv[d] = (double)__fsub_rn(vs[d], rv[d]) + (double)K.hz * dx[d];
+        Kk += dv[d] * dv[d] * m;
+        pe = (float)((double)pe - 0.5 * dv[d] * dv[d]);
+      }
+      if (O.potential)
+        O.potential[off + k] = pe;
+      L0 += (dx[1] * dv[2] - dx[2] * dv[1]) * m;
+      L1 += (dx[2] * dv[0] - dx[0] * dv[2]) * m;
+      L2 += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
+      Ms += m;
+      const uint8_t t = D.ty[p];
+      atomicAdd(&s_type_n[t & 7], 1);
+      atomicAdd(&s_type_m[t & 7], (double)m);
+      if (is_tracer_bits(t))
+        atomicMin(&s_first_tracer, k);
+    }
+    Et = block_sum(Et, sh);
+    Kk = block_sum(Kk, sh);
+    L0 = block_sum(L0, sh);
+    L1 = block_sum(L1, sh);
+    L2 = block_sum(L2, sh);
+    Ms = block_sum(Ms, sh);
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      float kin[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (nb > 1)
+      {
+        Et /= Ms;
+        Kk *= 0.5 / Ms;
+        kin[0] = (float)(Et - Kk);
+        kin[1] = (float)Kk;
+        kin[2] = (float)(L0 / Ms);
+        kin[3] = (float)(L1 / Ms);
+        kin[4] = (float)(L2 / Ms);
+      }
+      if (O.kinematics)
+        for (int q = 0; q < 5; q++)
+          O.kinematics[5 * s + q] = kin[q];
+      for (int t = 0; t < 6; t++)
+      {
+        if (O.nbound_type)
+          O.nbound_type[6 * s + t] = s_type_n[t];
+        if (O.mbound_type)
+          O.mbound_type[6 * s + t] = K.dm_only ? 0.f : (float)s_type_m[t];
+      }
+      long long ti;
+      if (st == kEmpty)
+        ti = -1;
+      else if (nb == 0 || K.dm_only || s_first_tracer == 0x7fffffff)
+        ti = 0;
+      else
+        ti = s_first_tracer;
+      O.tracer_index[s] = ti;
+      O.nbound[s] = nb;
+      O.mbound[s] = (st == kConverged || st == kMaxIter) ? D.mbound[s] : 0.f;
+      O.iterations[s] = D.iter[s];
+      O.status[s] = st == kConverged ? 0 : st == kDisrupted ? 1 : st == kEmpty ? 2 : 3;
+      float *mbp = D.mb_pos + 3 * s, *mbv = D.mb_vel + 3 * s;
+      if (nb > 0)
+      {
+        const int p0 = D.ord[off];
+        const float4 x0 = D.pm[p0], v0 = D.vu[p0];
+        mbp[0] = x0.x;
+        mbp[1] = x0.y;
+        mbp[2] = x0.z;
+        mbv[0] = v0.x;
+        mbv[1] = v0.y;
+        mbv[2] = v0.z;
+        O.most_bound_id[s] = D.id[D.ord[off + ti]];
+      }
+      if (O.core)
+      {
+        float *cr = O.core + 8 * s;
+        if (nb == 0)
+        {
+          for (int d = 0; d < 3; d++)
+          {
+            cr[d] = mbp[d];
+            cr[3 + d] = mbv[d];
+          }
+          cr[6] = cr[7] = 0.f;
+        }
+        else
+        {
+          // GetCorePhaseSpaceProperties: first CoreSize tracers, then non-tracers
+          const long long core_size =
+            max((long long)((float)nb * K.core_factor), K.core_min);
+          long long used = 0;
+          double msum = 0., ps[3] = {0., 0., 0.}, ps2[3] = {0., 0., 0.}, vs[3] = {0., 0., 0.},
+                 vs2[3] = {0., 0., 0.}, org[3] = {0., 0., 0.};
+          const float4 x0 = D.pm[D.ord[off]];
+          if (K.periodic)
+          {
+            org[0] = x0.x;
+            org[1] = x0.y;
+            org[2] = x0.z;
+          }
+          for (int pass = 0; pass < 2 && used != core_size; pass++)
+            for (int i = 0; i < nb; i++)
+            {
+              const int p = D.ord[off + i];
+              const bool tr = is_tracer_bits(D.ty[p]);
+              if ((tr && pass == 0) || (!tr && pass == 1))
+              {
+                used++;
+                const float4 x = D.pm[p], v = D.vu[p];
+                const float m = x.w;
+                msum += m;
+                const float xs[3] = {x.x, x.y, x.z}, vv[3] = {v.x, v.y, v.z};
+                for (int d = 0; d < 3; d++)
+                {
+                  double dx = xs[d];
+                  if (K.periodic)
+                    dx = nearest_d(dx - org[d], K.half, K.box);
+                  ps[d] += m * dx;
+                  ps2[d] += m * dx * dx;
+                  const double dvv = vv[d];
+                  vs[d] += m * dvv;
+                  vs2[d] += m * dvv * dvv;
+                }
+              }
+              if (used == core_size)
+                break;
+            }
+          for (int d = 0; d < 3; d++)
+          {
+            ps[d] /= msum;
+            ps2[d] /= msum;
+            float cp = (float)ps[d];
+            if (K.periodic)
+              cp = (float)((double)cp + org[d]);
+            cr[d] = cp;
+            ps2[d] -= ps[d] * ps[d];
+            vs[d] /= msum;
+            vs2[d] /= msum;
+            cr[3 + d] = (float)vs[d];
+            vs2[d] -= vs[d] * vs[d];
+          }
+          cr[6] = (float)sqrt(ps2[0] + ps2[1] + ps2[2]);
+          cr[7] = (float)sqrt(vs2[0] + vs2[1] + vs2[2]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+} // namespace hbtg

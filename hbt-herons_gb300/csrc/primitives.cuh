@@ -1,0 +1,285 @@
+// primitives.cuh - hand-written device-wide scan and LSD radix sort.
+//
+// Both are tile-based (2048 items per 256-thread block): a per-tile pass,
+// a scan of the per-tile totals (recursive) and a fix-up pass.  The radix
+// sort is stable, with 8-bit digits; segmented sorting is done by sorting on
+// the key and then, stably, on the segment id (see unbind.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace hbtg
+{
+
+constexpr int kScanThreads = 256;
+
+// Items per thread of a scan tile: 8 for 4/8-byte types, 4 for D4 (keeps the
+// tile in 32 KB of shared memory).
+template <typename T>
+__host__ __device__ constexpr int scan_items()
+{
+  return sizeof(T) > 8 ? 4 : 8;
+}
+template <typename T>
+__host__ __device__ constexpr int scan_tile()
+{
+  return kScanThreads * scan_items<T>();
+}
+
+struct D4
+{
+  double m, x, y, z;
+  __host__ __device__ D4 operator+(const D4 &o) const { return D4{m + o.m, x + o.x, y + o.y, z + o.z}; }
+};
+
+template <typename T>
+__device__ __forceinline__ T zero_of();
+template <>
+__device__ __forceinline__ int zero_of<int>() { return 0; }
+template <>
+__device__ __forceinline__ long long zero_of<long long>() { return 0; }
+template <>
+__device__ __forceinline__ D4 zero_of<D4>() { return D4{0., 0., 0., 0.}; }
+
+template <typename T>
+__device__ __forceinline__ T shfl_up(T v, int d)
+{
+  return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <>
+__device__ __forceinline__ D4 shfl_up<D4>(D4 v, int d)
+{
+  return D4{__shfl_up_sync(0xffffffffu, v.m, d), __shfl_up_sync(0xffffffffu, v.x, d),
+            __shfl_up_sync(0xffffffffu, v.y, d), __shfl_up_sync(0xffffffffu, v.z, d)};
+}
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+template <typename T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T &total)
+{
+  __shared__ T warp_tot[kScanThreads / kWarp];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T inc = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1)
+  {
+    T o = shfl_up(inc, d);
+    if (lane >= d)
+      inc = inc + o;
+  }
+  if (lane == 31)
+    warp_tot[warp] = inc;
+  __syncthreads();
+  T warp_off = zero_of<T>();
+  T tot = zero_of<T>();
+#pragma unroll
+  for (int w = 0; w < kScanThreads / kWarp; w++)
+  {
+    if (w < warp)
+      warp_off = warp_off + warp_tot[w];
+    tot = tot + warp_tot[w];
+  }
+  __syncthreads();
+  total = tot;
+  // exclusive = inclusive - v, written without subtraction (exact for doubles)
+  T excl = shfl_up(inc, 1);
+  if (lane == 0)
+    excl = zero_of<T>();
+  return warp_off + excl;
+}
+
+// Scans each tile; writes tile totals when `tile_sums` is non-null.
+template <typename T, bool Inclusive>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const T *__restrict__ in, T *__restrict__ out,
+                                                             T *__restrict__ tile_sums, long long n)
+{
+  constexpr int kTile = scan_tile<T>();
+  constexpr int kScanItems = scan_items<T>();
+  __shared__ T s[kTile];
+  const long long base = (long long)blockIdx.x * kTile;
+  for (int i = threadIdx.x; i < kTile; i += kScanThreads)
+    s[i] = (base + i < n) ? in[base + i] : zero_of<T>();
+  __syncthreads();
+  T local[kScanItems];
+  T acc = zero_of<T>();
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+  {
+    local[k] = acc;
+    acc = acc + s[threadIdx.x * kScanItems + k];
+  }
+  T total;
+  const T off = block_exclusive_scan(acc, total);
+#pragma unroll
+  for (int k = 0; k < kScanItems; k++)
+  {
+    const T v = s[threadIdx.x * kScanItems + k];
+    s[threadIdx.x * kScanItems + k] = Inclusive ? (off + local[k]) + v : off + local[k];
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kTile; i += kScanThreads)
+    if (base + i < n)
+      out[base + i] = s[i];
+  if (tile_sums && threadIdx.x == 0)
+    tile_sums[blockIdx.x] = total;
+}
+
+template <typename T>
+__global__ void k_add_tile_offsets(T *__restrict__ out, const T *__restrict__ tile_off, long long n)
+{
+  constexpr int kTile = scan_tile<T>();
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && i >= kTile)
+    out[i] = tile_off[i / kTile] + out[i];
+}
+
+// Scratch needed by scan<T>(n): sum over recursion levels of the tile counts.
+template <typename T>
+inline size_t scan_scratch_elems(long long n)
+{
+  constexpr int kTile = scan_tile<T>();
+  size_t tot = 0;
+  while (n > kTile)
+  {
+    n = (n + kTile - 1) / kTile;
+    tot += 2 * (size_t)n;
+  }
+  return tot + 2;
+}
+
+// Device-wide scan of n items (in may equal out).  `scratch` must hold
+// scan_scratch_elems(n) items of T.
+template <typename T, bool Inclusive>
+void scan(const T *in, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
+{
+  constexpr int kTile = scan_tile<T>();
+  if (n <= 0)
+    return;
+  const long long tiles = (n + kTile - 1) / kTile;
+  if (tiles == 1)
+  {
+    k_scan_tiles<T, Inclusive><<<1, kScanThreads, 0, st>>>(in, out, nullptr, n);
+    (*launches)++;
+    return;
+  }
+  T *sums = scratch, *sums_scanned = scratch + tiles;
+  k_scan_tiles<T, Inclusive><<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, sums, n);
+  scan<T, false>(sums, sums_scanned, tiles, scratch + 2 * tiles, st, launches);
+  k_add_tile_offsets<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, sums_scanned, n);
+  *launches += 2;
+}
+
+// ---------------------------------------------------------------------------
+// LSD radix sort, 8-bit digits, stable.  Keys K = uint32_t or uint64_t,
+// 32-bit values.
+// ---------------------------------------------------------------------------
+constexpr int kRadixThreads = 256;
+constexpr int kRadixItems = 8;
+constexpr int kRadixTile = kRadixThreads * kRadixItems;
+
+template <typename K>
+__global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const K *__restrict__ keys, long long n, int shift,
+                                                              uint32_t mask, int *__restrict__ table, int tiles)
+{
+  __shared__ int cnt[256];
+  cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kRadixTile;
+#pragma unroll
+  for (int k = 0; k < kRadixItems; k++)
+  {
+    const long long i = base + k * kRadixThreads + threadIdx.x;
+    if (i < n)
+      atomicAdd(&cnt[(uint32_t)(keys[i] >> shift) & mask], 1);
+  }
+  __syncthreads();
+  table[(long long)threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kRadixThreads)
+  k_radix_scatter(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
+                  uint32_t *__restrict__ vout, long long n, int shift, uint32_t mask, const int *__restrict__ table,
+                  int tiles)
+{
+  __shared__ int s_off[256];
+  __shared__ int s_base[256];
+  __shared__ int s_warp[kRadixThreads / kWarp][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  s_off[threadIdx.x] = table[(long long)threadIdx.x * tiles + blockIdx.x];
+  s_base[threadIdx.x] = 0;
+  const long long base = (long long)blockIdx.x * kRadixTile;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  for (int r = 0; r < kRadixItems; r++)
+  {
+#pragma unroll
+    for (int w = 0; w < kRadixThreads / kWarp; w++)
+      s_warp[w][threadIdx.x] = 0;
+    __syncthreads();
+    const long long i = base + r * kRadixThreads + threadIdx.x;
+    const bool valid = i < n;
+    K key = valid ? kin[i] : K(0);
+    uint32_t val = valid ? vin[i] : 0u;
+    const uint32_t d = valid ? ((uint32_t)(key >> shift) & mask) : (256u + lane);
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    if (valid && lane == leader)
+      s_warp[warp][d] = __popc(peers);
+    __syncthreads();
+    if (valid)
+    {
+      int rank = s_base[d] + __popc(peers & lt_mask);
+      for (int w = 0; w < warp; w++)
+        rank += s_warp[w][d];
+      const int dst = s_off[d] + rank;
+      kout[dst] = key;
+      vout[dst] = val;
+    }
+    __syncthreads();
+    int add = 0;
+#pragma unroll
+    for (int w = 0; w < kRadixThreads / kWarp; w++)
+      add += s_warp[w][threadIdx.x];
+    s_base[threadIdx.x] += add;
+  }
+}
+
+inline size_t radix_table_elems(long long n)
+{
+  const long long tiles = (n + kRadixTile - 1) / kRadixTile;
+  return (size_t)256 * tiles;
+}
+
+// Sorts (keys, vals) on bits [begin_bit, end_bit).  Ping-pongs between the
+// two buffer pairs; returns true when the result lies in (k_alt, v_alt).
+// `table` holds radix_table_elems(n) ints, `scan_scratch`
+// scan_scratch_elems<int>(radix_table_elems(n)) ints.
+template <typename K>
+bool radix_sort_pairs(K *keys, uint32_t *vals, K *k_alt, uint32_t *v_alt, long long n, int begin_bit, int end_bit,
+                      int *table, int *scan_scratch, cudaStream_t st, int64_t *launches)
+{
+  if (n <= 1 || end_bit <= begin_bit)
+    return false;
+  const int tiles = (int)((n + kRadixTile - 1) / kRadixTile);
+  bool flipped = false;
+  for (int shift = begin_bit; shift < end_bit; shift += 8)
+  {
+    const int bits = (end_bit - shift) < 8 ? (end_bit - shift) : 8;
+    const uint32_t mask = (1u << bits) - 1u;
+    const K *ki = flipped ? k_alt : keys;
+    const uint32_t *vi = flipped ? v_alt : vals;
+    K *ko = flipped ? keys : k_alt;
+    uint32_t *vo = flipped ? vals : v_alt;
+    k_radix_hist<K><<<tiles, kRadixThreads, 0, st>>>(ki, n, shift, mask, table, tiles);
+    scan<int, false>(table, table, (long long)256 * tiles, scan_scratch, st, launches);
+    k_radix_scatter<K><<<tiles, kRadixThreads, 0, st>>>(ki, vi, ko, vo, n, shift, mask, table, tiles);
+    *launches += 2;
+    flipped = !flipped;
+  }
+  return flipped;
+}
+
+} // namespace hbtg

@@ -1,0 +1,772 @@
+// unbind.cu - host orchestration and C ABI of libhbtg.so (include/hbt_unbind_gpu.h).
+//
+// One call unbinds a batch of subhaloes on one GPU.  All subhaloes still
+// iterating advance in lock step: each global iteration is a fixed kernel
+// sequence (plan, tree build, walk, energies, partition, sorts, frame,
+// control) over the packed active segments; subhaloes leave the active set
+// when they converge or disrupt, exactly where Subhalo_t::Unbind breaks out of
+// its loop (src/subhalo_unbind.cpp:555-758).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/hbt_unbind_gpu.h"
+#include "common.cuh"
+#include "kernels.cuh"
+#include "primitives.cuh"
+
+using namespace hbtg;
+
+namespace
+{
+
+struct CudaError
+{
+  cudaError_t err;
+};
+struct NoMem
+{
+};
+
+#define HBTG_CUDA(call)                                                                                                \
+  do                                                                                                                   \
+  {                                                                                                                    \
+    cudaError_t e_ = (call);                                                                                           \
+    if (e_ != cudaSuccess)                                                                                             \
+    {                                                                                                                  \
+      if (e_ == cudaErrorMemoryAllocation)                                                                             \
+        throw NoMem{};                                                                                                 \
+      throw CudaError{e_};                                                                                             \
+    }                                                                                                                  \
+  } while (0)
+
+// Grow-only device buffers, one per slot.
+enum Slot
+{
+  S_POS, S_VEL, S_MASS, S_U, S_ID, S_TYPE, S_OFF,
+  S_REFP, S_REFV, S_MBP, S_MBV, S_MBID,
+  S_ORDER, S_NB, S_MB, S_NBT, S_MBT, S_TI, S_KIN, S_CORE, S_EN, S_POT, S_ITER, S_STAT,
+  S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
+  S_SUBI, S_SUBF, S_BB, S_ROOT, S_COM,
+  S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
+  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER,
+  S_NUM
+};
+
+struct Pool
+{
+  void *ptr[S_NUM] = {};
+  size_t cap[S_NUM] = {};
+  void *get(int slot, size_t bytes)
+  {
+    if (bytes == 0)
+      bytes = 16;
+    if (cap[slot] >= bytes)
+      return ptr[slot];
+    if (ptr[slot])
+      cudaFree(ptr[slot]);
+    ptr[slot] = nullptr;
+    cap[slot] = 0;
+    const size_t want = bytes + bytes / 4;
+    void *p = nullptr;
+    if (cudaMalloc(&p, want) != cudaSuccess)
+    {
+      cudaGetLastError();
+      throw NoMem{};
+    }
+    ptr[slot] = p;
+    cap[slot] = want;
+    return p;
+  }
+  template <typename T>
+  T *get(int slot, size_t count)
+  {
+    return static_cast<T *>(get(slot, count * sizeof(T)));
+  }
+  void release()
+  {
+    for (int i = 0; i < S_NUM; i++)
+      if (ptr[i])
+        cudaFree(ptr[i]);
+    std::memset(ptr, 0, sizeof(ptr));
+    std::memset(cap, 0, sizeof(cap));
+  }
+};
+
+inline unsigned blocks_for(long long n, int threads)
+{
+  long long b = (n + threads - 1) / threads;
+  return (unsigned)std::max<long long>(1, std::min<long long>(b, 0x7fffffffLL));
+}
+
+} // namespace
+
+struct hbtg_handle
+{
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t stream = nullptr;
+  Pool pool;
+  hbtg_stats stats{};
+  bool count_interactions = false;
+  std::vector<cudaEvent_t> walk_events;
+};
+
+namespace
+{
+
+KParams make_kparams(const hbtg_params *p, bool count)
+{
+  KParams K;
+  K.box = (float)p->box_size;
+  K.half = (float)((double)K.box / 2.);
+  K.periodic = p->periodic != 0;
+  K.soft = (float)p->softening;
+  K.h = (float)(2.8 * (double)K.soft);
+  K.h_inv = (float)(1.0 / (2.8 * (double)K.soft));
+  K.res = (float)p->tree_node_resolution;
+  const float theta = (float)p->open_angle;
+  K.theta2 = theta * theta;
+  K.bmp = (float)p->bound_mass_precision;
+  K.min_part = (int)p->min_num_part;
+  K.min_tracer = (int)p->min_num_tracer;
+  K.tracer_mask = p->tracer_type_mask;
+  K.dm_only = p->dm_only != 0;
+  K.thermal = p->thermal != 0;
+  const float G = (float)p->G, a = (float)p->scale_factor;
+  K.G_over_a = (float)((double)G / (double)a);
+  K.a = a;
+  K.hz = (float)p->hubble;
+  K.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
+  K.core_min = p->sub_core_size_min;
+  K.core_factor = (float)p->sub_core_size_factor;
+  K.count_interactions = count ? 1 : 0;
+  return K;
+}
+
+int validate(const hbtg_params *p, const hbtg_batch *b, long long &N)
+{
+  if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
+    return HBTG_ERR_INVALID;
+  if (p->max_sample_size > 0)
+    return HBTG_ERR_UNSUPPORTED; // potential subsampling is not implemented on the GPU path
+  if (!(p->softening > 0) || !(p->open_angle > 0) || !(p->box_size > 0))
+    return HBTG_ERR_INVALID;
+  if (b->n_sub > 0 && b->offsets[0] != 0)
+    return HBTG_ERR_INVALID;
+  for (int64_t s = 0; s < b->n_sub; s++)
+    if (b->offsets[s + 1] < b->offsets[s])
+      return HBTG_ERR_INVALID;
+  N = b->n_sub > 0 ? b->offsets[b->n_sub] : 0;
+  if (N >= (1LL << 30) || b->n_sub >= (1LL << 30))
+    return HBTG_ERR_INVALID;
+  if (N > 0 && (!b->pos || !b->vel || !b->mass || !b->id || !b->order))
+    return HBTG_ERR_INVALID;
+  if (b->n_sub > 0 && (!b->ref_pos || !b->ref_vel || !b->mostbound_pos || !b->mostbound_vel ||
+                       !b->most_bound_id || !b->nbound || !b->mbound || !b->tracer_index || !b->iterations ||
+                       !b->status))
+    return HBTG_ERR_INVALID;
+  return HBTG_OK;
+}
+
+// Reads one int from device memory (synchronises the stream).
+int read_int(const int *d, cudaStream_t st)
+{
+  int h = 0;
+  HBTG_CUDA(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HBTG_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+struct Runner
+{
+  hbtg_handle *H;
+  cudaStream_t st;
+  KParams K;
+  DevState D;
+  int S;
+  long long N;
+  int seg_bits;
+  int64_t *launches;
+
+  void check() { HBTG_CUDA(cudaGetLastError()); }
+
+  // scan of n+1 counts (the last is a zero) into offs; returns the total
+  int scan_counts(const int *cnt, int *offs, long long n)
+  {
+    int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(n + 1, 256 * 4096)));
+    scan<int, false>(cnt, offs, n + 1, scr, st, launches);
+    check();
+    return read_int(offs + n, st);
+  }
+
+  // Sorts (keys, vals) of `total` packed items by key then by subhalo.
+  // Returns the array holding the sorted values.
+  template <typename Kt>
+  uint32_t *segmented_sort(Kt *keys, Kt *keys_alt, int key_bits, int total)
+  {
+    int *table = H->pool.get<int>(S_TABLE, radix_table_elems(std::max(total, 1)));
+    int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(
+                                             radix_table_elems(std::max(total, 1)) + 1, 256 * 4096)));
+    bool flip = radix_sort_pairs<Kt>(keys, D.val, keys_alt, D.val_alt, total, 0, key_bits, table, scr, st, launches);
+    uint32_t *v = flip ? D.val_alt : D.val;
+    uint32_t *v_other = flip ? D.val : D.val_alt;
+    if (S > 1 && seg_bits > 0)
+    {
+      k_segkeys<<<blocks_for(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
+      (*launches)++;
+      bool f2 = radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scr, st,
+                                           launches);
+      v = f2 ? v_other : v;
+    }
+    check();
+    return v;
+  }
+
+  void run()
+  {
+    const unsigned sb = blocks_for(S + 1, 256);
+    int global_iter = 0;
+    H->stats.interactions = 0;
+    H->stats.tree_nodes = 0;
+    float ms_walk = 0.f;
+    for (;;)
+    {
+      k_plan<<<sb, 256, 0, st>>>(D);
+      (*launches)++;
+      check();
+      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
+      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
+      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
+      if (part_total == 0 && src_total == 0)
+        break;
+      global_iter++;
+      // --- tree over the sources ---
+      if (src_total > 0)
+      {
+        k_bbox<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
+        k_root<<<sb, 256, 0, st>>>(D, K);
+        k_keys<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
+        *launches += 3;
+        check();
+        uint32_t *sorted = segmented_sort<unsigned long long>(D.key, D.key_alt, 63, src_total);
+        if (sorted != D.val)
+          HBTG_CUDA(cudaMemcpyAsync(D.val, sorted, sizeof(uint32_t) * src_total, cudaMemcpyDeviceToDevice, st));
+        k_keys_again<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
+        k_tree_count<<<blocks_for(src_total + 1, 256), 256, 0, st>>>(D, src_total);
+        *launches += 2;
+        check();
+        const int internal = scan_counts(D.cnt, D.X, src_total);
+        const long long records = (long long)src_total + internal;
+        if (records >= (1LL << 31) - 64)
+          throw NoMem{};
+        D.nodes = H->pool.get<NodeRec>(S_NODES, (size_t)records);
+        H->stats.tree_nodes += internal;
+        k_prefix_prep<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
+        (*launches)++;
+        D4 *d4scr = H->pool.get<D4>(S_D4SCR, scan_scratch_elems<D4>(src_total));
+        scan<D4, true>(D.P, D.P, src_total, d4scr, st, launches);
+        k_tree_emit<<<blocks_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
+        (*launches)++;
+        check();
+      }
+      // --- walk ---
+      if (chunk_total > 0)
+      {
+        cudaEvent_t e0 = H->walk_events[0], e1 = H->walk_events[1];
+        HBTG_CUDA(cudaEventRecord(e0, st));
+        const int warps_per_block = 8;
+        k_walk<<<blocks_for(chunk_total, warps_per_block), 32 * warps_per_block, 0, st>>>(D, K, chunk_total);
+        HBTG_CUDA(cudaEventRecord(e1, st));
+        (*launches)++;
+        H->stats.walk_launches++;
+        check();
+        HBTG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        HBTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        ms_walk += ms;
+      }
+      // --- energies and partition ---
+      if (part_total > 0)
+      {
+        k_energy<<<blocks_for(part_total, 256), 256, 0, st>>>(D, K, part_total);
+        k_part_flags<<<blocks_for(part_total + 1, 256), 256, 0, st>>>(D, part_total);
+        *launches += 2;
+        check();
+        int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(part_total + 1,
+                                                                                             256 * 4096)));
+        scan<int, false>(D.flags, D.F, part_total + 1, scr, st, launches);
+        k_part_count<<<sb, 256, 0, st>>>(D);
+        k_part_scatter<<<blocks_for(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_part_copy<<<blocks_for(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_after_part<<<sb, 256, 0, st>>>(D, K);
+        *launches += 4;
+        check();
+        // sort the newly unbound tails by energy
+        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
+        if (tail_total > 0)
+        {
+          k_energy_keys<<<blocks_for(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
+          (*launches)++;
+          uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, tail_total);
+          k_energy_write<<<blocks_for(tail_total, 256), 256, 0, st>>>(D, sorted, D.tail_off, tail_total, 0);
+          (*launches)++;
+          check();
+        }
+        // centre-of-mass frame and convergence
+        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
+        (*launches)++;
+        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
+        if (bound_total > 0)
+        {
+          k_com<<<blocks_for(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
+          (*launches)++;
+        }
+        k_control<<<sb, 256, 0, st>>>(D, K);
+        (*launches)++;
+        check();
+      }
+    }
+    H->stats.global_iterations = global_iter;
+    H->stats.ms_walk = ms_walk;
+    // final sort of the bound sets by binding energy
+    k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
+    (*launches)++;
+    const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);
+    if (fin_total > 0)
+    {
+      k_energy_keys<<<blocks_for(fin_total, 256), 256, 0, st>>>(D, D.fin_off, fin_total, 1);
+      (*launches)++;
+      uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, fin_total);
+      k_energy_write<<<blocks_for(fin_total, 256), 256, 0, st>>>(D, sorted, D.fin_off, fin_total, 1);
+      (*launches)++;
+      check();
+    }
+  }
+};
+
+// The batch with every array on the device (offsets on the host).
+int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaStream_t st)
+{
+  long long N = 0;
+  int rc = validate(p, b, N);
+  if (rc != HBTG_OK)
+    return rc;
+  const int S = (int)b->n_sub;
+  H->stats = hbtg_stats{};
+  H->stats.n_sub = S;
+  H->stats.n_particles = N;
+  if (S == 0)
+    return HBTG_OK;
+  int64_t launches = 0;
+  cudaEvent_t t0, t1;
+  HBTG_CUDA(cudaEventCreate(&t0));
+  HBTG_CUDA(cudaEventCreate(&t1));
+  HBTG_CUDA(cudaEventRecord(t0, st));
+
+  Runner R;
+  R.H = H;
+  R.st = st;
+  R.K = make_kparams(p, H->count_interactions);
+  R.S = S;
+  R.N = N;
+  R.launches = &launches;
+  int bits = 0;
+  while ((1LL << bits) < S)
+    bits++;
+  R.seg_bits = bits;
+  Pool &P = H->pool;
+  DevState &D = R.D;
+  D.S = S;
+  D.N = N;
+  long long *off = P.get<long long>(S_OFF, S + 1);
+  HBTG_CUDA(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
+  D.off = off;
+  const size_t n1 = (size_t)std::max<long long>(N, 1);
+  D.pm = P.get<float4>(S_PM, n1);
+  D.vu = P.get<float4>(S_VU, n1);
+  D.ty = P.get<uint8_t>(S_TY, n1);
+  D.seg_of = P.get<int>(S_SEG, n1);
+  D.ord = P.get<int>(S_ORD, n1);
+  D.ord_tmp = P.get<int>(S_ORDT, n1);
+  D.Ep = P.get<float>(S_EP, n1);
+  D.pot = P.get<float>(S_PHI, n1);
+  D.id = reinterpret_cast<const long long *>(b->id);
+  int *subi = P.get<int>(S_SUBI, (size_t)(S + 1) * 24);
+  int q = 0;
+  auto nexti = [&]() { return subi + (size_t)(S + 1) * (q++); };
+  D.n_s = nexti(); D.nbound = nexti(); D.nlast = nexti(); D.state = nexti(); D.corr = nexti(); D.iter = nexti();
+  D.wrap = nexti(); D.tracers = nexti(); D.nb_new = nexti(); D.src_begin = nexti(); D.src_cnt = nexti();
+  D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
+  D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
+  float *subf = P.get<float>(S_SUBF, (size_t)S * 8);
+  D.old_pos = subf;
+  D.old_vel = subf + 3 * (size_t)S;
+  D.mbound = subf + 6 * (size_t)S;
+  D.ref_pos = b->ref_pos;
+  D.ref_vel = b->ref_vel;
+  D.mb_pos = b->mostbound_pos;
+  D.mb_vel = b->mostbound_vel;
+  D.mb_id = reinterpret_cast<long long *>(b->most_bound_id);
+  unsigned *bb = P.get<unsigned>(S_BB, (size_t)S * 6);
+  D.bb_lo = bb;
+  D.bb_hi = bb + 3 * (size_t)S;
+  D.root = P.get<double>(S_ROOT, (size_t)S * 4);
+  D.com = P.get<double>(S_COM, (size_t)S * 7);
+  D.key = P.get<unsigned long long>(S_KEY, n1);
+  D.key_alt = P.get<unsigned long long>(S_KEYA, n1);
+  D.val = P.get<uint32_t>(S_VAL, n1);
+  D.val_alt = P.get<uint32_t>(S_VALA, n1);
+  D.k32 = P.get<uint32_t>(S_K32, n1);
+  D.k32_alt = P.get<uint32_t>(S_K32A, n1);
+  D.cnt = P.get<int>(S_CNT, n1 + 1);
+  D.X = P.get<int>(S_X, n1 + 1);
+  D.flags = P.get<int>(S_FLAGS, n1 + 1);
+  D.F = P.get<int>(S_F, n1 + 1);
+  D.P = P.get<D4>(S_P, n1);
+  D.nodes = P.get<NodeRec>(S_NODES, n1 * 2);
+  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+
+  if (N > 0)
+  {
+    k_repack<<<blocks_for(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
+    launches++;
+  }
+  k_init_subs<<<blocks_for(S, 256), 256, 0, st>>>(D);
+  launches++;
+  R.check();
+  R.run();
+
+  OutPtrs O;
+  O.order = reinterpret_cast<long long *>(b->order);
+  O.nbound = reinterpret_cast<long long *>(b->nbound);
+  O.nbound_type = reinterpret_cast<long long *>(b->nbound_type);
+  O.tracer_index = reinterpret_cast<long long *>(b->tracer_index);
+  O.most_bound_id = reinterpret_cast<long long *>(b->most_bound_id);
+  O.mbound = b->mbound;
+  O.mbound_type = b->mbound_type;
+  O.kinematics = b->kinematics;
+  O.core = b->core;
+  O.energy = b->energy;
+  O.potential = b->potential;
+  O.iterations = b->iterations;
+  O.status = b->status;
+  k_epilogue<<<std::min(S, 65535), 256, 0, st>>>(D, R.K, O);
+  launches++;
+  R.check();
+  HBTG_CUDA(cudaEventRecord(t1, st));
+  HBTG_CUDA(cudaEventSynchronize(t1));
+  float ms = 0.f;
+  HBTG_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  H->stats.ms_total = ms;
+  H->stats.kernel_launches = launches;
+  if (H->count_interactions)
+  {
+    unsigned long long c = 0;
+    HBTG_CUDA(cudaMemcpy(&c, D.interactions, sizeof(c), cudaMemcpyDeviceToHost));
+    H->stats.interactions = (int64_t)c;
+  }
+  // summary counters
+  std::vector<long long> nb(S);
+  HBTG_CUDA(cudaMemcpy(nb.data(), b->nbound, sizeof(long long) * S, cudaMemcpyDeviceToHost));
+  long long tot = 0;
+  for (long long v : nb)
+    tot += v;
+  H->stats.total_bound = tot;
+  int any_max = 0;
+  std::vector<int> stv(S);
+  HBTG_CUDA(cudaMemcpy(stv.data(), b->status, sizeof(int) * S, cudaMemcpyDeviceToHost));
+  for (int v : stv)
+    any_max |= (v == HBTG_SUB_MAX_ITER);
+  return any_max ? HBTG_ERR_MAX_ITER : HBTG_OK;
+}
+
+template <typename T>
+T *upload(Pool &P, int slot, const T *h, size_t n, cudaStream_t st, int64_t &bytes)
+{
+  if (!h)
+    return nullptr;
+  T *d = P.get<T>(slot, std::max<size_t>(n, 1));
+  if (n)
+    HBTG_CUDA(cudaMemcpyAsync(d, h, sizeof(T) * n, cudaMemcpyHostToDevice, st));
+  bytes += sizeof(T) * n;
+  return d;
+}
+template <typename T>
+T *alloc_out(Pool &P, int slot, const T *h, size_t n)
+{
+  return h ? P.get<T>(slot, std::max<size_t>(n, 1)) : nullptr;
+}
+template <typename T>
+void download(T *h, const T *d, size_t n, cudaStream_t st, int64_t &bytes)
+{
+  if (h && d && n)
+  {
+    HBTG_CUDA(cudaMemcpyAsync(h, d, sizeof(T) * n, cudaMemcpyDeviceToHost, st));
+    bytes += sizeof(T) * n;
+  }
+}
+
+int guarded(int (*fn)(void *), void *arg)
+{
+  try
+  {
+    return fn(arg);
+  }
+  catch (NoMem &)
+  {
+    cudaGetLastError();
+    return HBTG_ERR_NOMEM;
+  }
+  catch (CudaError &e)
+  {
+    (void)e;
+    return HBTG_ERR_CUDA;
+  }
+  catch (std::bad_alloc &)
+  {
+    return HBTG_ERR_NOMEM;
+  }
+  catch (...)
+  {
+    return HBTG_ERR_CUDA;
+  }
+}
+
+struct HostCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  hbtg_batch *b;
+};
+
+int host_call(void *arg)
+{
+  HostCall &c = *static_cast<HostCall *>(arg);
+  hbtg_handle *H = c.H;
+  hbtg_batch *b = c.b;
+  long long N = 0;
+  int rc = validate(c.p, b, N);
+  if (rc != HBTG_OK)
+    return rc;
+  HBTG_CUDA(cudaSetDevice(H->device));
+  cudaStream_t st = H->stream;
+  const size_t S = (size_t)b->n_sub;
+  Pool &P = H->pool;
+  int64_t h2d = 0, d2h = 0;
+  hbtg_batch d = *b;
+  d.pos = upload(P, S_POS, b->pos, 3 * N, st, h2d);
+  d.vel = upload(P, S_VEL, b->vel, 3 * N, st, h2d);
+  d.mass = upload(P, S_MASS, b->mass, N, st, h2d);
+  d.u = (c.p->thermal && b->u) ? upload(P, S_U, b->u, N, st, h2d) : nullptr;
+  d.id = upload(P, S_ID, b->id, N, st, h2d);
+  d.type = (c.p->dm_only || !b->type) ? nullptr : upload(P, S_TYPE, b->type, N, st, h2d);
+  d.ref_pos = upload(P, S_REFP, b->ref_pos, 3 * S, st, h2d);
+  d.ref_vel = upload(P, S_REFV, b->ref_vel, 3 * S, st, h2d);
+  d.mostbound_pos = upload(P, S_MBP, b->mostbound_pos, 3 * S, st, h2d);
+  d.mostbound_vel = upload(P, S_MBV, b->mostbound_vel, 3 * S, st, h2d);
+  d.most_bound_id = upload(P, S_MBID, b->most_bound_id, S, st, h2d);
+  d.order = alloc_out(P, S_ORDER, b->order, N);
+  d.nbound = alloc_out(P, S_NB, b->nbound, S);
+  d.mbound = alloc_out(P, S_MB, b->mbound, S);
+  d.nbound_type = alloc_out(P, S_NBT, b->nbound_type, 6 * S);
+  d.mbound_type = alloc_out(P, S_MBT, b->mbound_type, 6 * S);
+  d.tracer_index = alloc_out(P, S_TI, b->tracer_index, S);
+  d.kinematics = alloc_out(P, S_KIN, b->kinematics, 5 * S);
+  d.core = alloc_out(P, S_CORE, b->core, 8 * S);
+  d.energy = alloc_out(P, S_EN, b->energy, N);
+  d.potential = alloc_out(P, S_POT, b->potential, N);
+  d.iterations = alloc_out(P, S_ITER, b->iterations, S);
+  d.status = alloc_out(P, S_STAT, b->status, S);
+  rc = run_device(H, c.p, &d, st);
+  if (rc != HBTG_OK && rc != HBTG_ERR_MAX_ITER)
+    return rc;
+  download(b->order, d.order, N, st, d2h);
+  download(b->nbound, d.nbound, S, st, d2h);
+  download(b->mbound, d.mbound, S, st, d2h);
+  download(b->nbound_type, d.nbound_type, 6 * S, st, d2h);
+  download(b->mbound_type, d.mbound_type, 6 * S, st, d2h);
+  download(b->tracer_index, d.tracer_index, S, st, d2h);
+  download(b->kinematics, d.kinematics, 5 * S, st, d2h);
+  download(b->core, d.core, 8 * S, st, d2h);
+  download(b->energy, d.energy, N, st, d2h);
+  download(b->potential, d.potential, N, st, d2h);
+  download(b->iterations, d.iterations, S, st, d2h);
+  download(b->status, d.status, S, st, d2h);
+  download(b->ref_pos, d.ref_pos, 3 * S, st, d2h);
+  download(b->ref_vel, d.ref_vel, 3 * S, st, d2h);
+  download(b->mostbound_pos, d.mostbound_pos, 3 * S, st, d2h);
+  download(b->mostbound_vel, d.mostbound_vel, 3 * S, st, d2h);
+  download(b->most_bound_id, d.most_bound_id, S, st, d2h);
+  HBTG_CUDA(cudaStreamSynchronize(st));
+  H->stats.h2d_bytes = h2d;
+  H->stats.d2h_bytes = d2h;
+  return rc;
+}
+
+struct DevCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  hbtg_batch *b;
+  cudaStream_t st;
+};
+
+int dev_call(void *arg)
+{
+  DevCall &c = *static_cast<DevCall *>(arg);
+  HBTG_CUDA(cudaSetDevice(c.H->device));
+  const int rc = run_device(c.H, c.p, c.b, c.st);
+  HBTG_CUDA(cudaStreamSynchronize(c.st));
+  return rc;
+}
+
+} // namespace
+
+extern "C" {
+
+int hbtg_create(hbtg_handle **handle, int device)
+{
+  if (!handle)
+    return HBTG_ERR_INVALID;
+  *handle = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0)
+  {
+    cudaGetLastError();
+    return HBTG_ERR_NO_DEVICE;
+  }
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess)
+    return HBTG_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3)
+    return HBTG_ERR_NO_DEVICE; // built for sm_103a only
+  hbtg_handle *h = new (std::nothrow) hbtg_handle();
+  if (!h)
+    return HBTG_ERR_NOMEM;
+  h->device = device;
+  h->sm_count = prop.multiProcessorCount;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) !=
+                                                  cudaSuccess)
+  {
+    delete h;
+    return HBTG_ERR_CUDA;
+  }
+  h->walk_events.resize(2);
+  for (auto &e : h->walk_events)
+    if (cudaEventCreate(&e) != cudaSuccess)
+    {
+      delete h;
+      return HBTG_ERR_CUDA;
+    }
+  *handle = h;
+  return HBTG_OK;
+}
+
+int hbtg_destroy(hbtg_handle *h)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  cudaSetDevice(h->device);
+  h->pool.release();
+  for (auto &e : h->walk_events)
+    cudaEventDestroy(e);
+  if (h->stream)
+    cudaStreamDestroy(h->stream);
+  delete h;
+  return HBTG_OK;
+}
+
+int hbtg_unbind_batch(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  HostCall c{h, p, b};
+  return guarded(host_call, &c);
+}
+
+int hbtg_unbind_batch_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b, void *cuda_stream)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  DevCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream)};
+  return guarded(dev_call, &c);
+}
+
+int hbtg_get_stats(const hbtg_handle *h, hbtg_stats *s)
+{
+  if (!h || !s)
+    return HBTG_ERR_INVALID;
+  *s = h->stats;
+  return HBTG_OK;
+}
+
+int hbtg_set_count_interactions(hbtg_handle *h, int enable)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  h->count_interactions = enable != 0;
+  return HBTG_OK;
+}
+
+const char *hbtg_status_string(int status)
+{
+  switch (status)
+  {
+  case HBTG_OK:
+    return "ok";
+  case HBTG_ERR_INVALID:
+    return "invalid argument";
+  case HBTG_ERR_NOMEM:
+    return "out of memory";
+  case HBTG_ERR_CUDA:
+    return "CUDA error";
+  case HBTG_ERR_MAX_ITER:
+    return "a subhalo reached max_iterations";
+  case HBTG_ERR_UNSUPPORTED:
+    return "unsupported parameters";
+  case HBTG_ERR_NO_DEVICE:
+    return "no sm_103 CUDA device";
+  default:
+    return "unknown status";
+  }
+}
+
+void hbtg_default_params(hbtg_params *p)
+{
+  if (!p)
+    return;
+  std::memset(p, 0, sizeof(*p));
+  p->box_size = 100.0;
+  p->periodic = 1;
+  p->softening = 0.005;
+  p->tree_node_resolution = 0.0005;
+  p->open_angle = 0.45;
+  p->bound_mass_precision = 0.995;
+  p->min_num_part = 20;
+  p->min_num_tracer = 10;
+  p->tracer_type_mask = (1 << 1) | (1 << 4);
+  p->no_subsample_mask = 1 << 5;
+  p->max_sample_size = 1000;
+  p->refine_most_bound = 1;
+  p->refine_fraction = 0.1;
+  p->upscale_per_type = 1;
+  p->sub_core_size_min = 20;
+  p->sub_core_size_factor = 0.0;
+  p->dm_only = 0;
+  p->thermal = 0;
+  p->G = 43.0071;
+  p->scale_factor = 1.0;
+  p->hubble = 0.0;
+  p->max_iterations = 1000;
+  p->mode = 0;
+  p->seed = 0;
+}
+
+} // extern "C"

@@ -1,0 +1,161 @@
+"""Python binding of the GB300 unbinding library (libhbtg.so) through its C ABI.
+
+This is the product path: every call goes to the CUDA library.  There is no
+CPU fallback; if the library is missing or no sm_103 device is present the
+calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .abi import CallBuffers, CBatch, CStats, Inputs, Outputs, Params, STATUS_NAMES
+from .build import LIB
+
+_lib = None
+
+
+class UnbindError(RuntimeError):
+    def __init__(self, code, what):
+        super().__init__("%s failed: %s (%d)" % (what, STATUS_NAMES.get(code, "?"), code))
+        self.code = code
+
+
+def library(path=LIB):
+    """Loads libhbtg.so (built in-tree by hbtg.build.build_library)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise FileNotFoundError("libhbtg.so not built: run hbtg.build.build_library() (%s)" % path)
+        lib = C.CDLL(path)
+        lib.hbtg_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+        lib.hbtg_destroy.argtypes = [C.c_void_p]
+        lib.hbtg_unbind_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.hbtg_unbind_batch_device.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        lib.hbtg_get_stats.argtypes = [C.c_void_p, C.c_void_p]
+        lib.hbtg_set_count_interactions.argtypes = [C.c_void_p, C.c_int]
+        lib.hbtg_status_string.argtypes = [C.c_int]
+        lib.hbtg_status_string.restype = C.c_char_p
+        lib.hbtg_default_params.argtypes = [C.c_void_p]
+        lib.hbtg_default_params.restype = None
+        for fn in ("hbtg_create", "hbtg_destroy", "hbtg_unbind_batch", "hbtg_unbind_batch_device", "hbtg_get_stats",
+                   "hbtg_set_count_interactions"):
+            getattr(lib, fn).restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+class Unbinder:
+    """One device handle (hbtg_create/hbtg_destroy)."""
+
+    def __init__(self, device=0):
+        self.lib = library()
+        self.h = C.c_void_p()
+        rc = self.lib.hbtg_create(C.byref(self.h), device)
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_create")
+
+    def close(self):
+        if self.h:
+            self.lib.hbtg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def count_interactions(self, enable=True):
+        self.lib.hbtg_set_count_interactions(self.h, int(enable))
+
+    def unbind(self, inp: Inputs, params: Params, want_energy=True, want_potential=False, allow_max_iter=False):
+        """Host-pointer call (hbtg_unbind_batch)."""
+        buf = CallBuffers(inp, want_energy=want_energy, want_potential=want_potential)
+        rc = self.lib.hbtg_unbind_batch(self.h, C.byref(params), C.byref(buf.c))
+        if rc != 0 and not (rc == 4 and allow_max_iter):
+            raise UnbindError(rc, "hbtg_unbind_batch")
+        return buf.out
+
+    def unbind_raw(self, params: Params, cbatch: CBatch):
+        rc = self.lib.hbtg_unbind_batch(self.h, C.byref(params), C.byref(cbatch))
+        if rc != 0 and rc != 4:
+            raise UnbindError(rc, "hbtg_unbind_batch")
+        return rc
+
+    def unbind_device(self, params: Params, cbatch: CBatch, stream_ptr=0):
+        """Device-pointer call (hbtg_unbind_batch_device); cbatch holds device pointers
+        except `offsets` (host)."""
+        rc = self.lib.hbtg_unbind_batch_device(self.h, C.byref(params), C.byref(cbatch), C.c_void_p(stream_ptr))
+        if rc != 0 and rc != 4:
+            raise UnbindError(rc, "hbtg_unbind_batch_device")
+        return rc
+
+    def stats(self):
+        s = CStats()
+        self.lib.hbtg_get_stats(self.h, C.byref(s))
+        return s.as_dict()
+
+
+class DeviceBatch:
+    """Device-resident copy of a batch (torch tensors) and the CBatch pointing at it."""
+
+    def __init__(self, inp: Inputs, device="cuda:0", want_energy=True):
+        import torch
+        t = lambda a, dt=None: torch.from_numpy(np.ascontiguousarray(a)).to(device) if a is not None else None
+        self.offsets = np.ascontiguousarray(inp.offsets, dtype=np.int64)
+        n, ns = inp.n_particles, inp.n_sub
+        self.inp = inp
+        self.pos = t(inp.pos.astype(np.float32))
+        self.vel = t(inp.vel.astype(np.float32))
+        self.mass = t(inp.mass.astype(np.float32))
+        self.u = t(inp.u.astype(np.float32)) if inp.u is not None else None
+        self.id = t(inp.id.astype(np.int64))
+        self.type = t(inp.type.astype(np.uint8)) if inp.type is not None else None
+        self.ref_pos0 = t(inp.ref_pos.astype(np.float32))
+        self.ref_vel0 = t(inp.ref_vel.astype(np.float32))
+        self.mbp0 = t(inp.mostbound_pos.astype(np.float32))
+        self.mbv0 = t(inp.mostbound_vel.astype(np.float32))
+        self.mbid0 = t(inp.most_bound_id.astype(np.int64))
+        z = lambda shape, dt: torch.zeros(shape, dtype=dt, device=device)
+        self.ref_pos, self.ref_vel = z((ns, 3), torch.float32), z((ns, 3), torch.float32)
+        self.mbp, self.mbv = z((ns, 3), torch.float32), z((ns, 3), torch.float32)
+        self.mbid = z(ns, torch.int64)
+        self.order = z(max(n, 1), torch.int64)
+        self.nbound = z(ns, torch.int64)
+        self.mbound = z(ns, torch.float32)
+        self.nbound_type = z((ns, 6), torch.int64)
+        self.mbound_type = z((ns, 6), torch.float32)
+        self.tracer_index = z(ns, torch.int64)
+        self.kin = z((ns, 5), torch.float32)
+        self.core = z((ns, 8), torch.float32)
+        self.energy = z(max(n, 1), torch.float32) if want_energy else None
+        self.iterations = z(ns, torch.int32)
+        self.status = z(ns, torch.int32)
+        p = lambda x: None if x is None else x.data_ptr()
+        self.c = CBatch(ns, self.offsets.ctypes.data, p(self.pos), p(self.vel), p(self.mass), p(self.u), p(self.id),
+                        p(self.type), p(self.ref_pos), p(self.ref_vel), p(self.mbp), p(self.mbv), p(self.mbid),
+                        p(self.order), p(self.nbound), p(self.mbound), p(self.nbound_type), p(self.mbound_type),
+                        p(self.tracer_index), p(self.kin), p(self.core), p(self.energy), None, p(self.iterations),
+                        p(self.status))
+
+    def reset_inout(self):
+        """Restores the in/out frame arrays to the inputs (before each call)."""
+        self.ref_pos.copy_(self.ref_pos0)
+        self.ref_vel.copy_(self.ref_vel0)
+        self.mbp.copy_(self.mbp0)
+        self.mbv.copy_(self.mbv0)
+        self.mbid.copy_(self.mbid0)
+
+    def outputs(self) -> Outputs:
+        c = lambda x: None if x is None else x.cpu().numpy()
+        n = self.inp.n_particles
+        return Outputs(order=c(self.order)[:n], nbound=c(self.nbound), mbound=c(self.mbound),
+                       nbound_type=c(self.nbound_type), mbound_type=c(self.mbound_type),
+                       tracer_index=c(self.tracer_index), kinematics=c(self.kin), core=c(self.core),
+                       energy=None if self.energy is None else c(self.energy)[:n], potential=None,
+                       iterations=c(self.iterations), status=c(self.status), ref_pos=c(self.ref_pos),
+                       ref_vel=c(self.ref_vel), mostbound_pos=c(self.mbp), mostbound_vel=c(self.mbv),
+                       most_bound_id=c(self.mbid))

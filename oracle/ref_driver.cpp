@@ -217,7 +217,10 @@ extern "C" int ref_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthread
     omp_set_max_active_levels(1);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
     for (int64_t s = 0; s < b->n_sub; s++)
+    {
+      omp_set_num_threads(1); /* the inner loops stay serial even when the team has one thread */
       unbind_one(p, b, epoch, s);
+    }
   }
   return HBTG_OK;
 }

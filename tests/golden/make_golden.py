@@ -1,0 +1,63 @@
+"""Generates the golden fixtures of tests/golden/ by running the REFERENCE's
+own Subhalo_t::Unbind (compiled from the reference sources by
+oracle/build_oracle.py into oracle/_ref/) on seeded synthetic inputs.
+
+Run from the repository root where the reference sources are present:
+    python tests/golden/make_golden.py
+Each fixture holds the inputs (prefix in_), the parameters (prefix prm_) and
+the reference outputs (prefix out_).
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "hbt-herons_gb300"))
+
+from hbtg import abi, oracle, synthetic  # noqa: E402
+
+CASES = {
+    "small_dmo": (lambda: synthetic.small_cases(seed=0), dict(dm_only=1, box_size=100.0)),
+    "small_dmo_seed1": (lambda: synthetic.small_cases(seed=1), dict(dm_only=1, box_size=100.0)),
+    "small_hydro": (lambda: synthetic.small_hydro(seed=0), dict(thermal=1, box_size=200.0)),
+    "nfw_10k": (lambda: synthetic.nfw_single(n=10_000, seed=3), dict(dm_only=1, box_size=100.0)),
+    "batched_200": (lambda: synthetic.batched(n_sub=200, seed=4, nmax=4000), dict(dm_only=1, box_size=500.0)),
+}
+
+
+def make(name):
+    gen, kw = CASES[name]
+    inp = gen()
+    prm = abi.parity_params(**kw)
+    out = oracle.run_reference(inp, prm, nthreads=1, want_potential=True)
+    d = {}
+    for k in ("offsets", "pos", "vel", "mass", "id", "type", "u", "ref_pos", "ref_vel", "mostbound_pos",
+              "mostbound_vel", "most_bound_id"):
+        v = getattr(inp, k)
+        if v is not None:
+            d["in_" + k] = v
+    for k, v in prm.as_dict().items():
+        d["prm_" + k] = np.array(v)
+    for k, v in out.__dict__.items():
+        if v is not None:
+            d["out_" + k] = v
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")
+    np.savez_compressed(path, **d)
+    return path
+
+
+def load(path):
+    """Returns (inputs, params, reference outputs) of one fixture."""
+    z = np.load(path)
+    inp = abi.Inputs.load(z, prefix="in_")
+    prm = abi.Params()
+    for k, _ in abi.Params._fields_:
+        setattr(prm, k, z["prm_" + k].item())
+    out = abi.Outputs.load(z, prefix="out_")
+    return inp, prm, out
+
+
+if __name__ == "__main__":
+    for name in CASES:
+        print(make(name), os.path.getsize(os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")))

@@ -1,0 +1,124 @@
+"""Parity metrics between two unbinding results on the same inputs.
+
+Tolerances (stated by the project's correctness contract for the plain GPU
+path against the reference CPU Unbind):
+  * bound-membership mismatch  sum_s |B_s xor B'_s| / sum_s |B'_s| <= 1e-4
+  * total bound mass           relative difference <= 1e-5
+  * per-subhalo status         identical, except where one of the two sits
+                               within one particle of the disruption limit
+  * most-bound particle        identical ID, or a tie: the two candidates'
+                               oracle energies differ by <= ENERGY_TIE_REL*|E|
+  * binding energies           FP32 walk vs FP64 walk: median relative
+                               difference <= 1e-5 on particles bound in both
+"""
+from __future__ import annotations
+
+import numpy as np
+
+MEMBERSHIP_TOL = 1e-4
+MASS_TOL = 1e-5
+ENERGY_TIE_REL = 2e-5
+
+
+def bound_ids(inp, out, s):
+    off = inp.offsets[s]
+    nb = int(out.nbound[s])
+    return inp.id[off + out.order[off:off + nb]]
+
+
+def compare(inp, got, ref):
+    """Returns a dict of parity metrics of `got` against `ref`."""
+    ns = inp.n_sub
+    mism = 0
+    tot_ref = 0
+    worst_sub_rel = 0.0
+    status_diff = []
+    mb_diff = []
+    e_rel = []
+    for s in range(ns):
+        a, b = bound_ids(inp, got, s), bound_ids(inp, ref, s)
+        tot_ref += len(b)
+        if got.status[s] != ref.status[s]:
+            status_diff.append(s)
+        d = len(np.setxor1d(a, b, assume_unique=True))
+        mism += d
+        if len(b):
+            worst_sub_rel = max(worst_sub_rel, d / len(b))
+        if len(a) and len(b):
+            if a[0] != b[0]:
+                mb_diff.append(s)
+            # energies of particles bound in both, by ID
+            off = inp.offsets[s]
+            ea = dict(zip(a.tolist(), got.energy[off:off + len(a)].tolist()))
+            eb = got_e = None
+            common = np.intersect1d(a, b, assume_unique=True)
+            if len(common):
+                eb = dict(zip(b.tolist(), ref.energy[off:off + len(b)].tolist()))
+                ga = np.array([ea[i] for i in common[:2000]])
+                gb = np.array([eb[i] for i in common[:2000]])
+                e_rel.append(np.abs(ga - gb) / np.maximum(np.abs(gb), 1e-30))
+    e_rel = np.concatenate(e_rel) if e_rel else np.zeros(1)
+    m_got = float(np.sum(got.mbound.astype(np.float64)))
+    m_ref = float(np.sum(ref.mbound.astype(np.float64)))
+    return dict(
+        membership=mism / max(tot_ref, 1),
+        worst_sub_membership=worst_sub_rel,
+        mass_rel=abs(m_got - m_ref) / max(m_ref, 1e-30),
+        status_diff=status_diff,
+        mostbound_diff=mb_diff,
+        energy_rel_median=float(np.median(e_rel)),
+        energy_rel_p99=float(np.percentile(e_rel, 99)),
+        nbound_got=int(got.nbound.sum()),
+        nbound_ref=int(ref.nbound.sum()),
+    )
+
+
+def most_bound_is_tie(inp, got, ref, s):
+    """True if the two most-bound particles of subhalo s tie in the ref energies."""
+    off = inp.offsets[s]
+    nb = int(ref.nbound[s])
+    ids_ref = inp.id[off + ref.order[off:off + nb]]
+    e_ref = ref.energy[off:off + nb]
+    gid = inp.id[off + got.order[off]]
+    where = np.nonzero(ids_ref == gid)[0]
+    if not len(where):
+        return False
+    e_min = float(e_ref[0])
+    return abs(float(e_ref[where[0]]) - e_min) <= ENERGY_TIE_REL * abs(e_min)
+
+
+def near_disruption(inp, out, s, params):
+    """A subhalo within a few particles of the MinNumPartOfSub limit."""
+    nb = int(out.nbound[s])
+    return nb <= params.min_num_part + 2
+
+
+def assert_parity(inp, got, ref, params, membership_tol=MEMBERSHIP_TOL, mass_tol=MASS_TOL):
+    m = compare(inp, got, ref)
+    bad_status = [s for s in m["status_diff"]
+                  if not (near_disruption(inp, got, s, params) or near_disruption(inp, ref, s, params))]
+    assert not bad_status, ("status differs", bad_status, got.status[bad_status], ref.status[bad_status])
+    assert m["membership"] <= membership_tol, m
+    assert m["mass_rel"] <= mass_tol, m
+    bad_mb = [s for s in m["mostbound_diff"] if not most_bound_is_tie(inp, got, ref, s)]
+    assert not bad_mb, ("most-bound particle differs beyond a tie", bad_mb)
+    return m
+
+
+def check_invariants(inp, out):
+    """Structural invariants that hold at any size: order is a permutation of
+    each subhalo, bound particles come first with E < 0 sorted ascending,
+    disrupted/empty subhaloes have Nbound = 0 and identity order."""
+    for s in range(inp.n_sub):
+        off, end = inp.offsets[s], inp.offsets[s + 1]
+        n = end - off
+        o = out.order[off:end]
+        assert np.array_equal(np.sort(o), np.arange(n)), ("order is not a permutation", s)
+        nb = int(out.nbound[s])
+        if out.status[s] in (1, 2):
+            assert nb == 0
+            assert np.array_equal(o, np.arange(n))
+        else:
+            e = out.energy[off:off + nb]
+            assert np.all(e < 0), ("kept particle with E >= 0", s)
+            assert np.all(np.diff(e) >= 0), ("bound set not sorted by energy", s)

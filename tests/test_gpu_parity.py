@@ -1,0 +1,148 @@
+"""GPU parity: libhbtg.so (through its C ABI) against the CPU oracle and the
+reference golden fixtures, at sizes the oracle finishes in seconds, plus
+size-independent invariants at larger sizes."""
+import ctypes as C
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from hbtg import abi, oracle, synthetic
+from parity import assert_parity, check_invariants, compare
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
+
+
+def _load_golden(path):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(path), "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.load(path)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_gpu_matches_reference_golden(unbinder, path):
+    inp, prm, ref = _load_golden(path)
+    got = unbinder.unbind(inp, prm)
+    check_invariants(inp, got)
+    m = assert_parity(inp, got, ref, prm)
+    assert m["energy_rel_median"] < 1e-5, m
+
+
+def test_gpu_small_dmo_vs_oracle(unbinder):
+    inp = synthetic.small_cases(seed=7)
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    got = unbinder.unbind(inp, prm)
+    ref = oracle.run_port(inp, prm)
+    check_invariants(inp, got)
+    assert_parity(inp, got, ref, prm)
+    # empty subhalo conventions
+    empty = np.nonzero(ref.status == abi.SUB_EMPTY)[0]
+    assert np.array_equal(got.tracer_index[empty], ref.tracer_index[empty])
+
+
+def test_gpu_hydro_thermal_vs_oracle(unbinder):
+    inp = synthetic.hydro(seed=5, n_sub=40, nmin=100, nmax=20_000, box=300.0)
+    prm = abi.parity_params(thermal=1, box_size=300.0)
+    got = unbinder.unbind(inp, prm)
+    ref = oracle.run_port(inp, prm)
+    check_invariants(inp, got)
+    m = assert_parity(inp, got, ref, prm)
+    # per-type bound counts and masses
+    assert np.abs(got.nbound_type - ref.nbound_type).sum() <= max(2, 1e-4 * ref.nbound.sum())
+    rel = np.abs(got.mbound_type.sum(0) - ref.mbound_type.sum(0)) / np.maximum(ref.mbound_type.sum(0), 1e-30)
+    assert np.all(rel < 1e-4), rel
+
+
+def test_gpu_nfw_single_1e5(unbinder):
+    inp = synthetic.nfw_single(n=100_000, seed=0)
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    got = unbinder.unbind(inp, prm)
+    ref = oracle.run_port(inp, prm, inner_parallel=True)
+    check_invariants(inp, got)
+    m = assert_parity(inp, got, ref, prm)
+    assert got.iterations[0] == ref.iterations[0] or abs(int(got.nbound[0]) - int(ref.nbound[0])) <= 10
+    np.testing.assert_allclose(got.ref_pos, ref.ref_pos, rtol=0, atol=1e-4)
+    np.testing.assert_allclose(got.ref_vel, ref.ref_vel, rtol=1e-4, atol=1e-3)
+    np.testing.assert_allclose(got.kinematics, ref.kinematics, rtol=1e-3, atol=1e-3)
+
+
+def test_gpu_batched_vs_oracle(unbinder):
+    inp = synthetic.batched(n_sub=3000, seed=11, nmax=100_000)
+    prm = abi.parity_params(dm_only=1, box_size=500.0)
+    got = unbinder.unbind(inp, prm)
+    ref = oracle.run_port(inp, prm)
+    check_invariants(inp, got)
+    assert_parity(inp, got, ref, prm)
+
+
+def test_gpu_device_entry_matches_host_entry(unbinder):
+    torch = pytest.importorskip("torch")
+    from hbtg.gpu import DeviceBatch
+    inp = synthetic.small_cases(seed=2)
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    host = unbinder.unbind(inp, prm)
+    db = DeviceBatch(inp)
+    db.reset_inout()
+    unbinder.unbind_device(prm, db.c, torch.cuda.current_stream().cuda_stream)
+    dev = db.outputs()
+    for k in ("order", "nbound", "status", "mbound", "tracer_index", "iterations", "most_bound_id"):
+        assert np.array_equal(getattr(host, k), getattr(dev, k)), k
+
+
+def test_gpu_deterministic(unbinder):
+    inp = synthetic.batched(n_sub=500, seed=3, nmax=20_000)
+    prm = abi.parity_params(dm_only=1, box_size=500.0)
+    a = unbinder.unbind(inp, prm)
+    b = unbinder.unbind(inp, prm)
+    assert np.array_equal(a.order, b.order)
+    assert np.array_equal(a.energy, b.energy)
+
+
+def test_gpu_max_iterations_status(unbinder):
+    inp = synthetic.small_cases(seed=0)
+    prm = abi.parity_params(dm_only=1, box_size=100.0, max_iterations=1)
+    got = unbinder.unbind(inp, prm, allow_max_iter=True)
+    ref = oracle.run_port(inp, prm)
+    assert np.array_equal(got.status, ref.status)
+    assert np.all(got.iterations <= 1)
+
+
+def test_gpu_invalid_arguments(unbinder):
+    from hbtg.gpu import UnbindError
+    inp = synthetic.small_cases(seed=0)
+    prm = abi.parity_params(dm_only=1, box_size=100.0, softening=-1.0)
+    with pytest.raises(UnbindError) as e:
+        unbinder.unbind(inp, prm)
+    assert e.value.code == 1
+    prm = abi.parity_params(dm_only=1, box_size=100.0, max_sample_size=1000)
+    with pytest.raises(UnbindError) as e:
+        unbinder.unbind(inp, prm)
+    assert e.value.code == 5
+
+
+def test_gpu_invariants_large_batch(unbinder):
+    inp = synthetic.batched(total=3_000_000, seed=21)
+    prm = abi.parity_params(dm_only=1, box_size=500.0)
+    got = unbinder.unbind(inp, prm)
+    big = np.argsort(np.diff(inp.offsets))[-50:]
+    check_invariants(inp.subset(big), _subset_out(got, inp, big))
+    st = unbinder.stats()
+    assert st["total_bound"] == int(got.nbound.sum())
+
+
+def _subset_out(out, inp, subs):
+    rows = np.concatenate([np.arange(inp.offsets[s], inp.offsets[s + 1]) for s in subs])
+    d = {}
+    for k, v in out.__dict__.items():
+        if v is None:
+            d[k] = None
+        elif k in ("order", "energy", "potential"):
+            d[k] = v[rows]
+        else:
+            d[k] = v[subs]
+    return abi.Outputs(**d)

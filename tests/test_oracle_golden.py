@@ -1,0 +1,36 @@
+"""The CPU oracle (oracle/unbind_port.cpp) against the golden fixtures that the
+reference's own Subhalo_t::Unbind produced (tests/golden/make_golden.py).
+The restatement reproduces the reference bit for bit."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from hbtg import oracle
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
+
+
+def _load(path):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(path), "make_golden.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.load(path)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_port_matches_reference_golden(path):
+    inp, prm, ref = _load(path)
+    got = oracle.run_port(inp, prm, nthreads=2, want_potential=True)
+    for k, v in ref.__dict__.items():
+        if v is None:
+            continue
+        g = getattr(got, k)
+        assert np.array_equal(np.asarray(g), np.asarray(v)), (k, np.nonzero(np.asarray(g) != np.asarray(v)))
+
+
+def test_golden_fixtures_present():
+    names = {os.path.basename(p) for p in GOLDEN}
+    assert {"small_dmo.npz", "small_hydro.npz", "nfw_10k.npz", "batched_200.npz"} <= names
