@@ -1,0 +1,371 @@
+"""Benchmark: bound particles per second of batched iterative unbinding on GB300.
+
+Workload (one "step" = one unbinding pass over one batch): the batched plain
+method -- seeded synthetic NFW subhaloes with N_p ~ N^-1.9 on [20, 1e6],
+c ~ logN(ln 8, 0.3), a fraction U(0, 0.5) of each heated to U(1.5, 4) v_esc,
+in a 500-unit periodic box, drawn until the batch holds >= 5e7 particles.
+All subhaloes are unbound in one call.  Inputs are far larger than L2.
+
+Arms
+  (default)          this library.  `value`: device-resident inputs
+                     (hbtg_unbind_batch_device); `e2e`: the host-pointer C-ABI
+                     call (hbtg_unbind_batch) from pinned host buffers, copies
+                     inside the timed region.
+  --impl reference   the reference CPU algorithm on the host cores: the
+                     reference's own Unbind (oracle/_ref) where it was built,
+                     else the project's bit-identical restatement (oracle/),
+                     OpenMP over subhaloes as SubhaloSnapshot_t::RefineParticles.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "hbt-herons_gb300"))
+
+METRIC = "bound particles/s on 1 GB300, learned+batched vs plain GPU at ΔM_bound≤1e-4"
+UNIT = "bound particles/s"
+FLOPS_PER_INTERACTION = 13  # 3 sub, 5 for r^2, 2 opening test, 1 rsqrt, 2 accumulate
+
+
+def workload(total, seed):
+    from hbtg import abi, synthetic
+    inp = synthetic.batched(total=total, seed=seed)
+    prm = abi.parity_params(dm_only=1, box_size=500.0)
+    return inp, prm
+
+
+def cpu_sample(inp, target_particles):
+    """Systematic sample over the size-sorted subhaloes: keeps the N_p distribution."""
+    sizes = np.diff(inp.offsets)
+    frac = min(1.0, target_particles / max(1, inp.n_particles))
+    stride = max(1, int(round(1.0 / frac)))
+    order = np.argsort(sizes, kind="stable")
+    pick = np.sort(order[::stride])
+    return inp.subset(pick), stride
+
+
+def run_cpu(inp, prm, threads):
+    from hbtg import oracle
+    ref = None
+    try:
+        lib = oracle.reference_lib("dmo")
+        if lib is not None:
+            ref = "reference"
+    except Exception:
+        ref = None
+    t0 = time.perf_counter()
+    if ref == "reference":
+        out = oracle.run_reference(inp, prm, nthreads=threads)
+    else:
+        out = oracle.run_port(inp, prm, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return out, dt, ref or "port"
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        loaded = [s for s in sm if s > 0.5 * (max(sm) if sm else 1)]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(loaded)) if loaded else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def bench_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    inp, prm = workload(args.total, args.seed)
+    threads = os.cpu_count() or 1
+    sample, stride = cpu_sample(inp, args.ref_sample)
+    for _ in range(args.warmup):
+        run_cpu(sample, prm, threads)
+    times, bounds, kind = [], [], "port"
+    for _ in range(args.steps):
+        out, dt, kind = run_cpu(sample, prm, threads)
+        times.append(dt)
+        bounds.append(int(out.nbound.sum()))
+    rate = float(np.sum(bounds) / np.sum(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
+        "config": {"workload": "batched NFW subhaloes, N_p~N^-1.9 on [20,1e6], 500-unit box",
+                   "particles": inp.n_particles, "subhaloes": inp.n_sub},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "every %d-th subhalo of the size-sorted batch: %d subhaloes, %d particles" %
+                                   (stride, sample.n_sub, sample.n_particles)},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def bench_gpu(args):
+    import torch
+
+    from hbtg.build import build_library
+    from hbtg.gpu import DeviceBatch, Unbinder, measure_fp32_peak
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    build_library()
+    inp, prm = workload(args.total, args.seed + rank)  # weak scaling: one full batch per GPU
+    u = Unbinder(local)
+    db = DeviceBatch(inp, device="cuda:%d" % local)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        db.reset_inout()
+        u.unbind_device(prm, db.c, stream.cuda_stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    # interactions of one step (counted in an untimed pass)
+    u.count_interactions(True)
+    step()
+    counted = u.stats()
+    u.count_interactions(False)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    ms_walk, walk_launches, launches, bound = 0.0, 0, 0, 0
+    with Clocks(local) as clk:
+        barrier()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+            s = u.stats()
+            ms_walk += s["ms_walk"]
+            walk_launches += s["walk_launches"]
+            launches += s["kernel_launches"]
+            bound += s["total_bound"]
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    clocks = clk.summary()
+    t_max = ms
+    bound_all = bound
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+        b = torch.tensor([bound], device="cuda", dtype=torch.float64)
+        dist.all_reduce(b)
+        bound_all = float(b.item())
+    value = bound_all / (t_max * 1e-3)
+
+    # end to end: host buffers (pinned), copies inside the timed region
+    from hbtg.abi import CallBuffers
+    pinned = {}
+
+    def pin(a):
+        if a is None:
+            return None
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        arr = t.numpy()
+        arr[...] = a
+        pinned[id(arr)] = t
+        return arr
+
+    from hbtg.abi import Inputs
+    hin = Inputs(inp.offsets, pin(inp.pos), pin(inp.vel), pin(inp.mass), pin(inp.id), None, None,
+                 pin(inp.ref_pos), pin(inp.ref_vel), pin(inp.mostbound_pos), pin(inp.mostbound_vel),
+                 pin(inp.most_bound_id))
+    buf = CallBuffers(hin, want_energy=True)
+    for name in ("order", "energy", "nbound", "mbound", "tracer_index", "iterations", "status", "kinematics", "core",
+                 "nbound_type", "mbound_type"):
+        setattr(buf.out, name, pin(getattr(buf.out, name)))
+    buf = _rebind(buf)
+    u.unbind_raw(prm, buf.c)  # warm the host path once
+    e2e_times, h2d, d2h = [], 0, 0
+    for _ in range(args.steps):
+        _reset_frames(buf, hin)
+        barrier()
+        t0 = time.perf_counter()
+        u.unbind_raw(prm, buf.c)
+        e2e_times.append(time.perf_counter() - t0)
+        s = u.stats()
+        h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+    t_e2e = float(np.mean(e2e_times))
+    if world > 1:
+        t_e2e = _max_over_ranks(t_e2e)
+    e2e_value = (bound_all / args.steps) / t_e2e
+
+    # roofline of the dominant kernel (the tree walk)
+    peak = measure_fp32_peak(local)
+    walk_ms_per_launch = ms_walk / max(1, walk_launches)
+    flops_per_launch = counted["interactions"] * FLOPS_PER_INTERACTION / max(1, counted["walk_launches"])
+    achieved = flops_per_launch / (walk_ms_per_launch * 1e-3) / 1e12
+    traffic = _walk_traffic(counted)
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        sample, stride = cpu_sample(inp, args.cpu_sample)
+        threads = os.cpu_count() or 1
+        out, dt, kind = run_cpu(sample, prm, threads)
+        cpu = {"value": float(out.nbound.sum() / dt), "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": "every %d-th subhalo of the size-sorted batch: %d subhaloes, %d particles, %.1f s" %
+                         (stride, sample.n_sub, sample.n_particles, dt)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (walk) / f64 (reductions)",
+            "data": "synthetic (seeded NFW subhaloes)",
+            "config": {"workload": "batched plain method: NFW subhaloes N_p~N^-1.9 on [20,1e6] drawn to >=%.0e "
+                                   "particles, 500-unit periodic box" % args.total,
+                       "particles_per_gpu": inp.n_particles, "subhaloes_per_gpu": inp.n_sub,
+                       "bound_per_gpu_step": bound / args.steps, "open_angle": 0.45, "softening": 0.005,
+                       "bound_mass_precision": 0.995, "max_sample_size": 0,
+                       "l2": "inputs larger than L2 (%.1f GB of particle data)" % (inp.n_particles * 44 / 1e9),
+                       "global_iterations": counted["global_iterations"],
+                       "interactions_per_step": counted["interactions"], "parallelism": "dp%d" % world},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches // args.steps,
+            "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": "FP32 FMA throughput measured in-process (hbtg_measure_fp32_peak)",
+                         "flops_per_launch": flops_per_launch, "ms_per_launch": walk_ms_per_launch,
+                         "walk_share_of_step": ms_walk / max(ms, 1e-9)},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    u.close()
+    return 0
+
+
+def _rebind(buf):
+    from hbtg.abi import _ptr
+    o = buf.out
+    c = buf.c
+    c.order, c.energy, c.nbound, c.mbound = _ptr(o.order), _ptr(o.energy), _ptr(o.nbound), _ptr(o.mbound)
+    c.tracer_index, c.iterations, c.status = _ptr(o.tracer_index), _ptr(o.iterations), _ptr(o.status)
+    c.kinematics, c.core, c.nbound_type, c.mbound_type = _ptr(o.kinematics), _ptr(o.core), _ptr(o.nbound_type), \
+        _ptr(o.mbound_type)
+    return buf
+
+
+def _reset_frames(buf, hin):
+    buf.out.ref_pos[...] = hin.ref_pos
+    buf.out.ref_vel[...] = hin.ref_vel
+    buf.out.mostbound_pos[...] = hin.mostbound_pos
+    buf.out.mostbound_vel[...] = hin.mostbound_vel
+    buf.out.most_bound_id[...] = hin.most_bound_id
+
+
+def _max_over_ranks(x):
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _walk_traffic(counted):
+    """DRAM bytes per walk launch from the committed ncu summary of k_walk,
+    scaled from the captured case to this one by interactions per launch."""
+    path = os.path.join(HERE, "profiles", "k_walk_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    per_interaction = d["dram_bytes_per_launch"] / max(1.0, d["interactions_per_launch"])
+    return per_interaction * counted["interactions"] / max(1, counted["walk_launches"])
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--total", type=float, default=5e7, help="particles per batch")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--cpu-sample", type=float, default=1e6, help="particles in the CPU baseline sample")
+    ap.add_argument("--ref-sample", type=float, default=4e5, help="particles per reference-arm step")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    args.total = int(args.total)
+    args.cpu_sample = int(args.cpu_sample)
+    args.ref_sample = int(args.ref_sample)
+    if args.impl == "reference":
+        return bench_reference(args)
+    return bench_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -40,11 +40,22 @@ def library(path=LIB):
         lib.hbtg_status_string.restype = C.c_char_p
         lib.hbtg_default_params.argtypes = [C.c_void_p]
         lib.hbtg_default_params.restype = None
+        lib.hbtg_measure_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+        lib.hbtg_measure_fp32_peak.restype = C.c_int
         for fn in ("hbtg_create", "hbtg_destroy", "hbtg_unbind_batch", "hbtg_unbind_batch_device", "hbtg_get_stats",
                    "hbtg_set_count_interactions"):
             getattr(lib, fn).restype = C.c_int
         _lib = lib
     return _lib
+
+
+def measure_fp32_peak(device=0):
+    """FP32 FMA throughput of the device (TFLOP/s), measured by a kernel of the library."""
+    v = C.c_double()
+    rc = library().hbtg_measure_fp32_peak(device, C.byref(v))
+    if rc != 0:
+        raise UnbindError(rc, "hbtg_measure_fp32_peak")
+    return v.value
 
 
 class Unbinder:

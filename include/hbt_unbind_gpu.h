@@ -174,6 +174,10 @@ const char *hbtg_status_string(int status);
  * and a=1, Hz=0, G=43.0071 (src/config_parser.cpp:200 with default units). */
 void hbtg_default_params(hbtg_params *params);
 
+/* Measurement utility, no counterpart in the reference: FP32 FMA throughput
+ * of the device in TFLOP/s (the roofline denominator of the tree walk). */
+int hbtg_measure_fp32_peak(int device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif
