@@ -29,6 +29,9 @@
 
 namespace hbtg
 {
+// Internal linkage: each translation unit that launches these kernels gets its own copy.
+namespace
+{
 
 // Values of HBTConfig / Cosmology as the reference stores them (HBTReal = float).
 struct KParams
@@ -986,4 +989,5 @@ __global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs
   }
 }
 
+} // namespace
 } // namespace hbtg

@@ -1,0 +1,423 @@
+// noalloc.cu - hbtg_unbind_batch_noalloc: the batched unbinding for callers
+// that cannot allocate GPU memory.
+//
+// Who needs this: code that runs where cudaMalloc is not allowed or not
+// wanted -- inside a host callback or another library's allocation-free
+// section, in a process whose device memory is owned by a pool it must not
+// grow, or on a latency path where an allocation (which can synchronise the
+// device) is unacceptable.  Such callers pass device inputs and outputs as
+// for hbtg_unbind_batch_device; every working buffer (particle copies, keys,
+// sort buffers, tree nodes, per-subhalo state) comes from one file-scope
+// device array, g_noalloc_scratch, that the library reserves when it is
+// loaded and keeps on every GPU that loads it until the process exits.
+//
+// Limits: at most kNoAllocMaxParticles particles and kNoAllocMaxSubhaloes
+// subhaloes per call, and at most kNoAllocMaxRecords tree records (leaves
+// plus cells) in one iteration; larger calls are rejected with
+// HBTG_ERR_INVALID (sizes) or HBTG_ERR_NOMEM (tree larger than the reserve,
+// found mid-run; the outputs are then not written).
+//
+// Sharing: every call on a device uses the same array and leaves its contents
+// behind; each call initialises what it reads before reading it.  Calls whose
+// GPU work overlaps (two host threads, or two streams) race on the array and
+// must be serialised by the caller.
+//
+// Set-up: the first call on each device looks up the array's device address
+// with cudaGetSymbolAddress while that device is current (host code cannot
+// use the array's name as a device pointer).  Make that first call before
+// any stream capture begins.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/hbt_unbind_gpu.h"
+#include "common.cuh"
+#include "kernels.cuh"
+#include "primitives.cuh"
+
+using namespace hbtg;
+
+namespace
+{
+
+constexpr long long kNoAllocMaxParticles = 1LL << 16; // 65,536
+constexpr int kNoAllocMaxSubhaloes = 8192;
+constexpr long long kNoAllocMaxRecords = 3 * kNoAllocMaxParticles;
+
+constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte size of every carve-out, in carving order.
+constexpr size_t kN1 = (size_t)kNoAllocMaxParticles + 1;
+constexpr size_t kS1 = (size_t)kNoAllocMaxSubhaloes + 1;
+constexpr size_t kTable = (size_t)256 * ((kNoAllocMaxParticles + kRadixTile - 1) / kRadixTile);
+constexpr size_t kScanScr = 2 * (kN1 + kTable) / 64 + 4096; // > scan_scratch_elems<int> of any scan here
+constexpr size_t kD4Scr = 2 * kN1 / 256 + 256;              // > scan_scratch_elems<D4>(N)
+constexpr size_t kScratchBytes =
+  al(sizeof(long long) * kS1) +              // offsets
+  2 * al(sizeof(float4) * kN1) +             // pm, vu
+  al(kN1) +                                  // ty
+  5 * al(sizeof(int) * kN1) +                // seg_of, ord, ord_tmp, + Ep, pot (4 bytes each)
+  21 * al(sizeof(int) * kS1) +               // per-subhalo ints
+  al(sizeof(float) * 8 * kS1) +              // old frame, mbound
+  al(sizeof(unsigned) * 6 * kS1) +           // bounding boxes
+  al(sizeof(double) * 4 * kS1) +             // root cubes
+  al(sizeof(double) * 7 * kS1) +             // frame sums
+  2 * al(sizeof(unsigned long long) * kN1) + // key, key_alt
+  4 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt
+  4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
+  al(sizeof(D4) * kN1) +                     // prefix sums
+  al(sizeof(NodeRec) * kNoAllocMaxRecords) + // tree records
+  al(sizeof(int) * kTable) +                 // radix table
+  al(sizeof(int) * kScanScr) +               // scan scratch
+  al(sizeof(D4) * kD4Scr) +                  // D4 scan scratch
+  al(sizeof(unsigned long long));            // interaction counter
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_setup_mutex;
+unsigned char *g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (looked up once).
+int scratch_address(int device, unsigned char **out)
+{
+  if (device < 0 || device >= kMaxDevices)
+    return HBTG_ERR_NO_DEVICE;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  if (!g_scratch_addr[device])
+  {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+    {
+      cudaGetLastError();
+      return HBTG_ERR_CUDA;
+    }
+    g_scratch_addr[device] = static_cast<unsigned char *>(p);
+  }
+  *out = g_scratch_addr[device];
+  return HBTG_OK;
+}
+
+struct Carver
+{
+  unsigned char *base;
+  size_t used = 0;
+  bool overflow = false;
+  template <typename T>
+  T *take(size_t count)
+  {
+    const size_t bytes = al(sizeof(T) * std::max<size_t>(count, 1));
+    if (used + bytes > kScratchBytes)
+    {
+      overflow = true;
+      return nullptr;
+    }
+    T *p = reinterpret_cast<T *>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+struct Fail
+{
+  int code;
+};
+
+inline void ck(cudaError_t e)
+{
+  if (e != cudaSuccess)
+    throw Fail{HBTG_ERR_CUDA};
+}
+
+inline unsigned nblocks(long long n, int threads)
+{
+  return (unsigned)std::max<long long>(1, (n + threads - 1) / threads);
+}
+
+struct NoAllocRun
+{
+  cudaStream_t st;
+  KParams K;
+  DevState D;
+  int S;
+  int seg_bits;
+  int *table, *scan_scr;
+  D4 *d4_scr;
+  int64_t launches = 0;
+
+  void check() { ck(cudaGetLastError()); }
+
+  int read_int(const int *d)
+  {
+    int h = 0;
+    ck(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ck(cudaStreamSynchronize(st));
+    return h;
+  }
+
+  int scan_counts(const int *cnt, int *offs, long long n)
+  {
+    scan<int, false>(cnt, offs, n + 1, scan_scr, st, &launches);
+    check();
+    return read_int(offs + n);
+  }
+
+  template <typename Kt>
+  uint32_t *segmented_sort(Kt *keys, Kt *keys_alt, int key_bits, int total)
+  {
+    bool flip = radix_sort_pairs<Kt>(keys, D.val, keys_alt, D.val_alt, total, 0, key_bits, table, scan_scr, st,
+                                     &launches);
+    uint32_t *v = flip ? D.val_alt : D.val;
+    uint32_t *v_other = flip ? D.val : D.val_alt;
+    if (S > 1 && seg_bits > 0)
+    {
+      k_segkeys<<<nblocks(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
+      bool f2 = radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scan_scr, st,
+                                           &launches);
+      v = f2 ? v_other : v;
+    }
+    check();
+    return v;
+  }
+
+  void iterate()
+  {
+    const unsigned sb = nblocks(S + 1, 256);
+    for (;;)
+    {
+      k_plan<<<sb, 256, 0, st>>>(D);
+      check();
+      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
+      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
+      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
+      if (part_total == 0 && src_total == 0)
+        break;
+      if (src_total > 0)
+      {
+        k_bbox<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
+        k_root<<<sb, 256, 0, st>>>(D, K);
+        k_keys<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
+        check();
+        uint32_t *sorted = segmented_sort<unsigned long long>(D.key, D.key_alt, 63, src_total);
+        if (sorted != D.val)
+          ck(cudaMemcpyAsync(D.val, sorted, sizeof(uint32_t) * src_total, cudaMemcpyDeviceToDevice, st));
+        k_keys_again<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
+        k_tree_count<<<nblocks(src_total + 1, 256), 256, 0, st>>>(D, src_total);
+        check();
+        const int internal = scan_counts(D.cnt, D.X, src_total);
+        if ((long long)src_total + internal > kNoAllocMaxRecords)
+          throw Fail{HBTG_ERR_NOMEM}; // tree larger than the reserve
+        k_prefix_prep<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
+        scan<D4, true>(D.P, D.P, src_total, d4_scr, st, &launches);
+        k_tree_emit<<<nblocks(src_total, 128), 128, 0, st>>>(D, K, src_total);
+        check();
+      }
+      if (chunk_total > 0)
+      {
+        k_walk<<<nblocks(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+        check();
+      }
+      if (part_total > 0)
+      {
+        k_energy<<<nblocks(part_total, 256), 256, 0, st>>>(D, K, part_total);
+        k_part_flags<<<nblocks(part_total + 1, 256), 256, 0, st>>>(D, part_total);
+        check();
+        scan<int, false>(D.flags, D.F, part_total + 1, scan_scr, st, &launches);
+        k_part_count<<<sb, 256, 0, st>>>(D);
+        k_part_scatter<<<nblocks(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_part_copy<<<nblocks(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_after_part<<<sb, 256, 0, st>>>(D, K);
+        check();
+        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
+        if (tail_total > 0)
+        {
+          k_energy_keys<<<nblocks(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
+          uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, tail_total);
+          k_energy_write<<<nblocks(tail_total, 256), 256, 0, st>>>(D, sorted, D.tail_off, tail_total, 0);
+          check();
+        }
+        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
+        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
+        if (bound_total > 0)
+          k_com<<<nblocks(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
+        k_control<<<sb, 256, 0, st>>>(D, K);
+        check();
+      }
+    }
+    k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
+    const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);
+    if (fin_total > 0)
+    {
+      k_energy_keys<<<nblocks(fin_total, 256), 256, 0, st>>>(D, D.fin_off, fin_total, 1);
+      uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, fin_total);
+      k_energy_write<<<nblocks(fin_total, 256), 256, 0, st>>>(D, sorted, D.fin_off, fin_total, 1);
+      check();
+    }
+  }
+};
+
+KParams noalloc_kparams(const hbtg_params *p)
+{
+  KParams K;
+  K.box = (float)p->box_size;
+  K.half = (float)((double)K.box / 2.);
+  K.periodic = p->periodic != 0;
+  K.soft = (float)p->softening;
+  K.h = (float)(2.8 * (double)K.soft);
+  K.h_inv = (float)(1.0 / (2.8 * (double)K.soft));
+  K.res = (float)p->tree_node_resolution;
+  const float theta = (float)p->open_angle;
+  K.theta2 = theta * theta;
+  K.bmp = (float)p->bound_mass_precision;
+  K.min_part = (int)p->min_num_part;
+  K.min_tracer = (int)p->min_num_tracer;
+  K.tracer_mask = p->tracer_type_mask;
+  K.dm_only = p->dm_only != 0;
+  K.thermal = p->thermal != 0;
+  K.G_over_a = (float)((double)(float)p->G / (double)(float)p->scale_factor);
+  K.a = (float)p->scale_factor;
+  K.hz = (float)p->hubble;
+  K.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
+  K.core_min = p->sub_core_size_min;
+  K.core_factor = (float)p->sub_core_size_factor;
+  K.count_interactions = 0;
+  return K;
+}
+
+int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
+{
+  if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
+    return HBTG_ERR_INVALID;
+  if (p->max_sample_size > 0)
+    return HBTG_ERR_UNSUPPORTED;
+  if (!(p->softening > 0) || !(p->open_angle > 0) || !(p->box_size > 0))
+    return HBTG_ERR_INVALID;
+  const long long S = b->n_sub;
+  if (S == 0)
+    return HBTG_OK;
+  if (S > kNoAllocMaxSubhaloes || b->offsets[0] != 0)
+    return HBTG_ERR_INVALID;
+  for (long long s = 0; s < S; s++)
+    if (b->offsets[s + 1] < b->offsets[s])
+      return HBTG_ERR_INVALID;
+  const long long N = b->offsets[S];
+  if (N > kNoAllocMaxParticles)
+    return HBTG_ERR_INVALID; // larger than the static reserve
+  if (N > 0 && (!b->pos || !b->vel || !b->mass || !b->id || !b->order))
+    return HBTG_ERR_INVALID;
+  if (!b->ref_pos || !b->ref_vel || !b->mostbound_pos || !b->mostbound_vel || !b->most_bound_id || !b->nbound ||
+      !b->mbound || !b->tracer_index || !b->iterations || !b->status)
+    return HBTG_ERR_INVALID;
+
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess)
+    return HBTG_ERR_NO_DEVICE;
+  unsigned char *base = nullptr;
+  int rc = scratch_address(device, &base);
+  if (rc != HBTG_OK)
+    return rc;
+
+  NoAllocRun R;
+  R.st = st;
+  R.K = noalloc_kparams(p);
+  R.S = (int)S;
+  int bits = 0;
+  while ((1LL << bits) < S)
+    bits++;
+  R.seg_bits = bits;
+  Carver c{base};
+  DevState &D = R.D;
+  D.S = (int)S;
+  D.N = N;
+  long long *off = c.take<long long>(kS1);
+  D.off = off;
+  D.pm = c.take<float4>(kN1);
+  D.vu = c.take<float4>(kN1);
+  D.ty = c.take<uint8_t>(kN1);
+  D.seg_of = c.take<int>(kN1);
+  D.ord = c.take<int>(kN1);
+  D.ord_tmp = c.take<int>(kN1);
+  D.Ep = c.take<float>(kN1);
+  D.pot = c.take<float>(kN1);
+  int **ints[] = {&D.n_s, &D.nbound, &D.nlast, &D.state, &D.corr, &D.iter, &D.wrap, &D.tracers, &D.nb_new,
+                  &D.src_begin, &D.src_cnt, &D.src_off, &D.tgt_cnt, &D.chunk_cnt, &D.chunk_off, &D.part_cnt,
+                  &D.part_off, &D.tail_cnt, &D.tail_off, &D.fin_cnt, &D.fin_off};
+  for (int **pp : ints)
+    *pp = c.take<int>(kS1);
+  float *subf = c.take<float>(8 * kS1);
+  D.old_pos = subf;
+  D.old_vel = subf + 3 * kS1;
+  D.mbound = subf + 6 * kS1;
+  unsigned *bb = c.take<unsigned>(6 * kS1);
+  D.bb_lo = bb;
+  D.bb_hi = bb ? bb + 3 * kS1 : nullptr;
+  D.root = c.take<double>(4 * kS1);
+  D.com = c.take<double>(7 * kS1);
+  D.key = c.take<unsigned long long>(kN1);
+  D.key_alt = c.take<unsigned long long>(kN1);
+  D.val = c.take<uint32_t>(kN1);
+  D.val_alt = c.take<uint32_t>(kN1);
+  D.k32 = c.take<uint32_t>(kN1);
+  D.k32_alt = c.take<uint32_t>(kN1);
+  D.cnt = c.take<int>(kN1);
+  D.X = c.take<int>(kN1);
+  D.flags = c.take<int>(kN1);
+  D.F = c.take<int>(kN1);
+  D.P = c.take<D4>(kN1);
+  D.nodes = c.take<NodeRec>(kNoAllocMaxRecords);
+  R.table = c.take<int>(kTable);
+  R.scan_scr = c.take<int>(kScanScr);
+  R.d4_scr = c.take<D4>(kD4Scr);
+  D.interactions = c.take<unsigned long long>(1);
+  if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr ||
+      (size_t)scan_scratch_elems<D4>(kN1) > kD4Scr)
+    return HBTG_ERR_NOMEM; // layout does not fit the reserve (cannot happen with the constants above)
+  D.ref_pos = b->ref_pos;
+  D.ref_vel = b->ref_vel;
+  D.mb_pos = b->mostbound_pos;
+  D.mb_vel = b->mostbound_vel;
+  D.mb_id = reinterpret_cast<long long *>(b->most_bound_id);
+  D.id = reinterpret_cast<const long long *>(b->id);
+
+  try
+  {
+    ck(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
+    ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+    if (N > 0)
+      k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
+    k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D);
+    R.check();
+    R.iterate();
+    OutPtrs O;
+    O.order = reinterpret_cast<long long *>(b->order);
+    O.nbound = reinterpret_cast<long long *>(b->nbound);
+    O.nbound_type = reinterpret_cast<long long *>(b->nbound_type);
+    O.tracer_index = reinterpret_cast<long long *>(b->tracer_index);
+    O.most_bound_id = reinterpret_cast<long long *>(b->most_bound_id);
+    O.mbound = b->mbound;
+    O.mbound_type = b->mbound_type;
+    O.kinematics = b->kinematics;
+    O.core = b->core;
+    O.energy = b->energy;
+    O.potential = b->potential;
+    O.iterations = b->iterations;
+    O.status = b->status;
+    k_epilogue<<<(unsigned)std::min<long long>(S, 65535), 256, 0, st>>>(D, R.K, O);
+    R.check();
+    ck(cudaStreamSynchronize(st));
+  }
+  catch (Fail &f)
+  {
+    cudaGetLastError();
+    return f.code;
+  }
+  return HBTG_OK;
+}
+
+} // namespace
+
+extern "C" int hbtg_unbind_batch_noalloc(const hbtg_params *params, hbtg_batch *batch, void *cuda_stream)
+{
+  return noalloc_call(params, batch, static_cast<cudaStream_t>(cuda_stream));
+}

@@ -174,6 +174,18 @@ const char *hbtg_status_string(int status);
  * and a=1, Hz=0, G=43.0071 (src/config_parser.cpp:200 with default units). */
 void hbtg_default_params(hbtg_params *params);
 
+/* Unbinding for callers that cannot allocate GPU memory; no counterpart in
+ * the reference.  Same contract as hbtg_unbind_batch_device (device arrays,
+ * host offsets, work queued on `cuda_stream`, synchronised before return) but
+ * it needs no handle and calls no allocator: its working memory is a fixed
+ * reserve of about 17 MiB inside the library, held on every GPU that loads it
+ * until the process exits.  Limits: at most 65,536 particles and 8,192
+ * subhaloes per call (else HBTG_ERR_INVALID) and at most 196,608 tree records
+ * per iteration (else HBTG_ERR_NOMEM, outputs unwritten).  The first call on a
+ * device resolves the reserve's device address; make it before any stream
+ * capture.  All calls share the reserve: calls that overlap on the GPU race. */
+int hbtg_unbind_batch_noalloc(const hbtg_params *params, hbtg_batch *batch, void *cuda_stream);
+
 /* Measurement utility, no counterpart in the reference: FP32 FMA throughput
  * of the device in TFLOP/s (the roofline denominator of the tree walk). */
 int hbtg_measure_fp32_peak(int device, double *tflops);
