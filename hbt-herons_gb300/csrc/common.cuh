@@ -47,16 +47,14 @@ __device__ __forceinline__ double nearest_d(double x, double half, double box)
   return x > half ? x - box : (x < -half ? x + box : x);
 }
 
-// One node of a packed octree in depth-first preorder.  Leaves are the
-// particles themselves (crit = 0 so they are never opened).  A node's first
-// child is the next record; `skip` is the index just past its subtree.
-struct __align__(16) NodeRec
-{
-  float4 xyzm; // centre of mass and mass
-  float crit;  // open the node when r^2 < crit  (crit = len^2 / theta^2)
-  int skip;    // first record after this subtree
-  int pad0, pad1;
-};
+// The octree is an array of 16-byte slots in depth-first preorder.
+//   leaf (a particle): one slot  (x, y, z, m),             m >= 0 (sign bit clear)
+//   cell:              two slots (x, y, z, -crit) (m, skip_bits, 0, 0)
+// The sign bit of w marks a cell; crit = len^2 / theta^2 (open when r^2 < crit);
+// skip (an int stored in the float's bits) is the first slot after the
+// subtree.  A cell's first child starts two slots after it.  The walk reads
+// the second slot of a cell only when it accepts the cell.
+__device__ __forceinline__ bool slot_is_cell(float w) { return (__float_as_uint(w) & 0x80000000u) != 0; }
 
 // Per-subhalo status while iterating.
 enum SubState : int

@@ -83,7 +83,7 @@ struct DevState
   uint32_t *val, *val_alt, *k32, *k32_alt;
   int *cnt, *X, *flags, *F;
   D4 *P;
-  NodeRec *nodes;
+  float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
 };
 
@@ -331,8 +331,8 @@ __global__ void k_prefix_prep(DevState D, int total)
 }
 
 // Writes the particle leaf and the cells that start at item j, in preorder.
-// Record index: leaf of item j = j + X[j] + cnt[j]; cell (j, level lo+t) =
-// j + X[j] + t.  A cell's subtree ends after the leaf of its last particle.
+// Slot index: cell (j, level lo+t) = j + 2 X[j] + 2t; leaf of item j =
+// j + 2 X[j] + 2 cnt[j].  A cell's subtree ends after its last particle's leaf.
 __global__ void k_tree_emit(DevState D, KParams K, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,15 +343,10 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   int lo, hi;
   cell_levels(D, j, i, m, lo, hi);
   const int c = hi >= lo ? hi - lo + 1 : 0;
-  const int base = j + D.X[j];
+  const int base = j + 2 * D.X[j];
   const int p = (int)D.val[j];
   const float4 x = D.pm[p];
-  NodeRec leaf;
-  leaf.xyzm = x;
-  leaf.crit = 0.f;
-  leaf.skip = base + c + 1;
-  leaf.pad0 = leaf.pad1 = 0;
-  D.nodes[base + c] = leaf;
+  D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(x.w));
   if (c == 0)
     return;
   const double *r = D.root + 4 * s;
@@ -387,22 +382,22 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
       len = (len >= (double)K.res) ? 0.5 * len : len;
     const float lenf = (float)len;
     const float len2 = lenf * lenf;
-    NodeRec nd;
-    nd.xyzm = make_float4((float)(r[0] + (after.x - before.x) / mass), (float)(r[1] + (after.y - before.y) / mass),
-                          (float)(r[2] + (after.z - before.z) / mass), (float)mass);
-    nd.crit = __fdiv_rn(len2, K.theta2);
-    nd.skip = b + D.X[b] + D.cnt[b] + 1;
-    nd.pad0 = nd.pad1 = 0;
-    D.nodes[base + t] = nd;
+    const float crit = __fdiv_rn(len2, K.theta2);
+    const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
+    D.nodes[base + 2 * t] = make_float4((float)(r[0] + (after.x - before.x) / mass),
+                                        (float)(r[1] + (after.y - before.y) / mass),
+                                        (float)(r[2] + (after.z - before.z) / mass),
+                                        __uint_as_float(__float_as_uint(crit) | 0x80000000u));
+    D.nodes[base + 2 * t + 1] = make_float4((float)mass, __int_as_float(skip), 0.f, 0.f);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Tree walk: one warp evaluates 32 targets of one subhalo.  The warp visits
-// nodes in preorder; each lane applies the reference opening test for its own
-// target.  A lane that accepts a node skips its subtree (it stays idle until
-// the warp reaches the node's skip index); the warp descends when any lane
-// opens, else jumps to the skip index.  FP32 with Kahan-compensated sums.
+// Tree walk: one warp evaluates 32 neighbouring targets (key order) of one
+// subhalo; each lane walks the slots for its own target exactly as the
+// reference's stackless walk (open: next slot; accept: interact, jump to the
+// skip slot), so its interaction list is the reference's.  FP32 with
+// Kahan-compensated accumulation.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float spline_w(float u)
 {
@@ -413,19 +408,17 @@ __device__ __forceinline__ float spline_w(float u)
 }
 
 template <bool Wrap>
-__device__ __forceinline__ void walk_warp(const NodeRec *__restrict__ nodes, int root, float4 x, bool valid,
+__device__ __forceinline__ void walk_lane(const float4 *__restrict__ T, int root, float4 x, bool valid,
                                           float self_mass, const KParams &K, float &out, unsigned long long &cnt)
 {
   float sum = valid ? self_mass / K.soft : 0.f, comp = 0.f;
-  const int end = nodes[root].skip;
-  int idx = root, my_skip = valid ? root : 0x7fffffff;
+  const int end = valid ? __float_as_int(__ldg(&T[root + 1]).y) : root;
   const float h2 = K.h * K.h;
+  int idx = root;
   while (idx < end)
   {
-    const float4 n = __ldg(&nodes[idx].xyzm);
-    const int2 cs = __ldg(reinterpret_cast<const int2 *>(&nodes[idx].crit));
-    const bool active = idx >= my_skip;
-    float dx = n.x - x.x, dy = n.y - x.y, dz = n.z - x.z;
+    const float4 a = __ldg(&T[idx]);
+    float dx = a.x - x.x, dy = a.y - x.y, dz = a.z - x.z;
     if (Wrap)
     {
       dx = nearest_f(dx, K.half, K.box);
@@ -433,25 +426,35 @@ __device__ __forceinline__ void walk_warp(const NodeRec *__restrict__ nodes, int
       dz = nearest_f(dz, K.half, K.box);
     }
     const float r2 = dx * dx + dy * dy + dz * dz;
-    const bool open = active && (r2 < __int_as_float(cs.x));
-    if (active && !open)
+    float m;
+    int next;
+    if (slot_is_cell(a.w))
     {
-      float term;
-      if (r2 >= h2)
-        term = -n.w * rsqrtf(r2);
-      else
+      if (r2 < -a.w) // open: the first child follows the cell's two slots
       {
-        const float r = sqrtf(r2);
-        term = n.w * K.h_inv * spline_w(r * K.h_inv);
+        idx += 2;
+        continue;
       }
-      const float y = term - comp;
-      const float t = sum + y;
-      comp = (t - sum) - y;
-      sum = t;
-      my_skip = cs.y;
-      cnt++;
+      const float2 b = __ldg(reinterpret_cast<const float2 *>(&T[idx + 1]));
+      m = b.x;
+      next = __float_as_int(b.y);
     }
-    idx = __any_sync(0xffffffffu, open) ? idx + 1 : max(cs.y, idx + 1); // strictly increasing
+    else
+    {
+      m = a.w;
+      next = idx + 1;
+    }
+    float term;
+    if (r2 >= h2)
+      term = -m * rsqrtf(r2);
+    else
+      term = m * K.h_inv * spline_w(sqrtf(r2) * K.h_inv);
+    const float y = term - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+    cnt++;
+    idx = max(next, idx + 1); // strictly increasing
   }
   out = sum - comp;
 }
@@ -472,14 +475,14 @@ __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_c
     if (valid)
       p = corr ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t];
     const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int root = D.src_off[s] + D.X[D.src_off[s]];
+    const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
     float phi = 0.f;
     if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
       ;
     else if (D.wrap[s])
-      walk_warp<true>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+      walk_lane<true>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
     else
-      walk_warp<false>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+      walk_lane<false>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
     if (valid)
       D.pot[p] = phi * K.G_over_a;
   }
@@ -820,6 +823,9 @@ __global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs
       O.order[off + k] = (st == kConverged || st == kMaxIter) ? (long long)D.ord[off + k] - off : (long long)k;
     // per-particle outputs and sums over the bound set
     double Et = 0., Kk = 0., L0 = 0., L1 = 0., L2 = 0., Ms = 0.;
+    int my_type_n[6] = {0, 0, 0, 0, 0, 0};
+    double my_type_m[6] = {0., 0., 0., 0., 0., 0.};
+    int my_first_tracer = 0x7fffffff;
     const float *rp = D.ref_pos + 3 * s, *rv = D.ref_vel + 3 * s;
     for (int k = threadIdx.x; k < nb; k += blockDim.x)
     {
@@ -852,11 +858,27 @@ __global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs
       L2 += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
       Ms += m;
       const uint8_t t = D.ty[p];
-      atomicAdd(&s_type_n[t & 7], 1);
-      atomicAdd(&s_type_m[t & 7], (double)m);
-      if (is_tracer_bits(t))
-        atomicMin(&s_first_tracer, k);
+#pragma unroll
+      for (int q = 0; q < 6; q++)
+        if ((t & 7) == q)
+        {
+          my_type_n[q]++;
+          my_type_m[q] += (double)m;
+        }
+      if (is_tracer_bits(t) && k < my_first_tracer)
+        my_first_tracer = k;
     }
+    // combine the per-thread partials (shared atomics only once per thread)
+    for (int q = 0; q < 6; q++)
+    {
+      if (my_type_n[q])
+      {
+        atomicAdd(&s_type_n[q], my_type_n[q]);
+        atomicAdd(&s_type_m[q], my_type_m[q]);
+      }
+    }
+    if (my_first_tracer != 0x7fffffff)
+      atomicMin(&s_first_tracer, my_first_tracer);
     Et = block_sum(Et, sh);
     Kk = block_sum(Kk, sh);
     L0 = block_sum(L0, sh);

@@ -66,7 +66,7 @@ constexpr size_t kScratchBytes =
   4 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt
   4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
   al(sizeof(D4) * kN1) +                     // prefix sums
-  al(sizeof(NodeRec) * kNoAllocMaxRecords) + // tree records
+  al(sizeof(float4) * kNoAllocMaxRecords) +  // tree slots
   al(sizeof(int) * kTable) +                 // radix table
   al(sizeof(int) * kScanScr) +               // scan scratch
   al(sizeof(D4) * kD4Scr) +                  // D4 scan scratch
@@ -206,7 +206,7 @@ struct NoAllocRun
         k_tree_count<<<nblocks(src_total + 1, 256), 256, 0, st>>>(D, src_total);
         check();
         const int internal = scan_counts(D.cnt, D.X, src_total);
-        if ((long long)src_total + internal > kNoAllocMaxRecords)
+        if ((long long)src_total + 2LL * internal > kNoAllocMaxRecords)
           throw Fail{HBTG_ERR_NOMEM}; // tree larger than the reserve
         k_prefix_prep<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
         scan<D4, true>(D.P, D.P, src_total, d4_scr, st, &launches);
@@ -365,7 +365,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.flags = c.take<int>(kN1);
   D.F = c.take<int>(kN1);
   D.P = c.take<D4>(kN1);
-  D.nodes = c.take<NodeRec>(kNoAllocMaxRecords);
+  D.nodes = c.take<float4>(kNoAllocMaxRecords);
   R.table = c.take<int>(kTable);
   R.scan_scr = c.take<int>(kScanScr);
   R.d4_scr = c.take<D4>(kD4Scr);

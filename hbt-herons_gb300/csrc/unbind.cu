@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <vector>
@@ -260,10 +261,10 @@ struct Runner
         *launches += 2;
         check();
         const int internal = scan_counts(D.cnt, D.X, src_total);
-        const long long records = (long long)src_total + internal;
+        const long long records = (long long)src_total + 2LL * internal;
         if (records >= (1LL << 31) - 64)
           throw NoMem{};
-        D.nodes = H->pool.get<NodeRec>(S_NODES, (size_t)records);
+        D.nodes = H->pool.get<float4>(S_NODES, (size_t)records);
         H->stats.tree_nodes += internal;
         k_prefix_prep<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
         (*launches)++;
@@ -427,7 +428,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
   D.F = P.get<int>(S_F, n1 + 1);
   D.P = P.get<D4>(S_P, n1);
-  D.nodes = P.get<NodeRec>(S_NODES, n1 * 2);
+  D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
 
