@@ -1,0 +1,235 @@
+// driver.cuh - the lock-step unbinding iteration shared by every entry point.
+//
+// Subhalo_t::Unbind's loop (src/subhalo_unbind.cpp:555-758) run for all
+// subhaloes of a batch at once: each pass of the loop below is one iteration
+// for every subhalo still active; subhaloes leave the active set where the
+// reference breaks out of its loop.  The memory policy `Mem` supplies the
+// working buffers (a grow-only pool, or a fixed static reserve) and turns CUDA
+// errors into exceptions of its own type.
+//
+// Mem must provide:
+//   void check(cudaError_t)                      throws on error
+//   int *scan_scratch(long long n)               scratch for scan<int>(n)
+//   int *radix_table(long long n)                table for radix_sort_pairs(n)
+//   int *radix_scan_scratch(long long n)
+//   D4 *d4_scratch(long long n)                  scratch for scan<D4>(n)
+//   float4 *tree_slots(long long slots)          tree storage (may throw when too large)
+//   void mark(int phase)                         phase boundary for timing (may be a no-op)
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <utility>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "primitives.cuh"
+
+namespace hbtg
+{
+
+inline unsigned grid_for(long long n, int threads)
+{
+  long long b = (n + threads - 1) / threads;
+  return (unsigned)std::max<long long>(1, std::min<long long>(b, 0x7fffffffLL));
+}
+
+template <class Mem>
+struct IterationDriver
+{
+  Mem &mem;
+  cudaStream_t st;
+  KParams K;
+  DevState D;
+  int S = 0;
+  int seg_bits = 0;
+  int sm_count = 152;
+  int64_t launches = 0;
+  int64_t walk_launches = 0;
+  int64_t tree_nodes = 0;
+  int global_iter = 0;
+
+  IterationDriver(Mem &m, cudaStream_t s) : mem(m), st(s) {}
+
+  void check() { mem.check(cudaGetLastError()); }
+
+  int read_int(const int *d)
+  {
+    int h = 0;
+    mem.check(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
+    mem.check(cudaStreamSynchronize(st));
+    return h;
+  }
+
+  // Exclusive scan of n counts plus a trailing zero; returns the total.
+  int scan_counts(const int *cnt, int *offs, long long n)
+  {
+    scan<int, false>(cnt, offs, n + 1, mem.scan_scratch(n + 1), st, &launches);
+    check();
+    return read_int(offs + n);
+  }
+
+  // Sorts (k32, val) of `total` packed items by energy key, then stably by
+  // subhalo; returns the array holding the sorted particles.
+  uint32_t *sort_energy_keys(int total)
+  {
+    int *table = mem.radix_table(total), *scr = mem.radix_scan_scratch(total);
+    const bool flip =
+      radix_sort_pairs<uint32_t>(D.k32, D.val, D.k32_alt, D.val_alt, total, 0, 32, table, scr, st, &launches);
+    uint32_t *v = flip ? D.val_alt : D.val;
+    uint32_t *v_other = flip ? D.val : D.val_alt;
+    if (S > 1 && seg_bits > 0)
+    {
+      k_segkeys<<<grid_for(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
+      launches++;
+      const bool f2 =
+        radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scr, st, &launches);
+      v = f2 ? v_other : v;
+    }
+    check();
+    return v;
+  }
+
+  // Sorts the tree keys by key, then stably by subhalo carrying the keys, and
+  // leaves the result in D.key / D.val.
+  void sort_tree_keys(int total)
+  {
+    int *table = mem.radix_table(total), *scr = mem.radix_scan_scratch(total);
+    const bool flip =
+      radix_sort_pairs<unsigned long long>(D.key, D.val, D.key_alt, D.val_alt, total, 0, 63, table, scr, st,
+                                           &launches);
+    if (flip)
+    {
+      std::swap(D.key, D.key_alt);
+      std::swap(D.val, D.val_alt);
+    }
+    if (S > 1 && seg_bits > 0)
+    {
+      k_segkeys_iota<<<grid_for(total, 256), 256, 0, st>>>(D.val, D.seg_of, D.k32, D.perm, total);
+      launches++;
+      const bool f2 = radix_sort_pairs<uint32_t>(D.k32, D.perm, D.k32_alt, D.perm_alt, total, 0, seg_bits, table,
+                                                 scr, st, &launches);
+      const uint32_t *perm = f2 ? D.perm_alt : D.perm;
+      k_gather_keys<<<grid_for(total, 256), 256, 0, st>>>(D.key, D.val, perm, D.key_alt, D.val_alt, total);
+      launches++;
+      std::swap(D.key, D.key_alt);
+      std::swap(D.val, D.val_alt);
+    }
+    check();
+  }
+
+  void build_tree(int src_total)
+  {
+    const unsigned sb = grid_for(S + 1, 256);
+    mem.check(cudaMemsetAsync(D.fb_count, 0, sizeof(int), st));
+    k_bbox<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    k_root<<<sb, 256, 0, st>>>(D, K);
+    k_keys<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    k_keys_fallback<<<sm_count * 4, 256, 0, st>>>(D);
+    launches += 4;
+    check();
+    sort_tree_keys(src_total);
+    k_tree_count<<<grid_for(src_total + 1, 256), 256, 0, st>>>(D, src_total);
+    launches++;
+    check();
+    const int internal = scan_counts(D.cnt, D.X, src_total);
+    D.nodes = mem.tree_slots((long long)src_total + 2LL * internal);
+    tree_nodes += internal;
+    k_prefix_prep<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    launches++;
+    scan<D4, true>(D.P, D.P, src_total, mem.d4_scratch(src_total), st, &launches);
+    k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
+    launches++;
+    check();
+  }
+
+  void run()
+  {
+    const unsigned sb = grid_for(S + 1, 256);
+    mem.mark(-1);
+    for (;;)
+    {
+      k_plan<<<sb, 256, 0, st>>>(D);
+      launches++;
+      check();
+      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
+      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
+      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
+      mem.mark(0);
+      if (part_total == 0 && src_total == 0)
+        break;
+      global_iter++;
+      if (src_total > 0)
+        build_tree(src_total);
+      mem.mark(2);
+      if (chunk_total > 0)
+      {
+        k_walk<<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+        launches++;
+        walk_launches++;
+        check();
+      }
+      mem.mark(1);
+      if (part_total > 0)
+      {
+        k_energy<<<grid_for(part_total, 256), 256, 0, st>>>(D, K, part_total);
+        k_part_flags<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, part_total);
+        launches += 2;
+        check();
+        scan<int, false>(D.flags, D.F, part_total + 1, mem.scan_scratch(part_total + 1), st, &launches);
+        k_part_count<<<sb, 256, 0, st>>>(D);
+        k_part_scatter<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_part_copy<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+        k_after_part<<<sb, 256, 0, st>>>(D, K);
+        launches += 4;
+        check();
+        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
+        if (tail_total > 0)
+        {
+          k_energy_keys<<<grid_for(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
+          launches++;
+          uint32_t *sorted = sort_energy_keys(tail_total);
+          k_energy_write<<<grid_for(tail_total, 256), 256, 0, st>>>(D, sorted, D.tail_off, tail_total, 0);
+          launches++;
+          check();
+        }
+        mem.mark(3);
+        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
+        launches++;
+        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
+        if (bound_total > 0)
+        {
+          k_com<<<grid_for(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
+          launches++;
+        }
+        k_control<<<sb, 256, 0, st>>>(D, K);
+        launches++;
+        check();
+        mem.mark(4);
+      }
+    }
+    // final sort of the bound sets by binding energy
+    k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
+    launches++;
+    const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);
+    if (fin_total > 0)
+    {
+      k_energy_keys<<<grid_for(fin_total, 256), 256, 0, st>>>(D, D.fin_off, fin_total, 1);
+      launches++;
+      uint32_t *sorted = sort_energy_keys(fin_total);
+      k_energy_write<<<grid_for(fin_total, 256), 256, 0, st>>>(D, sorted, D.fin_off, fin_total, 1);
+      launches++;
+      check();
+    }
+  }
+
+  void epilogue(const OutPtrs &O)
+  {
+    k_epilogue<<<(unsigned)std::min(S, 65535), 256, 0, st>>>(D, K, O);
+    launches++;
+    check();
+    mem.mark(5);
+  }
+};
+
+} // namespace hbtg

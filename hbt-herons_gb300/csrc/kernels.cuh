@@ -77,10 +77,12 @@ struct DevState
   int *tail_cnt, *tail_off, *fin_cnt, *fin_off;
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
   double *root;            // [4S] centre xyz, side length
+  float *keyp;             // [8S] per-axis origin hi/lo, 2^21/side, exact levels (fast key descent)
+  int *fb_list, *fb_count; // packed items whose key needs the exact double descent
   double *com;             // [7S] M, sum m dx, sum m v
   // packed arrays
   unsigned long long *key, *key_alt;
-  uint32_t *val, *val_alt, *k32, *k32_alt;
+  uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
   int *cnt, *X, *flags, *F;
   D4 *P;
   float4 *nodes; // tree slots (see slot_is_cell)
@@ -230,6 +232,24 @@ __global__ void k_root(DevState D, KParams K)
   for (int d = 0; d < 3; d++)
     D.root[4 * s + d] = 0.5 * (hi[d] + lo[d]);
   D.root[4 * s + 3] = len;
+  // fast-descent constants: origin of the root cube per axis as a float pair,
+  // 2^21 / side, and the number of levels that must match the reference
+  // exactly (cells not smaller than TreeNodeResolution, plus one)
+  float *kp = D.keyp + 8 * s;
+  for (int d = 0; d < 3; d++)
+  {
+    const double o = 0.5 * (hi[d] + lo[d]) - 0.5 * len;
+    kp[d] = (float)o;
+    kp[3 + d] = (float)(o - (double)(float)o);
+  }
+  kp[6] = len > 0. ? (float)(2097152.0 / len) : 0.f;
+  int exact_levels = 21;
+  if (K.res > 0.f && len > 0.)
+  {
+    const double lv = floor(log2(len / (double)K.res)) + 2.;
+    exact_levels = lv < 1. ? 1 : (lv > 21. ? 21 : (int)lv);
+  }
+  kp[7] = __int_as_float(exact_levels);
   if (D.iter[s] == 1 && !D.corr[s]) // first iteration: the sources are every particle
     D.wrap[s] = K.periodic && (len > (double)K.half);
 }
@@ -258,15 +278,117 @@ __device__ __forceinline__ unsigned long long descent_key(float4 x, const double
   return key;
 }
 
+// Spreads the low 21 bits of v so that bit i lands on bit 3i.
+__device__ __forceinline__ unsigned long long spread3(unsigned long long v)
+{
+  v &= 0x1fffffULL;
+  v = (v | (v << 32)) & 0x1f00000000ffffULL;
+  v = (v | (v << 16)) & 0x1f0000ff0000ffULL;
+  v = (v | (v << 8)) & 0x100f00f00f00f00fULL;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ULL;
+  v = (v | (v << 2)) & 0x1249249249249249ULL;
+  return v;
+}
+
+// The same key without FP64 arithmetic for almost every particle.  Per axis,
+// the descent selects the 2^21-cell slab (cells left-open, right-closed)
+// containing x: index = ceil(t) - 1 with t = (x - origin) * 2^21 / side.  The
+// float estimate of t is within 0.75 slab widths of the exact value, so the
+// first `exact_levels` digits are exact unless t lies within one slab of a
+// boundary at those levels (or is not finite); then the reference's double
+// descent is used.  Digits below the exact levels only order particles inside
+// cells smaller than the tree resolution, where the reference itself breaks
+// ties at random (src/oct_tree.tpp:108-120).
+// Returns false when the float estimate cannot guarantee the exact digits.
+__device__ __forceinline__ bool descent_key_fast(float4 x, const float *kp, unsigned long long &key)
+{
+  key = 0;
+  const float inv = kp[6];
+  if (inv == 0.f) // zero-size cube: every digit is 0, as in the reference
+    return true;
+  const int lv = __float_as_int(kp[7]);
+  const float unit = __int_as_float((127 + 21 - lv) << 23); // 2^(21 - lv)
+  const float xs[3] = {x.x, x.y, x.z};
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+  {
+    const float t = __fmul_rn(__fsub_rn(__fsub_rn(xs[d], kp[d]), kp[3 + d]), inv);
+    if (!(t > -1e30f && t < 1e30f))
+      return false;
+    const float q = t / unit;
+    const float rem = (q - floorf(q)) * unit; // distance above the last exact-level boundary
+    if (rem < 1.5f || unit - rem < 1.5f)
+      return false;
+    float c = floorf(t);
+    c = c < 0.f ? 0.f : (c > 2097151.f ? 2097151.f : c);
+    key |= spread3((unsigned long long)c) << d;
+  }
+  return true;
+}
+
+// Keys by the fast descent; the few items it cannot decide are appended to
+// fb_list and finished by k_keys_fallback, so no warp diverges into FP64.
 __global__ void k_keys(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= total)
-    return;
-  const int s = find_segment<int>(D.src_off, D.S, j);
-  const int p = src_particle(D, s, j);
-  D.key[j] = descent_key(D.pm[p], D.root + 4 * s);
-  D.val[j] = (uint32_t)p;
+  bool need = false;
+  if (j < total)
+  {
+    const int s = find_segment<int>(D.src_off, D.S, j);
+    const int p = src_particle(D, s, j);
+    unsigned long long key;
+    need = !descent_key_fast(D.pm[p], D.keyp + 8 * s, key);
+    D.key[j] = key;
+    D.val[j] = (uint32_t)p;
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, need);
+  if (m)
+  {
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == __ffs(m) - 1)
+      base = atomicAdd(D.fb_count, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+    if (need)
+      D.fb_list[base + __popc(m & ((1u << lane) - 1u))] = j;
+  }
+}
+
+__global__ void k_keys_fallback(DevState D)
+{
+  const int n = *D.fb_count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+  {
+    const int j = D.fb_list[i];
+    const int p = (int)D.val[j];
+    D.key[j] = descent_key(D.pm[p], D.root + 4 * D.seg_of[p]);
+  }
+}
+
+// Segment keys of the key-sorted items, and the identity permutation that the
+// stable sort on segments will carry.
+__global__ void k_segkeys_iota(const uint32_t *__restrict__ val, const int *__restrict__ seg_of,
+                               uint32_t *__restrict__ k32, uint32_t *__restrict__ perm, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < total)
+  {
+    k32[j] = (uint32_t)seg_of[val[j]];
+    perm[j] = (uint32_t)j;
+  }
+}
+
+__global__ void k_gather_keys(const unsigned long long *__restrict__ kin, const uint32_t *__restrict__ vin,
+                              const uint32_t *__restrict__ perm, unsigned long long *__restrict__ kout,
+                              uint32_t *__restrict__ vout, int total)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total)
+  {
+    const uint32_t j = perm[i];
+    kout[i] = kin[j];
+    vout[i] = vin[j];
+  }
 }
 
 // After sorting on the key, a stable sort on the subhalo restores the packing.
@@ -276,15 +398,6 @@ __global__ void k_segkeys(const uint32_t *__restrict__ val, const int *__restric
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j < total)
     k32[j] = (uint32_t)seg_of[val[j]];
-}
-
-__global__ void k_keys_again(DevState D, int total)
-{
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= total)
-    return;
-  const int p = (int)D.val[j];
-  D.key[j] = descent_key(D.pm[p], D.root + 4 * D.seg_of[p]);
 }
 
 // Number of tree cells whose first particle (in key order) is item j:

@@ -32,6 +32,7 @@
 
 #include "../../include/hbt_unbind_gpu.h"
 #include "common.cuh"
+#include "driver.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
 
@@ -61,9 +62,11 @@ constexpr size_t kScratchBytes =
   al(sizeof(float) * 8 * kS1) +              // old frame, mbound
   al(sizeof(unsigned) * 6 * kS1) +           // bounding boxes
   al(sizeof(double) * 4 * kS1) +             // root cubes
+  al(sizeof(float) * 8 * kS1) +              // fast key-descent constants
   al(sizeof(double) * 7 * kS1) +             // frame sums
   2 * al(sizeof(unsigned long long) * kN1) + // key, key_alt
-  4 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt
+  6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
+  al(sizeof(int) * kN1) + al(sizeof(int)) +  // key fallback list and its count
   4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
   al(sizeof(D4) * kN1) +                     // prefix sums
   al(sizeof(float4) * kNoAllocMaxRecords) +  // tree slots
@@ -135,126 +138,41 @@ inline unsigned nblocks(long long n, int threads)
   return (unsigned)std::max<long long>(1, (n + threads - 1) / threads);
 }
 
-struct NoAllocRun
+// Memory policy of the no-allocation path: every buffer is a fixed carve-out
+// of the static reserve; a request beyond its size fails the call.
+struct StaticMem
 {
-  cudaStream_t st;
-  KParams K;
-  DevState D;
-  int S;
-  int seg_bits;
-  int *table, *scan_scr;
-  D4 *d4_scr;
-  int64_t launches = 0;
+  int *scan_scr = nullptr, *table = nullptr;
+  D4 *d4_scr = nullptr;
+  float4 *slots = nullptr;
 
-  void check() { ck(cudaGetLastError()); }
-
-  int read_int(const int *d)
+  void check(cudaError_t e) { ck(e); }
+  int *scan_scratch(long long n)
   {
-    int h = 0;
-    ck(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
-    ck(cudaStreamSynchronize(st));
-    return h;
+    if (scan_scratch_elems<int>(n) > kScanScr)
+      throw Fail{HBTG_ERR_NOMEM};
+    return scan_scr;
   }
-
-  int scan_counts(const int *cnt, int *offs, long long n)
+  int *radix_table(long long n)
   {
-    scan<int, false>(cnt, offs, n + 1, scan_scr, st, &launches);
-    check();
-    return read_int(offs + n);
+    if (radix_table_elems(std::max<long long>(n, 1)) > kTable)
+      throw Fail{HBTG_ERR_NOMEM};
+    return table;
   }
-
-  template <typename Kt>
-  uint32_t *segmented_sort(Kt *keys, Kt *keys_alt, int key_bits, int total)
+  int *radix_scan_scratch(long long n) { return scan_scratch(radix_table_elems(std::max<long long>(n, 1)) + 1); }
+  D4 *d4_scratch(long long n)
   {
-    bool flip = radix_sort_pairs<Kt>(keys, D.val, keys_alt, D.val_alt, total, 0, key_bits, table, scan_scr, st,
-                                     &launches);
-    uint32_t *v = flip ? D.val_alt : D.val;
-    uint32_t *v_other = flip ? D.val : D.val_alt;
-    if (S > 1 && seg_bits > 0)
-    {
-      k_segkeys<<<nblocks(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
-      bool f2 = radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scan_scr, st,
-                                           &launches);
-      v = f2 ? v_other : v;
-    }
-    check();
-    return v;
+    if (scan_scratch_elems<D4>(n) > kD4Scr)
+      throw Fail{HBTG_ERR_NOMEM};
+    return d4_scr;
   }
-
-  void iterate()
+  float4 *tree_slots(long long n)
   {
-    const unsigned sb = nblocks(S + 1, 256);
-    for (;;)
-    {
-      k_plan<<<sb, 256, 0, st>>>(D);
-      check();
-      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
-      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
-      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
-      if (part_total == 0 && src_total == 0)
-        break;
-      if (src_total > 0)
-      {
-        k_bbox<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
-        k_root<<<sb, 256, 0, st>>>(D, K);
-        k_keys<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
-        check();
-        uint32_t *sorted = segmented_sort<unsigned long long>(D.key, D.key_alt, 63, src_total);
-        if (sorted != D.val)
-          ck(cudaMemcpyAsync(D.val, sorted, sizeof(uint32_t) * src_total, cudaMemcpyDeviceToDevice, st));
-        k_keys_again<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
-        k_tree_count<<<nblocks(src_total + 1, 256), 256, 0, st>>>(D, src_total);
-        check();
-        const int internal = scan_counts(D.cnt, D.X, src_total);
-        if ((long long)src_total + 2LL * internal > kNoAllocMaxRecords)
-          throw Fail{HBTG_ERR_NOMEM}; // tree larger than the reserve
-        k_prefix_prep<<<nblocks(src_total, 256), 256, 0, st>>>(D, src_total);
-        scan<D4, true>(D.P, D.P, src_total, d4_scr, st, &launches);
-        k_tree_emit<<<nblocks(src_total, 128), 128, 0, st>>>(D, K, src_total);
-        check();
-      }
-      if (chunk_total > 0)
-      {
-        k_walk<<<nblocks(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
-        check();
-      }
-      if (part_total > 0)
-      {
-        k_energy<<<nblocks(part_total, 256), 256, 0, st>>>(D, K, part_total);
-        k_part_flags<<<nblocks(part_total + 1, 256), 256, 0, st>>>(D, part_total);
-        check();
-        scan<int, false>(D.flags, D.F, part_total + 1, scan_scr, st, &launches);
-        k_part_count<<<sb, 256, 0, st>>>(D);
-        k_part_scatter<<<nblocks(part_total, 256), 256, 0, st>>>(D, part_total);
-        k_part_copy<<<nblocks(part_total, 256), 256, 0, st>>>(D, part_total);
-        k_after_part<<<sb, 256, 0, st>>>(D, K);
-        check();
-        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
-        if (tail_total > 0)
-        {
-          k_energy_keys<<<nblocks(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
-          uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, tail_total);
-          k_energy_write<<<nblocks(tail_total, 256), 256, 0, st>>>(D, sorted, D.tail_off, tail_total, 0);
-          check();
-        }
-        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
-        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
-        if (bound_total > 0)
-          k_com<<<nblocks(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
-        k_control<<<sb, 256, 0, st>>>(D, K);
-        check();
-      }
-    }
-    k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
-    const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);
-    if (fin_total > 0)
-    {
-      k_energy_keys<<<nblocks(fin_total, 256), 256, 0, st>>>(D, D.fin_off, fin_total, 1);
-      uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, fin_total);
-      k_energy_write<<<nblocks(fin_total, 256), 256, 0, st>>>(D, sorted, D.fin_off, fin_total, 1);
-      check();
-    }
+    if (n > kNoAllocMaxRecords)
+      throw Fail{HBTG_ERR_NOMEM}; // tree larger than the reserve
+    return slots;
   }
+  void mark(int) {}
 };
 
 KParams noalloc_kparams(const hbtg_params *p)
@@ -318,8 +236,8 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   if (rc != HBTG_OK)
     return rc;
 
-  NoAllocRun R;
-  R.st = st;
+  StaticMem mem;
+  IterationDriver<StaticMem> R(mem, st);
   R.K = noalloc_kparams(p);
   R.S = (int)S;
   int bits = 0;
@@ -353,6 +271,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.bb_lo = bb;
   D.bb_hi = bb ? bb + 3 * kS1 : nullptr;
   D.root = c.take<double>(4 * kS1);
+  D.keyp = c.take<float>(8 * kS1);
   D.com = c.take<double>(7 * kS1);
   D.key = c.take<unsigned long long>(kN1);
   D.key_alt = c.take<unsigned long long>(kN1);
@@ -360,15 +279,20 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.val_alt = c.take<uint32_t>(kN1);
   D.k32 = c.take<uint32_t>(kN1);
   D.k32_alt = c.take<uint32_t>(kN1);
+  D.perm = c.take<uint32_t>(kN1);
+  D.perm_alt = c.take<uint32_t>(kN1);
+  D.fb_list = c.take<int>(kN1);
+  D.fb_count = c.take<int>(1);
   D.cnt = c.take<int>(kN1);
   D.X = c.take<int>(kN1);
   D.flags = c.take<int>(kN1);
   D.F = c.take<int>(kN1);
   D.P = c.take<D4>(kN1);
-  D.nodes = c.take<float4>(kNoAllocMaxRecords);
-  R.table = c.take<int>(kTable);
-  R.scan_scr = c.take<int>(kScanScr);
-  R.d4_scr = c.take<D4>(kD4Scr);
+  mem.slots = c.take<float4>(kNoAllocMaxRecords);
+  D.nodes = mem.slots;
+  mem.table = c.take<int>(kTable);
+  mem.scan_scr = c.take<int>(kScanScr);
+  mem.d4_scr = c.take<D4>(kD4Scr);
   D.interactions = c.take<unsigned long long>(1);
   if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr ||
       (size_t)scan_scratch_elems<D4>(kN1) > kD4Scr)
@@ -388,7 +312,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
     k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D);
     R.check();
-    R.iterate();
+    R.run();
     OutPtrs O;
     O.order = reinterpret_cast<long long *>(b->order);
     O.nbound = reinterpret_cast<long long *>(b->nbound);
@@ -403,8 +327,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
     O.potential = b->potential;
     O.iterations = b->iterations;
     O.status = b->status;
-    k_epilogue<<<(unsigned)std::min<long long>(S, 65535), 256, 0, st>>>(D, R.K, O);
-    R.check();
+    R.epilogue(O);
     ck(cudaStreamSynchronize(st));
   }
   catch (Fail &f)

@@ -16,6 +16,7 @@
 
 #include "../../include/hbt_unbind_gpu.h"
 #include "common.cuh"
+#include "driver.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
 
@@ -51,9 +52,9 @@ enum Slot
   S_REFP, S_REFV, S_MBP, S_MBV, S_MBID,
   S_ORDER, S_NB, S_MB, S_NBT, S_MBT, S_TI, S_KIN, S_CORE, S_EN, S_POT, S_ITER, S_STAT,
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
-  S_SUBI, S_SUBF, S_BB, S_ROOT, S_COM,
+  S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER,
+  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC,
   S_NUM
 };
 
@@ -114,6 +115,7 @@ struct hbtg_handle
   hbtg_stats stats{};
   bool count_interactions = false;
   std::vector<cudaEvent_t> walk_events;
+  std::vector<cudaEvent_t> phase_events; // phase boundaries of the last call, in order
 };
 
 namespace
@@ -182,169 +184,54 @@ int read_int(const int *d, cudaStream_t st)
   return h;
 }
 
-struct Runner
+// Memory policy of the pooled entry points: grow-only buffers owned by the
+// handle, CUDA events at phase boundaries for the per-phase times.
+struct PoolMem
 {
   hbtg_handle *H;
   cudaStream_t st;
-  KParams K;
-  DevState D;
-  int S;
-  long long N;
-  int seg_bits;
-  int64_t *launches;
+  std::vector<int> mark_phase;
 
-  void check() { HBTG_CUDA(cudaGetLastError()); }
-
-  // scan of n+1 counts (the last is a zero) into offs; returns the total
-  int scan_counts(const int *cnt, int *offs, long long n)
+  void check(cudaError_t e) { HBTG_CUDA(e); }
+  int *scan_scratch(long long n)
   {
-    int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(n + 1, 256 * 4096)));
-    scan<int, false>(cnt, offs, n + 1, scr, st, launches);
-    check();
-    return read_int(offs + n, st);
+    return H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(n, 256LL * 4096)));
   }
-
-  // Sorts (keys, vals) of `total` packed items by key then by subhalo.
-  // Returns the array holding the sorted values.
-  template <typename Kt>
-  uint32_t *segmented_sort(Kt *keys, Kt *keys_alt, int key_bits, int total)
+  int *radix_table(long long n) { return H->pool.get<int>(S_TABLE, radix_table_elems(std::max<long long>(n, 1))); }
+  int *radix_scan_scratch(long long n)
   {
-    int *table = H->pool.get<int>(S_TABLE, radix_table_elems(std::max(total, 1)));
-    int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(
-                                             radix_table_elems(std::max(total, 1)) + 1, 256 * 4096)));
-    bool flip = radix_sort_pairs<Kt>(keys, D.val, keys_alt, D.val_alt, total, 0, key_bits, table, scr, st, launches);
-    uint32_t *v = flip ? D.val_alt : D.val;
-    uint32_t *v_other = flip ? D.val : D.val_alt;
-    if (S > 1 && seg_bits > 0)
-    {
-      k_segkeys<<<blocks_for(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
-      (*launches)++;
-      bool f2 = radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scr, st,
-                                           launches);
-      v = f2 ? v_other : v;
-    }
-    check();
-    return v;
+    return H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(
+                                         std::max<long long>(radix_table_elems(std::max<long long>(n, 1)) + 1,
+                                                             256LL * 4096)));
   }
-
-  void run()
+  D4 *d4_scratch(long long n) { return H->pool.get<D4>(S_D4SCR, scan_scratch_elems<D4>(std::max<long long>(n, 1))); }
+  float4 *tree_slots(long long slots)
   {
-    const unsigned sb = blocks_for(S + 1, 256);
-    int global_iter = 0;
-    H->stats.interactions = 0;
-    H->stats.tree_nodes = 0;
-    float ms_walk = 0.f;
-    for (;;)
+    if (slots >= (1LL << 31) - 64)
+      throw NoMem{};
+    return H->pool.get<float4>(S_NODES, (size_t)slots);
+  }
+  void mark(int phase)
+  {
+    const size_t k = mark_phase.size();
+    if (k >= H->phase_events.size())
     {
-      k_plan<<<sb, 256, 0, st>>>(D);
-      (*launches)++;
-      check();
-      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
-      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
-      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
-      if (part_total == 0 && src_total == 0)
-        break;
-      global_iter++;
-      // --- tree over the sources ---
-      if (src_total > 0)
-      {
-        k_bbox<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
-        k_root<<<sb, 256, 0, st>>>(D, K);
-        k_keys<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
-        *launches += 3;
-        check();
-        uint32_t *sorted = segmented_sort<unsigned long long>(D.key, D.key_alt, 63, src_total);
-        if (sorted != D.val)
-          HBTG_CUDA(cudaMemcpyAsync(D.val, sorted, sizeof(uint32_t) * src_total, cudaMemcpyDeviceToDevice, st));
-        k_keys_again<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
-        k_tree_count<<<blocks_for(src_total + 1, 256), 256, 0, st>>>(D, src_total);
-        *launches += 2;
-        check();
-        const int internal = scan_counts(D.cnt, D.X, src_total);
-        const long long records = (long long)src_total + 2LL * internal;
-        if (records >= (1LL << 31) - 64)
-          throw NoMem{};
-        D.nodes = H->pool.get<float4>(S_NODES, (size_t)records);
-        H->stats.tree_nodes += internal;
-        k_prefix_prep<<<blocks_for(src_total, 256), 256, 0, st>>>(D, src_total);
-        (*launches)++;
-        D4 *d4scr = H->pool.get<D4>(S_D4SCR, scan_scratch_elems<D4>(src_total));
-        scan<D4, true>(D.P, D.P, src_total, d4scr, st, launches);
-        k_tree_emit<<<blocks_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
-        (*launches)++;
-        check();
-      }
-      // --- walk ---
-      if (chunk_total > 0)
-      {
-        cudaEvent_t e0 = H->walk_events[0], e1 = H->walk_events[1];
-        HBTG_CUDA(cudaEventRecord(e0, st));
-        const int warps_per_block = 8;
-        k_walk<<<blocks_for(chunk_total, warps_per_block), 32 * warps_per_block, 0, st>>>(D, K, chunk_total);
-        HBTG_CUDA(cudaEventRecord(e1, st));
-        (*launches)++;
-        H->stats.walk_launches++;
-        check();
-        HBTG_CUDA(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        HBTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-        ms_walk += ms;
-      }
-      // --- energies and partition ---
-      if (part_total > 0)
-      {
-        k_energy<<<blocks_for(part_total, 256), 256, 0, st>>>(D, K, part_total);
-        k_part_flags<<<blocks_for(part_total + 1, 256), 256, 0, st>>>(D, part_total);
-        *launches += 2;
-        check();
-        int *scr = H->pool.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(part_total + 1,
-                                                                                             256 * 4096)));
-        scan<int, false>(D.flags, D.F, part_total + 1, scr, st, launches);
-        k_part_count<<<sb, 256, 0, st>>>(D);
-        k_part_scatter<<<blocks_for(part_total, 256), 256, 0, st>>>(D, part_total);
-        k_part_copy<<<blocks_for(part_total, 256), 256, 0, st>>>(D, part_total);
-        k_after_part<<<sb, 256, 0, st>>>(D, K);
-        *launches += 4;
-        check();
-        // sort the newly unbound tails by energy
-        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
-        if (tail_total > 0)
-        {
-          k_energy_keys<<<blocks_for(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
-          (*launches)++;
-          uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, tail_total);
-          k_energy_write<<<blocks_for(tail_total, 256), 256, 0, st>>>(D, sorted, D.tail_off, tail_total, 0);
-          (*launches)++;
-          check();
-        }
-        // centre-of-mass frame and convergence
-        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
-        (*launches)++;
-        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
-        if (bound_total > 0)
-        {
-          k_com<<<blocks_for(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
-          (*launches)++;
-        }
-        k_control<<<sb, 256, 0, st>>>(D, K);
-        (*launches)++;
-        check();
-      }
+      cudaEvent_t e;
+      HBTG_CUDA(cudaEventCreate(&e));
+      H->phase_events.push_back(e);
     }
-    H->stats.global_iterations = global_iter;
-    H->stats.ms_walk = ms_walk;
-    // final sort of the bound sets by binding energy
-    k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
-    (*launches)++;
-    const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);
-    if (fin_total > 0)
+    HBTG_CUDA(cudaEventRecord(H->phase_events[k], st));
+    mark_phase.push_back(phase);
+  }
+  // Per-phase totals (ms): 0 plan, 1 walk, 2 tree, 3 partition, 4 frame, 5 final.
+  void phase_totals(double *ms)
+  {
+    for (size_t k = 1; k < mark_phase.size(); k++)
     {
-      k_energy_keys<<<blocks_for(fin_total, 256), 256, 0, st>>>(D, D.fin_off, fin_total, 1);
-      (*launches)++;
-      uint32_t *sorted = segmented_sort<uint32_t>(D.k32, D.k32_alt, 32, fin_total);
-      k_energy_write<<<blocks_for(fin_total, 256), 256, 0, st>>>(D, sorted, D.fin_off, fin_total, 1);
-      (*launches)++;
-      check();
+      float t = 0.f;
+      HBTG_CUDA(cudaEventElapsedTime(&t, H->phase_events[k - 1], H->phase_events[k]));
+      if (mark_phase[k] >= 0)
+        ms[mark_phase[k]] += t;
     }
   }
 };
@@ -362,19 +249,16 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   H->stats.n_particles = N;
   if (S == 0)
     return HBTG_OK;
-  int64_t launches = 0;
   cudaEvent_t t0, t1;
   HBTG_CUDA(cudaEventCreate(&t0));
   HBTG_CUDA(cudaEventCreate(&t1));
   HBTG_CUDA(cudaEventRecord(t0, st));
 
-  Runner R;
-  R.H = H;
-  R.st = st;
+  PoolMem mem{H, st, {}};
+  IterationDriver<PoolMem> R(mem, st);
   R.K = make_kparams(p, H->count_interactions);
   R.S = S;
-  R.N = N;
-  R.launches = &launches;
+  R.sm_count = H->sm_count;
   int bits = 0;
   while ((1LL << bits) < S)
     bits++;
@@ -416,6 +300,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.bb_lo = bb;
   D.bb_hi = bb + 3 * (size_t)S;
   D.root = P.get<double>(S_ROOT, (size_t)S * 4);
+  D.keyp = P.get<float>(S_KEYP, (size_t)S * 8);
   D.com = P.get<double>(S_COM, (size_t)S * 7);
   D.key = P.get<unsigned long long>(S_KEY, n1);
   D.key_alt = P.get<unsigned long long>(S_KEYA, n1);
@@ -423,6 +308,10 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.val_alt = P.get<uint32_t>(S_VALA, n1);
   D.k32 = P.get<uint32_t>(S_K32, n1);
   D.k32_alt = P.get<uint32_t>(S_K32A, n1);
+  D.perm = P.get<uint32_t>(S_PERM, n1);
+  D.perm_alt = P.get<uint32_t>(S_PERMA, n1);
+  D.fb_list = P.get<int>(S_FBL, n1);
+  D.fb_count = P.get<int>(S_FBC, 1);
   D.cnt = P.get<int>(S_CNT, n1 + 1);
   D.X = P.get<int>(S_X, n1 + 1);
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
@@ -435,10 +324,10 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   if (N > 0)
   {
     k_repack<<<blocks_for(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
-    launches++;
+    R.launches++;
   }
   k_init_subs<<<blocks_for(S, 256), 256, 0, st>>>(D);
-  launches++;
+  R.launches++;
   R.check();
   R.run();
 
@@ -456,17 +345,26 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   O.potential = b->potential;
   O.iterations = b->iterations;
   O.status = b->status;
-  k_epilogue<<<std::min(S, 65535), 256, 0, st>>>(D, R.K, O);
-  launches++;
-  R.check();
+  R.epilogue(O);
   HBTG_CUDA(cudaEventRecord(t1, st));
   HBTG_CUDA(cudaEventSynchronize(t1));
+  double phase_ms[6] = {0, 0, 0, 0, 0, 0};
+  mem.phase_totals(phase_ms);
+  H->stats.ms_plan = phase_ms[0];
+  H->stats.ms_walk = phase_ms[1];
+  H->stats.ms_tree = phase_ms[2];
+  H->stats.ms_part = phase_ms[3];
+  H->stats.ms_frame = phase_ms[4];
+  H->stats.ms_final = phase_ms[5];
   float ms = 0.f;
   HBTG_CUDA(cudaEventElapsedTime(&ms, t0, t1));
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   H->stats.ms_total = ms;
-  H->stats.kernel_launches = launches;
+  H->stats.kernel_launches = R.launches;
+  H->stats.walk_launches = R.walk_launches;
+  H->stats.global_iterations = R.global_iter;
+  H->stats.tree_nodes = R.tree_nodes;
   if (H->count_interactions)
   {
     unsigned long long c = 0;
@@ -677,6 +575,8 @@ int hbtg_destroy(hbtg_handle *h)
   cudaSetDevice(h->device);
   h->pool.release();
   for (auto &e : h->walk_events)
+    cudaEventDestroy(e);
+  for (auto &e : h->phase_events)
     cudaEventDestroy(e);
   if (h->stream)
     cudaStreamDestroy(h->stream);

@@ -118,7 +118,8 @@ class CStats(C.Structure):
     _fields_ = [
         ("n_sub", C.c_int64), ("n_particles", C.c_int64), ("total_bound", C.c_int64),
         ("global_iterations", C.c_int64), ("interactions", C.c_int64), ("tree_nodes", C.c_int64),
-        ("ms_total", C.c_double), ("ms_walk", C.c_double), ("walk_launches", C.c_int64),
+        ("ms_total", C.c_double), ("ms_walk", C.c_double), ("ms_plan", C.c_double), ("ms_tree", C.c_double),
+        ("ms_part", C.c_double), ("ms_frame", C.c_double), ("ms_final", C.c_double), ("walk_launches", C.c_int64),
         ("kernel_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
     ]
 

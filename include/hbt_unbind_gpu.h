@@ -132,6 +132,11 @@ typedef struct hbtg_stats
   int64_t tree_nodes;         /* internal nodes built, summed over iterations */
   double ms_total;            /* wall time of the device part of the last call (CUDA events) */
   double ms_walk;             /* summed tree-walk kernel time (CUDA events) */
+  double ms_plan;             /* per-iteration planning: packing scans and host reads */
+  double ms_tree;             /* tree builds: bounding cubes, keys, sorts, cells */
+  double ms_part;             /* energies, partition, sort of the removed tails */
+  double ms_frame;            /* centre-of-mass frames and convergence tests */
+  double ms_final;            /* final energy sort and epilogue */
   int64_t walk_launches;
   int64_t kernel_launches;    /* kernels launched by the last call */
   int64_t h2d_bytes, d2h_bytes;
