@@ -199,7 +199,8 @@ struct IterationDriver
         const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
         if (bound_total > 0)
         {
-          k_com<<<grid_for(bound_total, 256), 256, 0, st>>>(D, K, bound_total);
+          k_com<<<grid_for((bound_total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, K,
+                                                                                                     bound_total);
           launches++;
         }
         k_control<<<sb, 256, 0, st>>>(D, K);
@@ -223,9 +224,21 @@ struct IterationDriver
     }
   }
 
+  // Outputs.  fin_off still packs the bound sets of the finished subhaloes.
   void epilogue(const OutPtrs &O)
   {
-    k_epilogue<<<(unsigned)std::min(S, 65535), 256, 0, st>>>(D, K, O);
+    const unsigned sb = grid_for(S, 256);
+    k_epi_init<<<sb, 256, 0, st>>>(D);
+    k_epi_order<<<grid_for(std::max<long long>(D.N, 1), 256), 256, 0, st>>>(D, O);
+    launches += 2;
+    const int fin_total = read_int(D.fin_off + S);
+    if (fin_total > 0)
+    {
+      k_epi_particles<<<grid_for((fin_total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, K, O,
+                                                                                                        fin_total);
+      launches++;
+    }
+    k_epilogue<<<sb, 256, 0, st>>>(D, K, O);
     launches++;
     check();
     mem.mark(5);

@@ -77,9 +77,11 @@ struct DevState
   int *tail_cnt, *tail_off, *fin_cnt, *fin_off;
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
   double *root;            // [4S] centre xyz, side length
-  float *keyp;             // [8S] per-axis origin hi/lo, 2^21/side, exact levels (fast key descent)
+  float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
   int *fb_list, *fb_count; // packed items whose key needs the exact double descent
-  double *com;             // [7S] M, sum m dx, sum m v
+  double *com;             // [7S] M, sum m dx, sum m v (epilogue: kinematics sums)
+  double *tmass;           // [6S] bound mass per particle type (epilogue)
+  double *com_part;        // [7 x blocks] per-block frame sums of single-subhalo k_com blocks
   // packed arrays
   unsigned long long *key, *key_alt;
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
@@ -235,7 +237,7 @@ __global__ void k_root(DevState D, KParams K)
   // fast-descent constants: origin of the root cube per axis as a float pair,
   // 2^21 / side, and the number of levels that must match the reference
   // exactly (cells not smaller than TreeNodeResolution, plus one)
-  float *kp = D.keyp + 8 * s;
+  float *kp = D.keyp + 12 * s;
   for (int d = 0; d < 3; d++)
   {
     const double o = 0.5 * (hi[d] + lo[d]) - 0.5 * len;
@@ -250,6 +252,12 @@ __global__ void k_root(DevState D, KParams K)
     exact_levels = lv < 1. ? 1 : (lv > 21. ? 21 : (int)lv);
   }
   kp[7] = __int_as_float(exact_levels);
+  // halvings until the side drops below TreeNodeResolution: a cell at level L
+  // has side len * 2^-min(L, kstar) (src/gravity_tree.cpp:38-42)
+  int kstar = 0;
+  for (double l = len; l >= (double)K.res && kstar < 1000; l *= 0.5)
+    kstar++;
+  kp[8] = __int_as_float(kstar);
   if (D.iter[s] == 1 && !D.corr[s]) // first iteration: the sources are every particle
     D.wrap[s] = K.periodic && (len > (double)K.half);
 }
@@ -337,7 +345,7 @@ __global__ void k_keys(DevState D, int total)
     const int s = find_segment<int>(D.src_off, D.S, j);
     const int p = src_particle(D, s, j);
     unsigned long long key;
-    need = !descent_key_fast(D.pm[p], D.keyp + 8 * s, key);
+    need = !descent_key_fast(D.pm[p], D.keyp + 12 * s, key);
     D.key[j] = key;
     D.val[j] = (uint32_t)p;
   }
@@ -463,6 +471,7 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   if (c == 0)
     return;
   const double *r = D.root + 4 * s;
+  const int kstar = __float_as_int(D.keyp[12 * s + 8]);
   const unsigned long long kj = D.key[j];
   const D4 before = (j > 0) ? D.P[j - 1] : D4{0., 0., 0., 0.};
   for (int t = 0; t < c; t++)
@@ -489,17 +498,14 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
     }
     const D4 after = D.P[b];
     const double mass = after.m - before.m;
-    // side length: halved per level while not below the resolution (src/gravity_tree.cpp:38-42)
-    double len = r[3];
-    for (int l = 0; l < L; l++)
-      len = (len >= (double)K.res) ? 0.5 * len : len;
-    const float lenf = (float)len;
+    const double inv_m = 1.0 / mass;
+    const float lenf = (float)ldexp(r[3], -min(L, kstar));
     const float len2 = lenf * lenf;
     const float crit = __fdiv_rn(len2, K.theta2);
     const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
-    D.nodes[base + 2 * t] = make_float4((float)(r[0] + (after.x - before.x) / mass),
-                                        (float)(r[1] + (after.y - before.y) / mass),
-                                        (float)(r[2] + (after.z - before.z) / mass),
+    D.nodes[base + 2 * t] = make_float4((float)(r[0] + (after.x - before.x) * inv_m),
+                                        (float)(r[1] + (after.y - before.y) * inv_m),
+                                        (float)(r[2] + (after.z - before.z) * inv_m),
                                         __uint_as_float(__float_as_uint(crit) | 0x80000000u));
     D.nodes[base + 2 * t + 1] = make_float4((float)mass, __int_as_float(skip), 0.f, 0.f);
   }
@@ -787,58 +793,140 @@ __global__ void k_energy_write(DevState D, const uint32_t *__restrict__ sorted_v
   D.ord[D.off[s] + k] = (int)sorted_val[j];
 }
 
-// FP64 centre-of-mass sums over the bound set, wrapped about its first particle.
+// Adds Q per-thread partial sums into out[Q*seg + q]: a warp-segmented
+// reduction over lanes holding the same segment, then one atomic per segment.
+template <int Q>
+__device__ __forceinline__ void segmented_flush(double (&acc)[Q], int seg, double *out)
+{
+  const unsigned peers = __match_any_sync(0xffffffffu, seg);
+  const int lane = threadIdx.x & 31;
+  if (peers == 0xffffffffu)
+  {
+#pragma unroll
+    for (int q = 0; q < Q; q++)
+      for (int o = 16; o > 0; o >>= 1)
+        acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+    if (lane == 0 && seg >= 0)
+      for (int q = 0; q < Q; q++)
+        atomicAdd(&out[Q * seg + q], acc[q]);
+    return;
+  }
+  if (seg >= 0)
+    for (int q = 0; q < Q; q++)
+      if (acc[q] != 0.)
+        atomicAdd(&out[Q * seg + q], acc[q]);
+}
+
+constexpr int kItemsPerThread = 16;
+
+// Kahan-compensated float accumulator.
+struct KahanF
+{
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v)
+  {
+    const float y = v - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// Centre-of-mass sums over the bound set, wrapped about its first particle
+// (src/subhalo_unbind.cpp:151-198).  Each thread sums 16 consecutive items
+// with compensated float partials (FP64 is scarce on this GPU); the partials
+// are added in double.  Offsets that need the periodic wrap are formed in
+// double as the reference does.
 __global__ void k_com(DevState D, KParams K, int total)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = j < total;
+  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kItemsPerThread;
+  KahanF acc[7];
+  double out[7] = {0., 0., 0., 0., 0., 0., 0.};
   int s = -1;
-  double acc[7] = {0., 0., 0., 0., 0., 0., 0.};
-  if (valid)
-  {
-    s = find_segment<int>(D.fin_off, D.S, j);
-    const int k = j - D.fin_off[s];
-    const int p = D.ord[D.off[s] + k];
-    const float4 x = D.pm[p], v = D.vu[p];
-    const float4 o = D.pm[D.ord[D.off[s]]];
-    const float m = x.w;
-    acc[0] = m;
-    if (K.periodic)
-    {
-      acc[1] = nearest_d((double)x.x - (double)o.x, K.half, K.box) * m;
-      acc[2] = nearest_d((double)x.y - (double)o.y, K.half, K.box) * m;
-      acc[3] = nearest_d((double)x.z - (double)o.z, K.half, K.box) * m;
-    }
-    else
-    {
-      acc[1] = __fmul_rn(x.x, m);
-      acc[2] = __fmul_rn(x.y, m);
-      acc[3] = __fmul_rn(x.z, m);
-    }
-    acc[4] = __fmul_rn(v.x, m);
-    acc[5] = __fmul_rn(v.y, m);
-    acc[6] = __fmul_rn(v.z, m);
-  }
-  const unsigned peers = __match_any_sync(0xffffffffu, s);
-  const int lane = threadIdx.x & 31;
-  const int leader = __ffs(peers) - 1;
-  // segmented warp reduction: add values of higher peers into the leader
-#pragma unroll
-  for (int q = 0; q < 7; q++)
-  {
-    double v = acc[q];
-    for (int o = 1; o < 32; o <<= 1)
-    {
-      const double w = __shfl_down_sync(0xffffffffu, v, o);
-      const int src = lane + o;
-      if (src < 32 && ((peers >> src) & 1u))
-        v += w;
-    }
-    acc[q] = v;
-  }
-  if (valid && lane == leader)
+  auto flush = [&](int seg) {
     for (int q = 0; q < 7; q++)
-      atomicAdd(&D.com[7 * s + q], acc[q]);
+    {
+      const double v = acc[q].value();
+      if (v != 0.)
+        atomicAdd(&D.com[7 * seg + q], v);
+      acc[q] = KahanF();
+    }
+  };
+  if (first < total)
+  {
+    s = find_segment<int>(D.fin_off, D.S, (int)first);
+    const int last = (int)min((long long)total, first + kItemsPerThread);
+    float4 o = D.pm[D.ord[D.off[s]]];
+    for (int j = (int)first; j < last; j++)
+    {
+      if (j >= D.fin_off[s + 1])
+      { // next subhalo: flush the partial sums of this one
+        flush(s);
+        s = find_segment<int>(D.fin_off, D.S, j); // skips any run of empty segments
+        o = D.pm[D.ord[D.off[s]]];
+      }
+      const int p = D.ord[D.off[s] + (j - D.fin_off[s])];
+      const float4 x = D.pm[p], v = D.vu[p];
+      const float m = x.w;
+      acc[0].add(m);
+      const float xs[3] = {x.x, x.y, x.z}, os[3] = {o.x, o.y, o.z};
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+      {
+        if (K.periodic)
+        {
+          const float df = xs[d] - os[d];
+          if (fabsf(df) < 0.25f * K.half) // no wrap possible; x - o is exact or nearly so
+            acc[1 + d].add(__fmul_rn(df, m));
+          else
+            acc[1 + d].add((float)(nearest_d((double)xs[d] - (double)os[d], K.half, K.box) * m));
+        }
+        else
+          acc[1 + d].add(__fmul_rn(xs[d], m));
+      }
+      acc[4].add(__fmul_rn(v.x, m));
+      acc[5].add(__fmul_rn(v.y, m));
+      acc[6].add(__fmul_rn(v.z, m));
+    }
+    for (int q = 0; q < 7; q++)
+      out[q] = acc[q].value();
+  }
+  // A block whose items all belong to one subhalo writes a block-reduced
+  // partial instead of contending atomics; k_control adds those partials.
+  __shared__ int s_seg_lo, s_seg_hi;
+  __shared__ double s_part[7][8];
+  const long long b0 = (long long)blockIdx.x * blockDim.x * kItemsPerThread;
+  const long long b1 = min((long long)total, b0 + (long long)blockDim.x * kItemsPerThread);
+  if (threadIdx.x == 0)
+  {
+    s_seg_lo = find_segment<int>(D.fin_off, D.S, (int)b0);
+    s_seg_hi = (b1 <= D.fin_off[s_seg_lo + 1]) ? s_seg_lo : -1;
+  }
+  __syncthreads();
+  if (s_seg_hi >= 0)
+  {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 7; q++)
+    {
+      double v = out[q];
+      for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0)
+        s_part[q][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 7)
+    {
+      double v = 0.;
+      for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+        v += s_part[threadIdx.x][i];
+      D.com_part[7LL * blockIdx.x + threadIdx.x] = v;
+    }
+    return;
+  }
+  segmented_flush<7>(out, s, D.com);
 }
 
 // New frame, bound mass and convergence test (src/subhalo_unbind.cpp:687-690).
@@ -847,7 +935,20 @@ __global__ void k_control(DevState D, KParams K)
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.S || D.state[s] != kActive)
     return;
-  const double *c = D.com + 7 * s;
+  double c[7];
+  for (int q = 0; q < 7; q++)
+    c[q] = D.com[7 * s + q];
+  // add the partials of the k_com blocks lying entirely inside this subhalo
+  // (same test as k_com: the block's item range [b0, b1) lies in [lo, hi))
+  const long long per_block = 256LL * kItemsPerThread;
+  const long long lo = D.fin_off[s], hi = D.fin_off[s + 1], total = D.fin_off[D.S];
+  for (long long b = (lo + per_block - 1) / per_block; b * per_block < hi; b++)
+  {
+    const long long b1 = min(total, (b + 1) * per_block);
+    if (b1 <= hi)
+      for (int q = 0; q < 7; q++)
+        c[q] += D.com_part[7 * b + q];
+  }
   const double M = c[0];
   const float4 o = D.pm[D.ord[D.off[s]]];
   const double org[3] = {o.x, o.y, o.z};
@@ -894,63 +995,90 @@ struct OutPtrs
   int *iterations, *status;
 };
 
-template <typename T>
-__device__ __forceinline__ T block_sum(T v, T *sh)
+// Zeroes the per-subhalo accumulators of the epilogue.
+__global__ void k_epi_init(DevState D)
 {
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0)
-    sh[w] = v;
-  __syncthreads();
-  T t = 0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); i++)
-      t += sh[i];
-  return t; // valid in thread 0
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S)
+    return;
+  for (int q = 0; q < 7; q++)
+    D.com[7 * s + q] = 0.;
+  for (int t = 0; t < 6; t++)
+  {
+    reinterpret_cast<int *>(D.bb_lo)[6 * s + t] = 0;
+    D.tmass[6 * s + t] = 0.;
+  }
+  D.nb_new[s] = 0x7fffffff;
 }
 
-__global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs O)
+// The output permutation: for resolved subhaloes the energy order, else the
+// input order (the reference permutes Particles only on convergence,
+// src/subhalo_unbind.cpp:744-750).
+__global__ void k_epi_order(DevState D, OutPtrs O)
 {
-  __shared__ double sh[8];
-  __shared__ int s_type_n[6];
-  __shared__ double s_type_m[6];
-  __shared__ int s_first_tracer;
-  for (int s = blockIdx.x; s < D.S; s += gridDim.x)
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
   {
-    const int st = D.state[s];
+    const int s = D.seg_of[i];
     const long long off = D.off[s];
-    const int n = D.n_s[s];
-    const int nb = (st == kConverged || st == kMaxIter) ? D.nbound[s] : 0;
-    if (threadIdx.x < 6)
+    const int st = D.state[s];
+    O.order[i] = (st == kConverged || st == kMaxIter) ? (long long)D.ord[i] - off : i - off;
+  }
+}
+
+// Per-particle outputs of the bound sets (binding and potential energies) and
+// the FP64 sums of AverageKinematics (src/subhalo_unbind.cpp:200-249), the
+// per-type counts and masses of CountParticleTypes (src/subhalo.cpp:311-393)
+// and the first tracer position.  Items are the bound particles of finished
+// subhaloes packed by fin_off; each thread takes 16 consecutive items.
+__global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
+{
+  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kItemsPerThread;
+  double acc[6] = {0., 0., 0., 0., 0., 0.};
+  int tn[6] = {0, 0, 0, 0, 0, 0};
+  double tm[6] = {0., 0., 0., 0., 0., 0.};
+  int ft = 0x7fffffff;
+  int s = -1;
+  auto flush_types = [&](int seg) {
+    for (int t = 0; t < 6; t++)
+      if (tn[t])
+      {
+        atomicAdd(&reinterpret_cast<int *>(D.bb_lo)[6 * seg + t], tn[t]);
+        atomicAdd(&D.tmass[6 * seg + t], tm[t]);
+        tn[t] = 0;
+        tm[t] = 0.;
+      }
+    if (ft != 0x7fffffff)
+      atomicMin(&D.nb_new[seg], ft);
+    ft = 0x7fffffff;
+  };
+  if (first < total)
+  {
+    s = find_segment<int>(D.fin_off, D.S, (int)first);
+    const int last = (int)min((long long)total, first + kItemsPerThread);
+    for (int j = (int)first; j < last; j++)
     {
-      s_type_n[threadIdx.x] = 0;
-      s_type_m[threadIdx.x] = 0.;
-    }
-    if (threadIdx.x == 0)
-      s_first_tracer = 0x7fffffff;
-    __syncthreads();
-    // order
-    for (int k = threadIdx.x; k < n; k += blockDim.x)
-      O.order[off + k] = (st == kConverged || st == kMaxIter) ? (long long)D.ord[off + k] - off : (long long)k;
-    // per-particle outputs and sums over the bound set
-    double Et = 0., Kk = 0., L0 = 0., L1 = 0., L2 = 0., Ms = 0.;
-    int my_type_n[6] = {0, 0, 0, 0, 0, 0};
-    double my_type_m[6] = {0., 0., 0., 0., 0., 0.};
-    int my_first_tracer = 0x7fffffff;
-    const float *rp = D.ref_pos + 3 * s, *rv = D.ref_vel + 3 * s;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x)
-    {
+      if (j >= D.fin_off[s + 1])
+      {
+        for (int q = 0; q < 6; q++)
+          if (acc[q] != 0.)
+            atomicAdd(&D.com[7 * s + q], acc[q]);
+        for (int q = 0; q < 6; q++)
+          acc[q] = 0.;
+        flush_types(s);
+        s = find_segment<int>(D.fin_off, D.S, j); // skips any run of empty segments
+      }
+      const int k = j - D.fin_off[s];
+      const long long off = D.off[s];
       const int p = D.ord[off + k];
       const float4 x = D.pm[p], v = D.vu[p];
       const float e = D.Ep[p];
       if (O.energy)
         O.energy[off + k] = e;
       const float m = x.w;
-      Et += (double)__fmul_rn(e, m);
+      acc[0] += (double)__fmul_rn(e, m);
       if (K.thermal)
-        Et -= (double)__fmul_rn(v.w, m);
+        acc[0] -= (double)__fmul_rn(v.w, m);
+      const float *rp = D.ref_pos + 3 * s, *rv = D.ref_vel + 3 * s;
       const float xs[3] = {x.x, x.y, x.z}, vs[3] = {v.x, v.y, v.z};
       double dx[3], dv[3];
       float pe = K.thermal ? __fsub_rn(e, v.w) : e;
@@ -961,167 +1089,162 @@ __global__ void __launch_bounds__(256) k_epilogue(DevState D, KParams K, OutPtrs
           dx[d] = nearest_d(dx[d], K.half, K.box);
         dx[d] *= (double)K.a;
         dv[d] = (double)__fsub_rn(vs[d], rv[d]) + (double)K.hz * dx[d];
-        Kk += dv[d] * dv[d] * m;
+        acc[1] += dv[d] * dv[d] * m;
         pe = (float)((double)pe - 0.5 * dv[d] * dv[d]);
       }
       if (O.potential)
         O.potential[off + k] = pe;
-      L0 += (dx[1] * dv[2] - dx[2] * dv[1]) * m;
-      L1 += (dx[2] * dv[0] - dx[0] * dv[2]) * m;
-      L2 += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
-      Ms += m;
+      acc[2] += (dx[1] * dv[2] - dx[2] * dv[1]) * m;
+      acc[3] += (dx[2] * dv[0] - dx[0] * dv[2]) * m;
+      acc[4] += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
+      acc[5] += m;
       const uint8_t t = D.ty[p];
 #pragma unroll
       for (int q = 0; q < 6; q++)
         if ((t & 7) == q)
         {
-          my_type_n[q]++;
-          my_type_m[q] += (double)m;
+          tn[q]++;
+          tm[q] += (double)m;
         }
-      if (is_tracer_bits(t) && k < my_first_tracer)
-        my_first_tracer = k;
+      if (is_tracer_bits(t) && k < ft)
+        ft = k;
     }
-    // combine the per-thread partials (shared atomics only once per thread)
-    for (int q = 0; q < 6; q++)
-    {
-      if (my_type_n[q])
-      {
-        atomicAdd(&s_type_n[q], my_type_n[q]);
-        atomicAdd(&s_type_m[q], my_type_m[q]);
-      }
-    }
-    if (my_first_tracer != 0x7fffffff)
-      atomicMin(&s_first_tracer, my_first_tracer);
-    Et = block_sum(Et, sh);
-    Kk = block_sum(Kk, sh);
-    L0 = block_sum(L0, sh);
-    L1 = block_sum(L1, sh);
-    L2 = block_sum(L2, sh);
-    Ms = block_sum(Ms, sh);
-    __syncthreads();
-    if (threadIdx.x == 0)
-    {
-      float kin[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-      if (nb > 1)
-      {
-        Et /= Ms;
-        Kk *= 0.5 / Ms;
-        kin[0] = (float)(Et - Kk);
-        kin[1] = (float)Kk;
-        kin[2] = (float)(L0 / Ms);
-        kin[3] = (float)(L1 / Ms);
-        kin[4] = (float)(L2 / Ms);
-      }
-      if (O.kinematics)
-        for (int q = 0; q < 5; q++)
-          O.kinematics[5 * s + q] = kin[q];
-      for (int t = 0; t < 6; t++)
-      {
-        if (O.nbound_type)
-          O.nbound_type[6 * s + t] = s_type_n[t];
-        if (O.mbound_type)
-          O.mbound_type[6 * s + t] = K.dm_only ? 0.f : (float)s_type_m[t];
-      }
-      long long ti;
-      if (st == kEmpty)
-        ti = -1;
-      else if (nb == 0 || K.dm_only || s_first_tracer == 0x7fffffff)
-        ti = 0;
-      else
-        ti = s_first_tracer;
-      O.tracer_index[s] = ti;
-      O.nbound[s] = nb;
-      O.mbound[s] = (st == kConverged || st == kMaxIter) ? D.mbound[s] : 0.f;
-      O.iterations[s] = D.iter[s];
-      O.status[s] = st == kConverged ? 0 : st == kDisrupted ? 1 : st == kEmpty ? 2 : 3;
-      float *mbp = D.mb_pos + 3 * s, *mbv = D.mb_vel + 3 * s;
-      if (nb > 0)
-      {
-        const int p0 = D.ord[off];
-        const float4 x0 = D.pm[p0], v0 = D.vu[p0];
-        mbp[0] = x0.x;
-        mbp[1] = x0.y;
-        mbp[2] = x0.z;
-        mbv[0] = v0.x;
-        mbv[1] = v0.y;
-        mbv[2] = v0.z;
-        O.most_bound_id[s] = D.id[D.ord[off + ti]];
-      }
-      if (O.core)
-      {
-        float *cr = O.core + 8 * s;
-        if (nb == 0)
-        {
-          for (int d = 0; d < 3; d++)
-          {
-            cr[d] = mbp[d];
-            cr[3 + d] = mbv[d];
-          }
-          cr[6] = cr[7] = 0.f;
-        }
-        else
-        {
-          // GetCorePhaseSpaceProperties: first CoreSize tracers, then non-tracers
-          const long long core_size =
-            max((long long)((float)nb * K.core_factor), K.core_min);
-          long long used = 0;
-          double msum = 0., ps[3] = {0., 0., 0.}, ps2[3] = {0., 0., 0.}, vs[3] = {0., 0., 0.},
-                 vs2[3] = {0., 0., 0.}, org[3] = {0., 0., 0.};
-          const float4 x0 = D.pm[D.ord[off]];
-          if (K.periodic)
-          {
-            org[0] = x0.x;
-            org[1] = x0.y;
-            org[2] = x0.z;
-          }
-          for (int pass = 0; pass < 2 && used != core_size; pass++)
-            for (int i = 0; i < nb; i++)
-            {
-              const int p = D.ord[off + i];
-              const bool tr = is_tracer_bits(D.ty[p]);
-              if ((tr && pass == 0) || (!tr && pass == 1))
-              {
-                used++;
-                const float4 x = D.pm[p], v = D.vu[p];
-                const float m = x.w;
-                msum += m;
-                const float xs[3] = {x.x, x.y, x.z}, vv[3] = {v.x, v.y, v.z};
-                for (int d = 0; d < 3; d++)
-                {
-                  double dx = xs[d];
-                  if (K.periodic)
-                    dx = nearest_d(dx - org[d], K.half, K.box);
-                  ps[d] += m * dx;
-                  ps2[d] += m * dx * dx;
-                  const double dvv = vv[d];
-                  vs[d] += m * dvv;
-                  vs2[d] += m * dvv * dvv;
-                }
-              }
-              if (used == core_size)
-                break;
-            }
-          for (int d = 0; d < 3; d++)
-          {
-            ps[d] /= msum;
-            ps2[d] /= msum;
-            float cp = (float)ps[d];
-            if (K.periodic)
-              cp = (float)((double)cp + org[d]);
-            cr[d] = cp;
-            ps2[d] -= ps[d] * ps[d];
-            vs[d] /= msum;
-            vs2[d] /= msum;
-            cr[3 + d] = (float)vs[d];
-            vs2[d] -= vs[d] * vs[d];
-          }
-          cr[6] = (float)sqrt(ps2[0] + ps2[1] + ps2[2]);
-          cr[7] = (float)sqrt(vs2[0] + vs2[1] + vs2[2]);
-        }
-      }
-    }
-    __syncthreads();
+    flush_types(s);
   }
+  double acc7[7] = {acc[0], acc[1], acc[2], acc[3], acc[4], acc[5], 0.};
+  segmented_flush<7>(acc7, s, D.com);
+}
+
+// Scalar outputs of each subhalo (one thread per subhalo): kinematics, type
+// counts, tracer index, most-bound particle and ID, core phase-space
+// properties (src/subhalo_merge.cpp:94-181), status and iterations.
+__global__ void k_epilogue(DevState D, KParams K, OutPtrs O)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S)
+    return;
+  const int st = D.state[s];
+  const long long off = D.off[s];
+  const bool resolved = (st == kConverged || st == kMaxIter);
+  const int nb = resolved ? D.nbound[s] : 0;
+  const double *c = D.com + 7 * s;
+  float kin[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (nb > 1)
+  {
+    const double Ms = c[5];
+    const double Et = c[0] / Ms;
+    const double Kk = c[1] * (0.5 / Ms);
+    kin[0] = (float)(Et - Kk);
+    kin[1] = (float)Kk;
+    kin[2] = (float)(c[2] / Ms);
+    kin[3] = (float)(c[3] / Ms);
+    kin[4] = (float)(c[4] / Ms);
+  }
+  if (O.kinematics)
+    for (int q = 0; q < 5; q++)
+      O.kinematics[5 * s + q] = kin[q];
+  const int *tn = reinterpret_cast<const int *>(D.bb_lo) + 6 * s;
+  for (int t = 0; t < 6; t++)
+  {
+    if (O.nbound_type)
+      O.nbound_type[6 * s + t] = resolved ? tn[t] : 0;
+    if (O.mbound_type)
+      O.mbound_type[6 * s + t] = (K.dm_only || !resolved) ? 0.f : (float)D.tmass[6 * s + t];
+  }
+  const int first_tracer = D.nb_new[s];
+  long long ti;
+  if (st == kEmpty)
+    ti = -1;
+  else if (nb == 0 || K.dm_only || first_tracer == 0x7fffffff)
+    ti = 0;
+  else
+    ti = first_tracer;
+  O.tracer_index[s] = ti;
+  O.nbound[s] = nb;
+  O.mbound[s] = resolved ? D.mbound[s] : 0.f;
+  O.iterations[s] = D.iter[s];
+  O.status[s] = st == kConverged ? 0 : st == kDisrupted ? 1 : st == kEmpty ? 2 : 3;
+  float *mbp = D.mb_pos + 3 * s, *mbv = D.mb_vel + 3 * s;
+  if (nb > 0)
+  {
+    const int p0 = D.ord[off];
+    const float4 x0 = D.pm[p0], v0 = D.vu[p0];
+    mbp[0] = x0.x;
+    mbp[1] = x0.y;
+    mbp[2] = x0.z;
+    mbv[0] = v0.x;
+    mbv[1] = v0.y;
+    mbv[2] = v0.z;
+    O.most_bound_id[s] = D.id[D.ord[off + ti]];
+  }
+  if (!O.core)
+    return;
+  float *cr = O.core + 8 * s;
+  if (nb == 0)
+  {
+    for (int d = 0; d < 3; d++)
+    {
+      cr[d] = mbp[d];
+      cr[3 + d] = mbv[d];
+    }
+    cr[6] = cr[7] = 0.f;
+    return;
+  }
+  // first CoreSize tracers, then non-tracers
+  const long long core_size = max((long long)((float)nb * K.core_factor), K.core_min);
+  long long used = 0;
+  double msum = 0., ps[3] = {0., 0., 0.}, ps2[3] = {0., 0., 0.}, vs[3] = {0., 0., 0.}, vs2[3] = {0., 0., 0.},
+         org[3] = {0., 0., 0.};
+  const float4 x0 = D.pm[D.ord[off]];
+  if (K.periodic)
+  {
+    org[0] = x0.x;
+    org[1] = x0.y;
+    org[2] = x0.z;
+  }
+  for (int pass = 0; pass < 2 && used != core_size; pass++)
+    for (int i = 0; i < nb; i++)
+    {
+      const int p = D.ord[off + i];
+      const bool tr = is_tracer_bits(D.ty[p]);
+      if ((tr && pass == 0) || (!tr && pass == 1))
+      {
+        used++;
+        const float4 x = D.pm[p], v = D.vu[p];
+        const float m = x.w;
+        msum += m;
+        const float xs[3] = {x.x, x.y, x.z}, vv[3] = {v.x, v.y, v.z};
+        for (int d = 0; d < 3; d++)
+        {
+          double dx = xs[d];
+          if (K.periodic)
+            dx = nearest_d(dx - org[d], K.half, K.box);
+          ps[d] += m * dx;
+          ps2[d] += m * dx * dx;
+          const double dvv = vv[d];
+          vs[d] += m * dvv;
+          vs2[d] += m * dvv * dvv;
+        }
+      }
+      if (used == core_size)
+        break;
+    }
+  for (int d = 0; d < 3; d++)
+  {
+    ps[d] /= msum;
+    ps2[d] /= msum;
+    float cp = (float)ps[d];
+    if (K.periodic)
+      cp = (float)((double)cp + org[d]);
+    cr[d] = cp;
+    ps2[d] -= ps[d] * ps[d];
+    vs[d] /= msum;
+    vs2[d] /= msum;
+    cr[3 + d] = (float)vs[d];
+    vs2[d] -= vs[d] * vs[d];
+  }
+  cr[6] = (float)sqrt(ps2[0] + ps2[1] + ps2[2]);
+  cr[7] = (float)sqrt(vs2[0] + vs2[1] + vs2[2]);
 }
 
 } // namespace

@@ -54,7 +54,7 @@ enum Slot
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC,
+  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP,
   S_NUM
 };
 
@@ -300,8 +300,10 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.bb_lo = bb;
   D.bb_hi = bb + 3 * (size_t)S;
   D.root = P.get<double>(S_ROOT, (size_t)S * 4);
-  D.keyp = P.get<float>(S_KEYP, (size_t)S * 8);
+  D.keyp = P.get<float>(S_KEYP, (size_t)S * 12);
   D.com = P.get<double>(S_COM, (size_t)S * 7);
+  D.tmass = P.get<double>(S_TMASS, (size_t)S * 6);
+  D.com_part = P.get<double>(S_COMP, 7 * ((size_t)N / (256 * kItemsPerThread) + 2));
   D.key = P.get<unsigned long long>(S_KEY, n1);
   D.key_alt = P.get<unsigned long long>(S_KEYA, n1);
   D.val = P.get<uint32_t>(S_VAL, n1);
