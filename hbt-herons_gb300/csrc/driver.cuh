@@ -139,6 +139,21 @@ struct IterationDriver
     launches++;
     scan<D4, true>(D.P, D.P, src_total, mem.d4_scratch(src_total), st, &launches);
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
+    k_record_key_order<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    launches += 2;
+    check();
+  }
+
+  // Targets of the correction walks in key order (see k_tgt_flags).
+  void correction_targets()
+  {
+    const int total = scan_counts(D.sp_cnt, D.sp_off, S);
+    if (total == 0)
+      return;
+    k_tgt_flags<<<grid_for(total + 1, 256), 256, 0, st>>>(D, total);
+    launches++;
+    scan<int, false>(D.flags, D.F, total + 1, mem.scan_scratch(total + 1), st, &launches);
+    k_tgt_scatter<<<grid_for(total, 256), 256, 0, st>>>(D, total);
     launches++;
     check();
   }
@@ -161,6 +176,7 @@ struct IterationDriver
       global_iter++;
       if (src_total > 0)
         build_tree(src_total);
+      correction_targets();
       mem.mark(2);
       if (chunk_total > 0)
       {

@@ -65,6 +65,9 @@ struct DevState
   uint8_t *ty; // bits 0-2 type, bit 3 tracer
   int *seg_of; // subhalo of each particle
   int *ord, *ord_tmp; // current energy order: global particle index at each position
+  int *sp;            // per subhalo: its particles in key order at the last full tree build
+  int *tgt;           // per subhalo: correction-walk targets (bound particles in key order)
+  uint8_t *bnd;       // 1 while a particle is in its subhalo's bound set
   float *Ep;  // binding energy per particle
   float *pot; // tree potential per particle (G/a applied)
   const long long *id;
@@ -75,6 +78,8 @@ struct DevState
   // per-iteration plan
   int *src_begin, *src_cnt, *src_off, *tgt_cnt, *chunk_cnt, *chunk_off, *part_cnt, *part_off;
   int *tail_cnt, *tail_off, *fin_cnt, *fin_off;
+  int *sp_cnt, *sp_off;    // correction subhaloes: key-order list lengths and packing
+  int *sp_len;             // length of each subhalo's key-order list
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
   double *root;            // [4S] centre xyz, side length
   float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
@@ -116,6 +121,7 @@ __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, c
     const int s = find_segment<long long>(D.off, D.S, i);
     D.seg_of[i] = s;
     D.ord[i] = (int)i;
+    D.bnd[i] = 1;
   }
 }
 
@@ -144,12 +150,12 @@ __global__ void k_plan(DevState D)
     return;
   if (s == D.S)
   { // trailing zero so that the exclusive scans yield the totals
-    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = 0;
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.sp_cnt[s] = 0;
     return;
   }
   if (D.state[s] != kActive)
   {
-    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tgt_cnt[s] = 0;
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tgt_cnt[s] = D.sp_cnt[s] = 0;
     return;
   }
   D.iter[s] += 1;
@@ -171,6 +177,14 @@ __global__ void k_plan(DevState D)
   D.tgt_cnt[s] = tgt;
   D.chunk_cnt[s] = (tgt + kWarp - 1) / kWarp;
   D.part_cnt[s] = D.nlast[s];
+  // a full build records the key order (sp_len); a correction walk compacts it
+  if (!D.corr[s])
+  {
+    D.sp_len[s] = D.nlast[s];
+    D.sp_cnt[s] = 0;
+  }
+  else
+    D.sp_cnt[s] = D.sp_len[s];
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
   D.tracers[s] = 0;
@@ -408,6 +422,42 @@ __global__ void k_segkeys(const uint32_t *__restrict__ val, const int *__restric
     k32[j] = (uint32_t)seg_of[val[j]];
 }
 
+// After a full tree build: remember each such subhalo's particles in key order.
+__global__ void k_record_key_order(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  if (!D.corr[s])
+    D.sp[D.off[s] + (j - D.src_off[s])] = (int)D.val[j];
+}
+
+// Correction walks: the bound particles in the key order of the last full
+// build, so that a warp's 32 targets are neighbours (flag, scan, scatter).
+__global__ void k_tgt_flags(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > total)
+    return;
+  if (j == total)
+  {
+    D.flags[j] = 0;
+    return;
+  }
+  const int s = find_segment<int>(D.sp_off, D.S, j);
+  D.flags[j] = D.bnd[D.sp[D.off[s] + (j - D.sp_off[s])]];
+}
+
+__global__ void k_tgt_scatter(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total || !D.flags[j])
+    return;
+  const int s = find_segment<int>(D.sp_off, D.S, j);
+  D.tgt[D.off[s] + (D.F[j] - D.F[D.sp_off[s]])] = D.sp[D.off[s] + (j - D.sp_off[s])];
+}
+
 // Number of tree cells whose first particle (in key order) is item j:
 // levels lo..hi, where lo is one past the common prefix with the previous key
 // and hi the common prefix with the next key (a cell needs two particles).
@@ -592,7 +642,7 @@ __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_c
     const bool corr = D.corr[s] != 0;
     int p = 0;
     if (valid)
-      p = corr ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t];
+      p = corr ? D.tgt[D.off[s] + t] : (int)D.val[D.src_off[s] + t];
     const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
     float phi = 0.f;
@@ -706,6 +756,7 @@ __global__ void k_part_scatter(DevState D, int total)
     const int dest = bound ? rb : D.nb_new[s] + (k - rb);
     const int p = D.ord[D.off[s] + k];
     D.ord_tmp[D.off[s] + dest] = p;
+    D.bnd[p] = bound ? 1 : 0;
     tracer = (bound && is_tracer_bits(D.ty[p])) ? 1 : 0;
   }
   const unsigned peers = __match_any_sync(0xffffffffu, s);

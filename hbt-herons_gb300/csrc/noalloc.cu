@@ -57,8 +57,9 @@ constexpr size_t kScratchBytes =
   al(sizeof(long long) * kS1) +              // offsets
   2 * al(sizeof(float4) * kN1) +             // pm, vu
   al(kN1) +                                  // ty
-  5 * al(sizeof(int) * kN1) +                // seg_of, ord, ord_tmp, + Ep, pot (4 bytes each)
-  21 * al(sizeof(int) * kS1) +               // per-subhalo ints
+  7 * al(sizeof(int) * kN1) +                // seg_of, ord, ord_tmp, sp, tgt + Ep, pot (4 bytes each)
+  al(kN1) +                                  // bound flags
+  24 * al(sizeof(int) * kS1) +               // per-subhalo ints
   al(sizeof(float) * 8 * kS1) +              // old frame, mbound
   al(sizeof(unsigned) * 6 * kS1) +           // bounding boxes
   al(sizeof(double) * 4 * kS1) +             // root cubes
@@ -258,11 +259,14 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.seg_of = c.take<int>(kN1);
   D.ord = c.take<int>(kN1);
   D.ord_tmp = c.take<int>(kN1);
+  D.sp = c.take<int>(kN1);
+  D.tgt = c.take<int>(kN1);
+  D.bnd = c.take<uint8_t>(kN1);
   D.Ep = c.take<float>(kN1);
   D.pot = c.take<float>(kN1);
   int **ints[] = {&D.n_s, &D.nbound, &D.nlast, &D.state, &D.corr, &D.iter, &D.wrap, &D.tracers, &D.nb_new,
                   &D.src_begin, &D.src_cnt, &D.src_off, &D.tgt_cnt, &D.chunk_cnt, &D.chunk_off, &D.part_cnt,
-                  &D.part_off, &D.tail_cnt, &D.tail_off, &D.fin_cnt, &D.fin_off};
+                  &D.part_off, &D.tail_cnt, &D.tail_off, &D.fin_cnt, &D.fin_off, &D.sp_cnt, &D.sp_off, &D.sp_len};
   for (int **pp : ints)
     *pp = c.take<int>(kS1);
   float *subf = c.take<float>(8 * kS1);

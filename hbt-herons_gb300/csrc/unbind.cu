@@ -54,7 +54,7 @@ enum Slot
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP,
+  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND,
   S_NUM
 };
 
@@ -277,16 +277,20 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.seg_of = P.get<int>(S_SEG, n1);
   D.ord = P.get<int>(S_ORD, n1);
   D.ord_tmp = P.get<int>(S_ORDT, n1);
+  D.sp = P.get<int>(S_SP, n1);
+  D.tgt = P.get<int>(S_TGT, n1);
+  D.bnd = P.get<uint8_t>(S_BND, n1);
   D.Ep = P.get<float>(S_EP, n1);
   D.pot = P.get<float>(S_PHI, n1);
   D.id = reinterpret_cast<const long long *>(b->id);
-  int *subi = P.get<int>(S_SUBI, (size_t)(S + 1) * 24);
+  int *subi = P.get<int>(S_SUBI, (size_t)(S + 1) * 26);
   int q = 0;
   auto nexti = [&]() { return subi + (size_t)(S + 1) * (q++); };
   D.n_s = nexti(); D.nbound = nexti(); D.nlast = nexti(); D.state = nexti(); D.corr = nexti(); D.iter = nexti();
   D.wrap = nexti(); D.tracers = nexti(); D.nb_new = nexti(); D.src_begin = nexti(); D.src_cnt = nexti();
   D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
   D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
+  D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti();
   float *subf = P.get<float>(S_SUBF, (size_t)S * 8);
   D.old_pos = subf;
   D.old_vel = subf + 3 * (size_t)S;
