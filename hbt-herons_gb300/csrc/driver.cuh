@@ -49,7 +49,13 @@ struct IterationDriver
   int64_t tree_nodes = 0;
   int global_iter = 0;
 
-  IterationDriver(Mem &m, cudaStream_t s) : mem(m), st(s) {}
+  IterationDriver(Mem &m, cudaStream_t s) : mem(m), st(s)
+  {
+    // the walk uses no shared memory: give the whole on-chip array to L1
+    cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    cudaGetLastError();
+  }
 
   void check() { mem.check(cudaGetLastError()); }
 
@@ -164,7 +170,7 @@ struct IterationDriver
     mem.mark(-1);
     for (;;)
     {
-      k_plan<<<sb, 256, 0, st>>>(D);
+      k_plan<<<sb, 256, 0, st>>>(D, K);
       launches++;
       check();
       const int src_total = scan_counts(D.src_cnt, D.src_off, S);
@@ -174,13 +180,27 @@ struct IterationDriver
       if (part_total == 0 && src_total == 0)
         break;
       global_iter++;
+      if (K.max_sample > 0)
+      { // upscale factors of the subsampled subhaloes
+        k_upscale<<<(unsigned)std::min(S, 65535), 256, 0, st>>>(D, K);
+        launches++;
+        check();
+      }
       if (src_total > 0)
         build_tree(src_total);
+      if (K.max_sample > 0 && part_total > 0)
+      {
+        k_record_candidates<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+        launches++;
+      }
       correction_targets();
       mem.mark(2);
       if (chunk_total > 0)
       {
-        k_walk<<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+        if (K.count_interactions)
+          k_walk<true><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+        else
+          k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
         launches++;
         walk_launches++;
         check();
@@ -238,6 +258,30 @@ struct IterationDriver
       launches++;
       check();
     }
+    if (K.max_sample > 0 && K.refine)
+      refine_order();
+  }
+
+  // RefineBindingEnergyOrder for the converged subsampled subhaloes.
+  void refine_order()
+  {
+    const unsigned sb = grid_for(S + 1, 256);
+    k_plan_refine<<<sb, 256, 0, st>>>(D, K);
+    launches++;
+    check();
+    const int src_total = scan_counts(D.src_cnt, D.src_off, S);
+    const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
+    if (src_total == 0)
+      return;
+    build_tree(src_total);
+    k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+    k_refine_keys<<<grid_for(src_total, 256), 256, 0, st>>>(D, K, src_total);
+    launches += 2;
+    check();
+    uint32_t *sorted = sort_energy_keys(src_total);
+    k_refine_write<<<grid_for(src_total, 256), 256, 0, st>>>(D, sorted, src_total);
+    launches++;
+    check();
   }
 
   // Outputs.  fin_off still packs the bound sets of the finished subhaloes.

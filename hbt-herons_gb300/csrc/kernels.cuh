@@ -51,6 +51,11 @@ struct KParams
   long long core_min;
   float core_factor;
   int count_interactions;
+  int max_sample;       // MaxSampleSizeOfPotentialEstimate (0 = off)
+  int nosub_mask;       // DoNotSubsampleParticleBitMask
+  int upscale_per_type; // PotentialEstimateUpscaleMassesPerType
+  int refine;           // RefineMostBoundParticle (with subsampling on)
+  float refine_frac;    // BoundFractionCenterRefinement
 };
 
 // Device views of the batch state.
@@ -80,6 +85,9 @@ struct DevState
   int *tail_cnt, *tail_off, *fin_cnt, *fin_off;
   int *sp_cnt, *sp_off;    // correction subhaloes: key-order list lengths and packing
   int *sp_len;             // length of each subhalo's key-order list
+  int *nunsample;          // leading particles exempt from subsampling (CountUnsampledParticles)
+  int *ngrav;              // tree sources of a subsampled iteration (0 = not subsampled)
+  float *factor;           // [6S] mass upscale factor per type of the current iteration
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
   double *root;            // [4S] centre xyz, side length
   float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
@@ -103,6 +111,16 @@ __device__ __forceinline__ int lcp_levels(unsigned long long a, unsigned long lo
 }
 
 __device__ __forceinline__ bool is_tracer_bits(uint8_t t) { return (t & 8u) != 0; }
+__device__ __forceinline__ bool is_nosub_bits(uint8_t t) { return (t & 16u) != 0; }
+
+// EnergySnapshot_t::GetMass (src/subhalo_unbind.cpp:91-101): the particle mass
+// times its type's upscale factor, except for types exempt from subsampling.
+__device__ __forceinline__ float source_mass(const DevState &D, int s, int p)
+{
+  const float m = D.pm[p].w;
+  const uint8_t t = D.ty[p];
+  return is_nosub_bits(t) ? m : __fmul_rn(m, D.factor[6 * s + (t & 7)]);
+}
 
 // ---------------------------------------------------------------------------
 // Set-up
@@ -117,7 +135,8 @@ __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, c
     int t = K.dm_only ? 1 : (type ? (int)type[i] : 1);
     t = t < 0 ? 0 : (t > 5 ? 5 : t);
     const bool tr = K.dm_only || ((1 << t) & K.tracer_mask);
-    D.ty[i] = (uint8_t)(t | (tr ? 8 : 0));
+    const bool ns = !K.dm_only && ((1 << t) & K.nosub_mask);
+    D.ty[i] = (uint8_t)(t | (tr ? 8 : 0) | (ns ? 16 : 0));
     const int s = find_segment<long long>(D.off, D.S, i);
     D.seg_of[i] = s;
     D.ord[i] = (int)i;
@@ -125,7 +144,7 @@ __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, c
   }
 }
 
-__global__ void k_init_subs(DevState D)
+__global__ void k_init_subs(DevState D, KParams K)
 {
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < D.S; s += gridDim.x * blockDim.x)
   {
@@ -139,11 +158,20 @@ __global__ void k_init_subs(DevState D)
     D.wrap[s] = 0;
     D.tracers[s] = 0;
     D.mbound[s] = 0.f;
+    D.ngrav[s] = 0;
+    for (int t = 0; t < 6; t++)
+      D.factor[6 * s + t] = 1.f;
+    // PrepareParticlesForSubsampling put the exempt types first (done by the caller)
+    int ns = 0;
+    if (K.max_sample > 0 && n > K.max_sample)
+      while (ns < n && is_nosub_bits(D.ty[D.off[s] + ns]))
+        ns++;
+    D.nunsample[s] = ns;
   }
 }
 
 // Per-iteration plan: ranges of tree sources, walk targets and partition.
-__global__ void k_plan(DevState D)
+__global__ void k_plan(DevState D, KParams K)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s > D.S)
@@ -160,12 +188,22 @@ __global__ void k_plan(DevState D)
   }
   D.iter[s] += 1;
   int tgt;
+  D.ngrav[s] = 0;
+  for (int t = 0; t < 6; t++)
+    D.factor[6 * s + t] = 1.f;
   if (!D.corr[s])
   {
     D.nlast[s] = D.nbound[s];
     D.src_begin[s] = 0;
     D.src_cnt[s] = D.nlast[s];
     tgt = D.nlast[s];
+    // SetMassUpscaleFactor (src/subhalo_unbind.cpp:374-391): only the leading
+    // MaxSample (+ exempt) particles are tree sources; k_upscale sets the factors
+    if (K.max_sample > 0 && !(D.nlast[s] < K.max_sample + D.nunsample[s]))
+    {
+      D.ngrav[s] = K.max_sample + D.nunsample[s];
+      D.src_cnt[s] = D.ngrav[s];
+    }
   }
   else
   {
@@ -429,8 +467,107 @@ __global__ void k_record_key_order(DevState D, int total)
   if (j >= total)
     return;
   const int s = find_segment<int>(D.src_off, D.S, j);
-  if (!D.corr[s])
+  if (!D.corr[s] && !D.ngrav[s])
     D.sp[D.off[s] + (j - D.src_off[s])] = (int)D.val[j];
+}
+
+// Subsampled subhaloes: the sources are not every candidate, so their
+// correction targets come from the energy-list order instead (packed by part_off).
+__global__ void k_record_candidates(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  if (!D.corr[s] && D.ngrav[s])
+  {
+    const long long g = D.off[s] + (j - D.part_off[s]);
+    D.sp[g] = D.ord[g];
+  }
+}
+
+// Mass upscale factors of the subsampled subhaloes, one block per subhalo
+// (GetMassUpscaleFactor[PerParticleType], src/subhalo_unbind.cpp:290-361).
+// Sums are in double; the factors follow the reference's float formulas.
+__global__ void __launch_bounds__(256) k_upscale(DevState D, KParams K)
+{
+  __shared__ double sh[14][8];
+  for (int s = blockIdx.x; s < D.S; s += gridDim.x)
+  {
+    if (D.state[s] != kActive || D.corr[s] || !D.ngrav[s])
+      continue;
+    const long long off = D.off[s];
+    const int ns = D.nunsample[s], nl = D.nlast[s], ms = K.max_sample;
+    double v[14] = {0.}; // sub[6], tot[6], unsampled, all
+    for (int k = threadIdx.x; k < nl; k += blockDim.x)
+    {
+      const int p = D.ord[off + k];
+      const double m = D.pm[p].w;
+      const int t = D.ty[p] & 7;
+      if (k < ns)
+        v[12] += m;
+      else if (k < ns + ms)
+        v[t] += m;
+      else
+        v[6 + t] += m;
+      v[13] += m;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = 0; q < 14; q++)
+    {
+      double x = v[q];
+      for (int o = 16; o > 0; o >>= 1)
+        x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0)
+        sh[q][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      double tot[14];
+      for (int q = 0; q < 14; q++)
+      {
+        tot[q] = 0.;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++)
+          tot[q] += sh[q][i];
+      }
+      float f[6];
+      if (!K.dm_only && K.upscale_per_type)
+      {
+        float sub[6], all[6];
+        for (int t = 0; t < 6; t++)
+        {
+          sub[t] = (float)tot[t];
+          all[t] = (float)(tot[6 + t] + tot[t]);
+        }
+        for (int t = 0; t < 6; t++)
+          f[t] = sub[t] != 0.f ? __fdiv_rn(all[t], sub[t]) : 0.f;
+        float true_m = 0.f, scaled_m = 0.f;
+        for (int t = 0; t < 6; t++)
+        {
+          true_m = __fadd_rn(true_m, all[t]);
+          scaled_m = __fadd_rn(scaled_m, __fmul_rn(sub[t], f[t]));
+        }
+        const float r = __fdiv_rn(true_m, scaled_m);
+        for (int t = 0; t < 6; t++)
+          f[t] = __fmul_rn(f[t], r);
+      }
+      else
+      {
+        // Mlast: the bound mass of the previous iteration (the initial sum on the first)
+        const float mlast = D.iter[s] == 1 ? (float)tot[13] : D.mbound[s];
+        float msub = 0.f;
+        for (int t = 0; t < 6; t++)
+          msub = (float)((double)msub + tot[t]);
+        const float fac = __fdiv_rn(__fsub_rn(mlast, (float)tot[12]), msub);
+        for (int t = 0; t < 6; t++)
+          f[t] = fac;
+      }
+      for (int t = 0; t < 6; t++)
+        D.factor[6 * s + t] = f[t];
+    }
+    __syncthreads();
+  }
 }
 
 // Correction walks: the bound particles in the key order of the last full
@@ -495,9 +632,10 @@ __global__ void k_prefix_prep(DevState D, int total)
   if (j >= total)
     return;
   const int p = (int)D.val[j];
-  const double *r = D.root + 4 * D.seg_of[p];
+  const int s = D.seg_of[p];
+  const double *r = D.root + 4 * s;
   const float4 x = D.pm[p];
-  const double m = x.w;
+  const double m = source_mass(D, s, p);
   D.P[j] = D4{m, m * ((double)x.x - r[0]), m * ((double)x.y - r[1]), m * ((double)x.z - r[2])};
 }
 
@@ -517,7 +655,7 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   const int base = j + 2 * D.X[j];
   const int p = (int)D.val[j];
   const float4 x = D.pm[p];
-  D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(x.w));
+  D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(source_mass(D, s, p)));
   if (c == 0)
     return;
   const double *r = D.root + 4 * s;
@@ -628,6 +766,7 @@ __device__ __forceinline__ void walk_lane(const float4 *__restrict__ T, int root
   out = sum - comp;
 }
 
+template <bool Count>
 __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_chunks)
 {
   const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -640,22 +779,25 @@ __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_c
     const int t = (c - D.chunk_off[s]) * kWarp + lane;
     const bool valid = t < D.tgt_cnt[s];
     const bool corr = D.corr[s] != 0;
+    const int ngrav = D.ngrav[s];
     int p = 0;
-    if (valid)
-      p = corr ? D.tgt[D.off[s] + t] : (int)D.val[D.src_off[s] + t];
+    if (valid) // correction: key-ordered bound set; subsampled: every candidate; else the sources
+      p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
     const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    // self term: only targets that are tree sources (with their upscaled mass)
+    const float self = (!valid || corr) ? 0.f : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w);
     const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
     float phi = 0.f;
     if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
       ;
     else if (D.wrap[s])
-      walk_lane<true>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+      walk_lane<true>(D.nodes, root, x, valid, self, K, phi, cnt);
     else
-      walk_lane<false>(D.nodes, root, x, valid, corr ? 0.f : x.w, K, phi, cnt);
+      walk_lane<false>(D.nodes, root, x, valid, self, K, phi, cnt);
     if (valid)
       D.pot[p] = phi * K.G_over_a;
   }
-  if (K.count_interactions)
+  if (Count)
   {
     for (int o = 16; o > 0; o >>= 1)
       cnt += __shfl_down_sync(0xffffffffu, cnt, o);
@@ -804,9 +946,16 @@ __global__ void k_after_part(DevState D, KParams K)
     D.state[s] = kDisrupted;
     return;
   }
+  { // CountUnsampledParticles (src/subhalo_unbind.cpp:446-461)
+    int k = 0;
+    const int ns = D.nunsample[s];
+    while (k < ns && is_nosub_bits(D.ty[D.ord[D.off[s] + k]]))
+      k++;
+    D.nunsample[s] = k;
+  }
   const int ndiff = D.nlast[s] - nb;
   D.tail_cnt[s] = ndiff;
-  if (ndiff < nb)
+  if (ndiff < nb && (K.max_sample <= 0 || ndiff < K.max_sample))
   {
     D.corr[s] = 1;
     for (int d = 0; d < 3; d++)
@@ -817,6 +966,58 @@ __global__ void k_after_part(DevState D, KParams K)
   }
   for (int q = 0; q < 7; q++)
     D.com[7 * s + q] = 0.;
+}
+
+// RefineBindingEnergyOrder (src/subhalo_unbind.cpp:395-425, 712-738): for a
+// converged subsampled subhalo, the leading max(MaxSample, fraction*Nbound)
+// particles are re-ordered by their binding energy in the tree of just those
+// particles.  The stored energies are left as they were (so, as in the
+// reference, they are no longer in order there).
+__global__ void k_plan_refine(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > D.S)
+    return;
+  if (s == D.S)
+  {
+    D.src_cnt[s] = D.chunk_cnt[s] = 0;
+    return;
+  }
+  D.src_cnt[s] = D.chunk_cnt[s] = D.tgt_cnt[s] = 0;
+  const int nb = D.nbound[s];
+  if (D.state[s] != kConverged || nb <= K.max_sample)
+    return;
+  const int size = max(K.max_sample, (int)(K.refine_frac * (float)nb));
+  D.src_begin[s] = 0;
+  D.src_cnt[s] = size;
+  D.tgt_cnt[s] = size;
+  D.chunk_cnt[s] = (size + kWarp - 1) / kWarp;
+  D.corr[s] = 0;
+  D.ngrav[s] = 0;
+  for (int t = 0; t < 6; t++)
+    D.factor[6 * s + t] = 1.f;
+}
+
+__global__ void k_refine_keys(DevState D, KParams K, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int p = (int)D.val[j];
+  const int s = D.seg_of[p];
+  const float4 x = D.pm[p], v = D.vu[p];
+  float dv[3];
+  rel_vel(make_float3(x.x, x.y, x.z), make_float3(v.x, v.y, v.z), D.ref_pos + 3 * s, D.ref_vel + 3 * s, K, dv);
+  D.k32[j] = float_to_ordered(__fadd_rn(__fmul_rn(0.5f, norm2_rn(dv)), D.pot[p]));
+}
+
+__global__ void k_refine_write(DevState D, const uint32_t *__restrict__ sorted_val, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  D.ord[D.off[s] + (j - D.src_off[s])] = (int)sorted_val[j];
 }
 
 // Keys for sorting ranges by energy: ordered float, value = particle.

@@ -59,7 +59,8 @@ constexpr size_t kScratchBytes =
   al(kN1) +                                  // ty
   7 * al(sizeof(int) * kN1) +                // seg_of, ord, ord_tmp, sp, tgt + Ep, pot (4 bytes each)
   al(kN1) +                                  // bound flags
-  24 * al(sizeof(int) * kS1) +               // per-subhalo ints
+  26 * al(sizeof(int) * kS1) +               // per-subhalo ints
+  al(sizeof(float) * 6 * kS1) +              // mass upscale factors
   al(sizeof(float) * 8 * kS1) +              // old frame, mbound
   al(sizeof(unsigned) * 6 * kS1) +           // bounding boxes
   al(sizeof(double) * 4 * kS1) +             // root cubes
@@ -202,6 +203,11 @@ KParams noalloc_kparams(const hbtg_params *p)
   K.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
   K.core_min = p->sub_core_size_min;
   K.core_factor = (float)p->sub_core_size_factor;
+  K.max_sample = (int)std::min<int64_t>(p->max_sample_size, 1 << 30);
+  K.nosub_mask = p->no_subsample_mask;
+  K.upscale_per_type = p->upscale_per_type != 0;
+  K.refine = p->refine_most_bound != 0;
+  K.refine_frac = (float)p->refine_fraction;
   K.count_interactions = 0;
   return K;
 }
@@ -210,7 +216,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
 {
   if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
     return HBTG_ERR_INVALID;
-  if (p->max_sample_size > 0)
+  if (p->max_sample_size > 0 && !p->prepared_subsample)
     return HBTG_ERR_UNSUPPORTED;
   if (!(p->softening > 0) || !(p->open_angle > 0) || !(p->box_size > 0))
     return HBTG_ERR_INVALID;
@@ -266,7 +272,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.pot = c.take<float>(kN1);
   int **ints[] = {&D.n_s, &D.nbound, &D.nlast, &D.state, &D.corr, &D.iter, &D.wrap, &D.tracers, &D.nb_new,
                   &D.src_begin, &D.src_cnt, &D.src_off, &D.tgt_cnt, &D.chunk_cnt, &D.chunk_off, &D.part_cnt,
-                  &D.part_off, &D.tail_cnt, &D.tail_off, &D.fin_cnt, &D.fin_off, &D.sp_cnt, &D.sp_off, &D.sp_len};
+                  &D.part_off, &D.tail_cnt, &D.tail_off, &D.fin_cnt, &D.fin_off, &D.sp_cnt, &D.sp_off, &D.sp_len, &D.nunsample, &D.ngrav};
   for (int **pp : ints)
     *pp = c.take<int>(kS1);
   float *subf = c.take<float>(8 * kS1);
@@ -276,6 +282,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   unsigned *bb = c.take<unsigned>(6 * kS1);
   D.bb_lo = bb;
   D.bb_hi = bb ? bb + 3 * kS1 : nullptr;
+  D.factor = c.take<float>(6 * kS1);
   D.root = c.take<double>(4 * kS1);
   D.keyp = c.take<float>(12 * kS1);
   D.com = c.take<double>(7 * kS1);
@@ -318,7 +325,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
     ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
     if (N > 0)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
-    k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D);
+    k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D, R.K);
     R.check();
     R.run();
     OutPtrs O;

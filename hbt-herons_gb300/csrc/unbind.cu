@@ -54,7 +54,7 @@ enum Slot
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND,
+  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_NUM
 };
 
@@ -146,6 +146,11 @@ KParams make_kparams(const hbtg_params *p, bool count)
   K.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
   K.core_min = p->sub_core_size_min;
   K.core_factor = (float)p->sub_core_size_factor;
+  K.max_sample = (int)std::min<int64_t>(p->max_sample_size, 1 << 30);
+  K.nosub_mask = p->no_subsample_mask;
+  K.upscale_per_type = p->upscale_per_type != 0;
+  K.refine = p->refine_most_bound != 0;
+  K.refine_frac = (float)p->refine_fraction;
   K.count_interactions = count ? 1 : 0;
   return K;
 }
@@ -154,8 +159,8 @@ int validate(const hbtg_params *p, const hbtg_batch *b, long long &N)
 {
   if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
     return HBTG_ERR_INVALID;
-  if (p->max_sample_size > 0)
-    return HBTG_ERR_UNSUPPORTED; // potential subsampling is not implemented on the GPU path
+  if (p->max_sample_size > 0 && !p->prepared_subsample)
+    return HBTG_ERR_UNSUPPORTED; // the caller must run PrepareParticlesForSubsampling first
   if (!(p->softening > 0) || !(p->open_angle > 0) || !(p->box_size > 0))
     return HBTG_ERR_INVALID;
   if (b->n_sub > 0 && b->offsets[0] != 0)
@@ -283,14 +288,15 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.Ep = P.get<float>(S_EP, n1);
   D.pot = P.get<float>(S_PHI, n1);
   D.id = reinterpret_cast<const long long *>(b->id);
-  int *subi = P.get<int>(S_SUBI, (size_t)(S + 1) * 26);
+  int *subi = P.get<int>(S_SUBI, (size_t)(S + 1) * 28);
   int q = 0;
   auto nexti = [&]() { return subi + (size_t)(S + 1) * (q++); };
   D.n_s = nexti(); D.nbound = nexti(); D.nlast = nexti(); D.state = nexti(); D.corr = nexti(); D.iter = nexti();
   D.wrap = nexti(); D.tracers = nexti(); D.nb_new = nexti(); D.src_begin = nexti(); D.src_cnt = nexti();
   D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
   D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
-  D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti();
+  D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti(); D.nunsample = nexti(); D.ngrav = nexti();
+  D.factor = P.get<float>(S_FACTOR, (size_t)S * 6);
   float *subf = P.get<float>(S_SUBF, (size_t)S * 8);
   D.old_pos = subf;
   D.old_vel = subf + 3 * (size_t)S;
@@ -332,7 +338,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
     k_repack<<<blocks_for(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
     R.launches++;
   }
-  k_init_subs<<<blocks_for(S, 256), 256, 0, st>>>(D);
+  k_init_subs<<<blocks_for(S, 256), 256, 0, st>>>(D, R.K);
   R.launches++;
   R.check();
   R.run();
@@ -604,6 +610,37 @@ int hbtg_unbind_batch_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b
     return HBTG_ERR_INVALID;
   DevCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream)};
   return guarded(dev_call, &c);
+}
+
+int hbtg_prepare_subsampling(const hbtg_params *p, const hbtg_batch *b, int64_t *perm)
+{
+  if (!p || !b || !perm || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
+    return HBTG_ERR_INVALID;
+  for (int64_t s = 0; s < b->n_sub; s++)
+    if (b->offsets[s + 1] < b->offsets[s])
+      return HBTG_ERR_INVALID;
+  std::srand((unsigned)p->seed);
+  std::vector<int64_t> idx;
+  for (int64_t s = 0; s < b->n_sub; s++)
+  {
+    const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+    idx.resize(n);
+    for (int64_t k = 0; k < n; k++)
+      idx[k] = k;
+    if (p->max_sample_size > 0 && n > p->max_sample_size)
+    {
+      auto exempt = [&](int64_t k) {
+        if (p->dm_only || !b->type)
+          return false;
+        return ((1 << b->type[off + k]) & p->no_subsample_mask) != 0;
+      };
+      auto it = std::partition(idx.begin(), idx.end(), exempt);
+      std::random_shuffle(it, idx.end());
+    }
+    for (int64_t k = 0; k < n; k++)
+      perm[off + k] = idx[k];
+  }
+  return HBTG_OK;
 }
 
 int hbtg_get_stats(const hbtg_handle *h, hbtg_stats *s)

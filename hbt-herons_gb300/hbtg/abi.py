@@ -49,6 +49,7 @@ class Params(C.Structure):
         ("max_iterations", C.c_int32),
         ("mode", C.c_int32),
         ("seed", C.c_int64),
+        ("prepared_subsample", C.c_int32),
     ]
 
     def as_dict(self):
@@ -83,6 +84,7 @@ def default_params(**overrides) -> Params:
     p.max_iterations = 1000
     p.mode = 0
     p.seed = 0
+    p.prepared_subsample = 0
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise KeyError(k)

@@ -27,6 +27,7 @@
 //            (InternalEnergy when thermal energy is used)
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -69,8 +70,21 @@ public:
 
   // Unbinds every subhalo pointed to by `subs` in one GPU call.
   template <class Subhalo>
-  void unbind(const hbtg_params &params, const std::vector<Subhalo *> &subs, const Options &opt)
+  void unbind(const hbtg_params &params_in, const std::vector<Subhalo *> &subs, const Options &opt)
   {
+    hbtg_params params = params_in;
+    if (params.max_sample_size > 0 && !params.prepared_subsample)
+    { // PrepareParticlesForSubsampling, as Unbind does it (src/subhalo_unbind.cpp:430-443, 522-524):
+      // exempt types first, the rest shuffled with the process's rand() sequence
+      for (Subhalo *sub : subs)
+        if ((int64_t)sub->Particles.size() > params.max_sample_size)
+        {
+          auto it = std::partition(sub->Particles.begin(), sub->Particles.end(),
+                                   [&](const auto &p) { return exempt(p, params, opt); });
+          std::random_shuffle(it, sub->Particles.end());
+        }
+      params.prepared_subsample = 1;
+    }
     const int64_t ns = (int64_t)subs.size();
     std::vector<int64_t> offsets(ns + 1, 0);
     for (int64_t s = 0; s < ns; s++)
@@ -142,6 +156,16 @@ public:
   }
 
 private:
+  template <class P>
+  static auto exempt(const P &p, const hbtg_params &prm, const Options &opt) -> decltype((void)p.Type, bool())
+  {
+    return opt.has_types && !prm.dm_only && (((1 << (int)p.Type) & prm.no_subsample_mask) != 0);
+  }
+  template <class P>
+  static bool exempt(const P &, const hbtg_params &, ...)
+  {
+    return false;
+  }
   template <class V, class P>
   static auto set_type(V &type, int64_t g, const P &p, const Options &opt) -> decltype((void)p.Type)
   {

@@ -81,6 +81,10 @@ typedef struct hbtg_params
   int32_t max_iterations;      /* bound on the unbinding loop (no counterpart in the reference) */
   int32_t mode;                /* 0 = reference tree geometry (parity); other values reserved */
   int64_t seed;                /* seeds the tie-break of sub-resolution cells (reference: drand48) */
+  int32_t prepared_subsample;  /* 1 = particles already prepared for subsampling: DoNotSubsample types
+                                  first, the rest in random order (PrepareParticlesForSubsampling,
+                                  src/subhalo_unbind.cpp:430-443).  The GPU path requires it when
+                                  max_sample_size > 0; the subsample is the leading entries. */
 } hbtg_params;
 
 /* A batch of subhaloes in CSR layout: subhalo s owns particles
@@ -164,6 +168,17 @@ int hbtg_unbind_batch(hbtg_handle *handle, const hbtg_params *params, hbtg_batch
  * `cuda_stream` (a cudaStream_t, NULL = legacy default stream) and the call
  * returns after the stream is synchronised. */
 int hbtg_unbind_batch_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch, void *cuda_stream);
+
+/* Host-side PrepareParticlesForSubsampling (src/subhalo_unbind.cpp:430-443,
+ * 522-524) for every subhalo of a batch (host arrays; no device work): for a
+ * subhalo with more than max_sample_size particles, DoNotSubsample types first
+ * (std::partition) and the rest shuffled (std::random_shuffle after
+ * srand(seed), subhaloes in order), exactly as the reference reorders
+ * Particles.  Writes perm[offsets[s]+k] = input local index to place at
+ * position k (identity for the others).  Apply it to the particle arrays, call
+ * hbtg_unbind_batch with prepared_subsample = 1, and compose the returned
+ * order with perm.  Required before the GPU path when max_sample_size > 0. */
+int hbtg_prepare_subsampling(const hbtg_params *params, const hbtg_batch *batch, int64_t *perm);
 
 /* Fills `stats` with the counters of the last call on this handle. */
 int hbtg_get_stats(const hbtg_handle *handle, hbtg_stats *stats);

@@ -203,6 +203,7 @@ extern "C" int ref_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthread
   set_config(p, b);
   EpochSnapshot_t epoch(p->scale_factor, p->hubble);
   srand48(p->seed);
+  srand((unsigned)p->seed);
   if (nthreads <= 0)
     nthreads = omp_get_max_threads();
   if (inner_parallel)

@@ -19,8 +19,11 @@
  *   Snapshot_t::RelativeVelocity          src/snapshot.h:135-148
  *   Subhalo_t::CountParticleTypes         src/subhalo.cpp:311-393
  *   Subhalo_t::GetCorePhaseSpaceProperties src/subhalo_merge.cpp:94-181
- * Potential subsampling (MaxSampleSizeOfPotentialEstimate > 0) is not
- * restated; such calls return HBTG_ERR_UNSUPPORTED.
+ * and potential subsampling (MaxSampleSizeOfPotentialEstimate > 0):
+ *   PrepareParticlesForSubsampling        src/subhalo_unbind.cpp:430-443
+ *   Get/SetMassUpscaleFactor[PerType]     src/subhalo_unbind.cpp:290-391
+ *   CountUnsampledParticles               src/subhalo_unbind.cpp:446-461
+ *   RefineBindingEnergyOrder              src/subhalo_unbind.cpp:395-425
  *
  * Build with -ffp-contract=off (oracle/build_oracle.py) so that no multiply-
  * add is fused: the reference is built the same way for comparison.
@@ -55,6 +58,9 @@ struct Cfg
   bool dm_only, thermal, want_energy, want_potential;
   float G, a, hz;
   int max_iter;
+  int64_t max_sample;
+  bool refine, upscale_per_type, prepare_inside;
+  float refine_frac;
 };
 
 inline double wrap_d(double x, const Cfg &c)
@@ -85,6 +91,7 @@ struct Entry /* ParticleEnergy_t, src/subhalo_unbind.cpp:12-16 */
 };
 
 inline bool is_tracer(const Part &q, const Cfg &c) { return c.dm_only || (((1 << q.type) & c.tracer_mask) != 0); }
+inline bool no_subsample(const Part &q, const Cfg &c) { return !c.dm_only && (((1 << q.type) & c.nosub_mask) != 0); }
 
 /* RelativeVelocity (src/snapshot.h:135-148), all float. */
 inline void rel_vel(const float *x, const float *v, const float *rx, const float *rv, const Cfg &c, float *dv)
@@ -447,22 +454,63 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
   }
   else
   {
+    /* PrepareParticlesForSubsampling (src/subhalo_unbind.cpp:430-443, 522-524) */
+    int64_t nunsample = 0;
+    if (c.max_sample > 0 && n > c.max_sample)
+    {
+      if (c.prepare_inside)
+      {
+        auto it = std::partition(P.begin(), P.end(), [&](const Part &q) { return no_subsample(q, c); });
+        nunsample = it - P.begin();
+        std::random_shuffle(P.begin() + nunsample, P.end());
+      }
+      else
+        while (nunsample < n && no_subsample(P[nunsample], c))
+          nunsample++;
+    }
     for (int64_t i = 0; i < n; i++)
       E[i].p = i;
     nbound = n;
+    /* initial AccumulateMass (src/subhalo_unbind.cpp:537-541) */
+    {
+      if (c.dm_only)
+      {
+        float m = 0.f;
+        for (int64_t i = 0; i < n; i++)
+          m += P[i].m;
+        mbound = m;
+      }
+      else
+      {
+        float mt[HBTG_TYPE_MAX] = {0.f};
+        for (int64_t i = 0; i < n; i++)
+          mt[P[i].type] += P[i].m;
+        float m = 0.f;
+        for (int t = 0; t < HBTG_TYPE_MAX; t++)
+          m += mt[t];
+        mbound = m;
+      }
+    }
     int64_t nlast = n;
     bool correction = false;
     float old_pos[3] = {0, 0, 0}, old_vel[3] = {0, 0, 0};
     Tree tree;
     std::vector<const float *> src_x;
     std::vector<float> src_m;
+    float factor[HBTG_TYPE_MAX] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+    /* EnergySnapshot_t::GetMass with the current upscale factors (src/subhalo_unbind.cpp:91-101) */
+    auto scaled_mass = [&](const Part &q) -> float {
+      if (c.dm_only)
+        return q.m * factor[1];
+      return no_subsample(q, c) ? q.m : q.m * factor[q.type];
+    };
     auto gather_sources = [&](int64_t first, int64_t count) {
       src_x.resize(count);
       src_m.resize(count);
       for (int64_t i = 0; i < count; i++)
       {
         src_x[i] = P[E[first + i].p].x;
-        src_m[i] = P[E[first + i].p].m;
+        src_m[i] = scaled_mass(P[E[first + i].p]);
       }
     };
     for (;;)
@@ -491,14 +539,53 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
       else
       {
         nlast = nbound;
-        gather_sources(0, nlast);
-        tree.build(nlast, src_x.data(), src_m.data(), c);
+        const float mlast = mbound;
+        /* SetMassUpscaleFactor (src/subhalo_unbind.cpp:374-391) */
+        int64_t ngrav = nlast;
+        if (c.max_sample > 0 && !(nlast < c.max_sample + nunsample))
+        {
+          ngrav = c.max_sample + nunsample;
+          if (!c.dm_only && c.upscale_per_type)
+          { /* GetMassUpscaleFactorPerParticleType (src/subhalo_unbind.cpp:323-361) */
+            float sub[HBTG_TYPE_MAX] = {0.f}, tot[HBTG_TYPE_MAX] = {0.f};
+            for (int64_t i = nunsample; i < nunsample + c.max_sample; i++)
+              sub[P[E[i].p].type] += P[E[i].p].m;
+            for (int64_t i = nunsample + c.max_sample; i < nlast; i++)
+              tot[P[E[i].p].type] += P[E[i].p].m;
+            for (int t = 0; t < HBTG_TYPE_MAX; t++)
+              tot[t] += sub[t];
+            for (int t = 0; t < HBTG_TYPE_MAX; t++)
+              factor[t] = sub[t] ? tot[t] / sub[t] : 0.f;
+            float true_m = 0.f, scaled_m = 0.f;
+            for (int t = 0; t < HBTG_TYPE_MAX; t++)
+            {
+              true_m += tot[t];
+              scaled_m += sub[t] * factor[t];
+            }
+            for (int t = 0; t < HBTG_TYPE_MAX; t++)
+              factor[t] *= true_m / scaled_m;
+          }
+          else
+          { /* GetMassUpscaleFactor (src/subhalo_unbind.cpp:290-317) */
+            float munsampled = 0.f;
+            for (int64_t i = 0; i < nunsample; i++)
+              munsampled += P[E[i].p].m;
+            const float mtrue = mlast - munsampled;
+            float msub = 0.f;
+            for (int64_t i = nunsample; i < nunsample + c.max_sample; i++)
+              msub += P[E[i].p].m;
+            for (int t = 0; t < HBTG_TYPE_MAX; t++)
+              factor[t] = mtrue / msub;
+          }
+        }
+        gather_sources(0, ngrav);
+        tree.build(ngrav, src_x.data(), src_m.data(), c);
         g_cells += tree.num_cells();
 #pragma omp parallel for schedule(dynamic, 256) reduction(+ : interactions) if (inner_parallel)
         for (int64_t i = 0; i < nlast; i++)
         {
           const Part &q = P[E[i].p];
-          const double phi = tree.potential(q.x, q.m, &interactions);
+          const double phi = tree.potential(q.x, i < ngrav ? scaled_mass(q) : 0.f, &interactions);
           float dv[3];
           rel_vel(q.x, q.v, ref_pos, ref_vel, c, dv);
           float e = (float)((double)norm2_f(dv) * 0.5 + phi);
@@ -506,6 +593,8 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
             e += q.u;
           E[i].E = e;
         }
+        for (int t = 0; t < HBTG_TYPE_MAX; t++) /* ResetMassUpscaleFactor */
+          factor[t] = 1.f;
       }
       /* RemoveUnboundParticles: stable partition on E < 0 */
       {
@@ -520,6 +609,12 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
             tmp.push_back(E[i]);
         std::copy(tmp.begin(), tmp.end(), E.begin());
         nbound = nb;
+      }
+      { /* CountUnsampledParticles (src/subhalo_unbind.cpp:446-461) */
+        int64_t k = 0;
+        while (k < nunsample && no_subsample(P[E[k].p], c))
+          k++;
+        nunsample = k;
       }
       int64_t tracers = 0;
       if (c.dm_only)
@@ -546,7 +641,7 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
       }
       std::sort(E.begin() + nbound, E.begin() + nlast, [](const Entry &a, const Entry &q) { return a.E < q.E; });
       const int64_t ndiff = nlast - nbound;
-      if (ndiff < nbound)
+      if (ndiff < nbound && (c.max_sample <= 0 || ndiff < c.max_sample))
       {
         correction = true;
         for (int d = 0; d < 3; d++)
@@ -590,6 +685,29 @@ void unbind_one(const Cfg &c, const hbtg_batch *b, int64_t s, bool inner_paralle
       if ((float)nbound >= (float)nlast * c.bmp)
       {
         std::sort(E.begin(), E.begin() + nbound, [](const Entry &a, const Entry &q) { return a.E < q.E; });
+        if (c.max_sample > 0 && c.refine && nbound > c.max_sample)
+        { /* RefineBindingEnergyOrder (src/subhalo_unbind.cpp:395-425, 715-738) */
+          const int64_t size = std::max(c.max_sample, (int64_t)(c.refine_frac * (float)nbound));
+          gather_sources(0, size);
+          tree.build(size, src_x.data(), src_m.data(), c);
+          g_cells += tree.num_cells();
+          std::vector<Entry> inner(size);
+          for (int64_t i = 0; i < size; i++)
+          {
+            const Part &q = P[E[i].p];
+            const double phi = tree.potential(q.x, q.m, &interactions);
+            float dv[3];
+            rel_vel(q.x, q.v, ref_pos, ref_vel, c, dv);
+            inner[i].p = i;
+            inner[i].E = (float)((double)norm2_f(dv) * 0.5 + phi);
+          }
+          std::sort(inner.begin(), inner.end(), [](const Entry &a, const Entry &q) { return a.E < q.E; });
+          std::vector<Entry> moved(size);
+          for (int64_t i = 0; i < size; i++)
+            moved[i] = E[inner[i].p];
+          for (int64_t i = 0; i < size; i++)
+            E[i] = moved[i];
+        }
         std::vector<Part> Q(n);
         for (int64_t i = 0; i < n; i++)
         {
@@ -740,6 +858,11 @@ Cfg make_cfg(const hbtg_params *p, const hbtg_batch *b)
   c.a = (float)p->scale_factor;
   c.hz = (float)p->hubble;
   c.max_iter = p->max_iterations > 0 ? p->max_iterations : 1000000;
+  c.max_sample = p->max_sample_size;
+  c.refine = p->refine_most_bound != 0;
+  c.refine_frac = (float)p->refine_fraction;
+  c.upscale_per_type = p->upscale_per_type != 0;
+  c.prepare_inside = p->prepared_subsample == 0;
   return c;
 }
 
@@ -752,13 +875,12 @@ extern "C" int oracle_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthr
 {
   if (!p || !b || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
     return HBTG_ERR_INVALID;
-  if (p->max_sample_size > 0)
-    return HBTG_ERR_UNSUPPORTED;
   for (int64_t s = 0; s < b->n_sub; s++)
     if (b->offsets[s + 1] < b->offsets[s])
       return HBTG_ERR_INVALID;
   const Cfg c = make_cfg(p, b);
   srand48(p->seed);
+  srand((unsigned)p->seed);
   g_interactions = 0;
   g_cells = 0;
   if (nthreads <= 0)

@@ -23,6 +23,11 @@ CASES = {
     "small_hydro": (lambda: synthetic.small_hydro(seed=0), dict(thermal=1, box_size=200.0)),
     "nfw_10k": (lambda: synthetic.nfw_single(n=10_000, seed=3), dict(dm_only=1, box_size=100.0)),
     "batched_200": (lambda: synthetic.batched(n_sub=200, seed=4, nmax=4000), dict(dm_only=1, box_size=500.0)),
+    # potential subsampling on (the reference default MaxSampleSizeOfPotentialEstimate = 1000)
+    "subsampled_dmo": (lambda: synthetic.batched(n_sub=12, seed=8, nmin=1200, nmax=8000, box=500.0),
+                       dict(dm_only=1, box_size=500.0, max_sample_size=1000)),
+    "subsampled_hydro": (lambda: synthetic.hydro(seed=9, n_sub=8, nmin=1500, nmax=8000, box=300.0),
+                         dict(thermal=1, box_size=300.0, max_sample_size=1000)),
 }
 
 

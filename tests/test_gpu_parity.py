@@ -24,11 +24,23 @@ def _load_golden(path):
     return mod.load(path)
 
 
+def unbind_any(unbinder, inp, prm, **kw):
+    """GPU call; with subsampling on, the particles are first prepared on the host
+    (the reference's PrepareParticlesForSubsampling) and the order composed back."""
+    if prm.max_sample_size > 0 and not prm.prepared_subsample:
+        from hbtg import subsample
+        prep, perm = subsample.prepare(inp, prm)
+        p2 = abi.Params.from_buffer_copy(prm)
+        p2.prepared_subsample = 1
+        return subsample.compose(unbinder.unbind(prep, p2, **kw), inp, perm)
+    return unbinder.unbind(inp, prm, **kw)
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_gpu_matches_reference_golden(unbinder, path):
     inp, prm, ref = _load_golden(path)
-    got = unbinder.unbind(inp, prm)
-    check_invariants(inp, got)
+    got = unbind_any(unbinder, inp, prm)
+    check_invariants(inp, got, sorted_energies=not (prm.max_sample_size > 0 and prm.refine_most_bound))
     m = assert_parity(inp, got, ref, prm)
     assert m["energy_rel_median"] < 1e-5, m
 
@@ -146,3 +158,33 @@ def _subset_out(out, inp, subs):
         else:
             d[k] = v[subs]
     return abi.Outputs(**d)
+
+
+def test_gpu_subsampled_batched_vs_oracle(unbinder):
+    """Potential subsampling (the reference default, MaxSampleSizeOfPotentialEstimate =
+    1000) with RefineMostBoundParticle on a batch that mixes small and large subhaloes."""
+    inp = synthetic.batched(n_sub=400, seed=13, nmax=60_000)
+    prm = abi.parity_params(dm_only=1, box_size=500.0, max_sample_size=1000)
+    got = unbind_any(unbinder, inp, prm)
+    ref = oracle.run_port(inp, prm, nthreads=1)
+    check_invariants(inp, got, sorted_energies=False)
+    assert_parity(inp, got, ref, prm)
+
+
+def test_gpu_subsampled_hydro_per_type_and_total(unbinder):
+    inp = synthetic.hydro(seed=12, n_sub=20, nmin=1500, nmax=20_000, box=300.0)
+    for per_type in (1, 0):
+        prm = abi.parity_params(thermal=1, box_size=300.0, max_sample_size=1000, upscale_per_type=per_type)
+        got = unbind_any(unbinder, inp, prm)
+        ref = oracle.run_port(inp, prm, nthreads=1)
+        check_invariants(inp, got, sorted_energies=False)
+        assert_parity(inp, got, ref, prm)
+
+
+def test_gpu_subsampling_requires_prepared_particles(unbinder):
+    from hbtg.gpu import UnbindError
+    inp = synthetic.batched(n_sub=20, seed=1, nmax=5000)
+    prm = abi.parity_params(dm_only=1, box_size=500.0, max_sample_size=1000)
+    with pytest.raises(UnbindError) as e:
+        unbinder.unbind(inp, prm)
+    assert e.value.code == 5

@@ -23,7 +23,8 @@ def _load(path):
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_port_matches_reference_golden(path):
     inp, prm, ref = _load(path)
-    got = oracle.run_port(inp, prm, nthreads=2, want_potential=True)
+    # one thread: subsampling draws from the process-global rand() sequence
+    got = oracle.run_port(inp, prm, nthreads=1, want_potential=True)
     for k, v in ref.__dict__.items():
         if v is None:
             continue
