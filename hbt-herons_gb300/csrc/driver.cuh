@@ -164,10 +164,31 @@ struct IterationDriver
     check();
   }
 
+  // One tree walk over `chunk_total` packed 32-target chunks.
+  void walk(int chunk_total)
+  {
+    if (chunk_total <= 0)
+      return;
+    if (K.count_interactions)
+      k_walk<true><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+    else
+      k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+    launches++;
+    walk_launches++;
+    check();
+  }
+
   void run()
   {
-    const unsigned sb = grid_for(S + 1, 256);
     mem.mark(-1);
+    iterate();
+    finish();
+  }
+
+  // The lock-step loop until no subhalo is active.
+  void iterate()
+  {
+    const unsigned sb = grid_for(S + 1, 256);
     for (;;)
     {
       k_plan<<<sb, 256, 0, st>>>(D, K);
@@ -195,16 +216,7 @@ struct IterationDriver
       }
       correction_targets();
       mem.mark(2);
-      if (chunk_total > 0)
-      {
-        if (K.count_interactions)
-          k_walk<true><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
-        else
-          k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
-        launches++;
-        walk_launches++;
-        check();
-      }
+      walk(chunk_total);
       mem.mark(1);
       if (part_total > 0)
       {
@@ -245,7 +257,12 @@ struct IterationDriver
         mem.mark(4);
       }
     }
-    // final sort of the bound sets by binding energy
+  }
+
+  // Final sort of the bound sets by binding energy (and RefineBindingEnergyOrder).
+  void finish()
+  {
+    const unsigned sb = grid_for(S + 1, 256);
     k_plan_counts<<<sb, 256, 0, st>>>(D, 1);
     launches++;
     const int fin_total = scan_counts(D.fin_cnt, D.fin_off, S);

@@ -102,6 +102,14 @@ struct DevState
   D4 *P;
   float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
+  int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
+  // warm start (null on the plain path)
+  int *warm = nullptr;       // 1 = started from a proposal, 2 = restarted cold, 3 = warm start verified
+  int *nexcl = nullptr;      // particles the proposal excluded (parked at the end of the segment at the start)
+  int *iter_extra = nullptr; // iterations spent before a cold restart
+  int *flag_s = nullptr;     // per-subhalo scratch flag of the warm-start stages
+  int *self_cnt = nullptr;   // leading targets of a correction-type walk that are also sources
+  float *ref0 = nullptr;     // [6S] input frame, restored for a cold restart
 };
 
 __device__ __forceinline__ int lcp_levels(unsigned long long a, unsigned long long b)
@@ -310,7 +318,9 @@ __global__ void k_root(DevState D, KParams K)
   for (double l = len; l >= (double)K.res && kstar < 1000; l *= 0.5)
     kstar++;
   kp[8] = __int_as_float(kstar);
-  if (D.iter[s] == 1 && !D.corr[s]) // first iteration: the sources are every particle
+  // first iteration: the sources are every particle (a warm start decides the
+  // wrap from every particle before it starts)
+  if (D.iter[s] == 1 && !D.corr[s] && !(D.warm && D.warm[s] == 1))
     D.wrap[s] = K.periodic && (len > (double)K.half);
 }
 
@@ -785,7 +795,9 @@ __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_c
       p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
     const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     // self term: only targets that are tree sources (with their upscaled mass)
-    const float self = (!valid || corr) ? 0.f : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w);
+    const int nself = (corr && D.self_cnt) ? D.self_cnt[s] : 0;
+    const float self =
+      !valid ? 0.f : (corr ? (t < nself ? x.w : 0.f) : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w));
     const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
     float phi = 0.f;
     if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
@@ -933,6 +945,8 @@ __global__ void k_after_part(DevState D, KParams K)
     return;
   const int nb = D.nb_new[s];
   D.nbound[s] = nb;
+  if (D.nb1 && D.iter[s] == 1)
+    D.nb1[s] = nb;
   const int tracers = K.dm_only ? nb : D.tracers[s];
   if (nb < K.min_part || tracers < K.min_tracer)
   {
@@ -1181,12 +1195,10 @@ __global__ void k_com(DevState D, KParams K, int total)
   segmented_flush<7>(out, s, D.com);
 }
 
-// New frame, bound mass and convergence test (src/subhalo_unbind.cpp:687-690).
-__global__ void k_control(DevState D, KParams K)
+// Frame and bound mass from the k_com sums of subhalo s
+// (CentreOfMassReferenceFrame, src/subhalo_unbind.cpp:151-198).
+__device__ void frame_from_sums(DevState &D, const KParams &K, int s)
 {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.S || D.state[s] != kActive)
-    return;
   double c[7];
   for (int q = 0; q < 7; q++)
     c[q] = D.com[7 * s + q];
@@ -1213,6 +1225,15 @@ __global__ void k_control(DevState D, KParams K)
     D.ref_vel[3 * s + d] = (float)(c[4 + d] / M);
   }
   D.mbound[s] = (float)M;
+}
+
+// New frame, bound mass and convergence test (src/subhalo_unbind.cpp:687-690).
+__global__ void k_control(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || D.state[s] != kActive)
+    return;
+  frame_from_sums(D, K, s);
   const int nb = D.nbound[s];
   if ((float)nb >= __fmul_rn((float)D.nlast[s], K.bmp))
     D.state[s] = kConverged;
@@ -1224,6 +1245,9 @@ __global__ void k_plan_counts(DevState D, int mode)
 {
   // mode 0: fin_cnt = nbound of active subhaloes (frame sums)
   // mode 1: fin_cnt = nbound of converged / stopped subhaloes (final sort)
+  // mode 2: fin_cnt = nbound of the subhaloes flagged in flag_s (warm-start
+  //         frames), whose frame sums are zeroed
+  // mode 3: as mode 2 with nlast (the set the last iteration evaluated)
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s > D.S)
     return;
@@ -1233,8 +1257,17 @@ __global__ void k_plan_counts(DevState D, int mode)
     return;
   }
   const int st = D.state[s];
-  const bool take = mode == 0 ? (st == kActive) : (st == kConverged || st == kMaxIter);
-  D.fin_cnt[s] = take ? D.nbound[s] : 0;
+  bool take;
+  if (mode >= 2)
+  {
+    take = D.flag_s[s] != 0;
+    if (take)
+      for (int q = 0; q < 7; q++)
+        D.com[7 * s + q] = 0.;
+  }
+  else
+    take = mode == 0 ? (st == kActive) : (st == kConverged || st == kMaxIter);
+  D.fin_cnt[s] = take ? (mode == 3 ? D.nlast[s] : D.nbound[s]) : 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -1414,7 +1447,7 @@ __global__ void k_epilogue(DevState D, KParams K, OutPtrs O)
   O.tracer_index[s] = ti;
   O.nbound[s] = nb;
   O.mbound[s] = resolved ? D.mbound[s] : 0.f;
-  O.iterations[s] = D.iter[s];
+  O.iterations[s] = D.iter[s] + (D.iter_extra ? D.iter_extra[s] : 0);
   O.status[s] = st == kConverged ? 0 : st == kDisrupted ? 1 : st == kEmpty ? 2 : 3;
   float *mbp = D.mb_pos + 3 * s, *mbv = D.mb_vel + 3 * s;
   if (nb > 0)

@@ -19,6 +19,7 @@
 #include "driver.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
+#include "warm.cuh"
 
 using namespace hbtg;
 
@@ -55,6 +56,7 @@ enum Slot
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
   S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
+  S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
   S_NUM
 };
 
@@ -116,6 +118,15 @@ struct hbtg_handle
   bool count_interactions = false;
   std::vector<cudaEvent_t> walk_events;
   std::vector<cudaEvent_t> phase_events; // phase boundaries of the last call, in order
+  // learned warm start (hbtg_set_model)
+  bool has_model = false;
+  float threshold = 0.5f;
+  long long min_particles = 0;
+  // state of the last unbinding call, for hbtg_trace_labels_device
+  int last_S = 0;
+  long long last_N = 0;
+  int *last_ord = nullptr, *last_nlast = nullptr, *last_state = nullptr, *last_seg = nullptr, *last_nb1 = nullptr;
+  long long *last_off = nullptr;
 };
 
 namespace
@@ -154,6 +165,16 @@ KParams make_kparams(const hbtg_params *p, bool count)
   K.count_interactions = count ? 1 : 0;
   return K;
 }
+
+// What a warm-started call adds to a plain one (device pointers).
+struct WarmArgs
+{
+  const uint8_t *proposal = nullptr; // explicit proposal, or null to run the handle's model
+  const long long *nb_prev = nullptr;
+  const float *e_prev = nullptr;
+  long long min_n = 0;
+  float *features_only = nullptr; // compute the features into this [6N] array and stop
+};
 
 int validate(const hbtg_params *p, const hbtg_batch *b, long long &N)
 {
@@ -228,7 +249,7 @@ struct PoolMem
     HBTG_CUDA(cudaEventRecord(H->phase_events[k], st));
     mark_phase.push_back(phase);
   }
-  // Per-phase totals (ms): 0 plan, 1 walk, 2 tree, 3 partition, 4 frame, 5 final.
+  // Per-phase totals (ms): 0 plan, 1 walk, 2 tree, 3 partition, 4 frame, 5 final, 6 warm-start proposal.
   void phase_totals(double *ms)
   {
     for (size_t k = 1; k < mark_phase.size(); k++)
@@ -242,12 +263,17 @@ struct PoolMem
 };
 
 // The batch with every array on the device (offsets on the host).
-int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaStream_t st)
+int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaStream_t st,
+               const WarmArgs *wa = nullptr)
 {
   long long N = 0;
   int rc = validate(p, b, N);
   if (rc != HBTG_OK)
     return rc;
+  if (wa && p->max_sample_size > 0)
+    return HBTG_ERR_UNSUPPORTED; // the warm start does not combine with potential subsampling
+  if (wa && !wa->proposal && !wa->features_only && !H->has_model)
+    return HBTG_ERR_INVALID; // no model set on the handle
   const int S = (int)b->n_sub;
   H->stats = hbtg_stats{};
   H->stats.n_sub = S;
@@ -296,6 +322,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
   D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
   D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti(); D.nunsample = nexti(); D.ngrav = nexti();
+  D.nb1 = P.get<int>(S_NB1, (size_t)S + 1);
   D.factor = P.get<float>(S_FACTOR, (size_t)S * 6);
   float *subf = P.get<float>(S_SUBF, (size_t)S * 8);
   D.old_pos = subf;
@@ -341,7 +368,67 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   k_init_subs<<<blocks_for(S, 256), 256, 0, st>>>(D, R.K);
   R.launches++;
   R.check();
-  R.run();
+  WarmCounters wc;
+  if (!wa)
+    R.run();
+  else
+  {
+    int *wi = P.get<int>(S_WARMI, (size_t)(S + 1) * 5);
+    D.warm = wi;
+    D.nexcl = wi + (S + 1);
+    D.iter_extra = wi + 2 * (size_t)(S + 1);
+    D.flag_s = wi + 3 * (size_t)(S + 1);
+    D.self_cnt = wi + 4 * (size_t)(S + 1);
+    HBTG_CUDA(cudaMemsetAsync(D.self_cnt, 0, sizeof(int) * (S + 1), st));
+    D.ref0 = P.get<float>(S_REF0, (size_t)S * 6);
+    WarmBufs W;
+    W.nb_prev = wa->nb_prev;
+    W.e_prev = wa->e_prev;
+    W.rmax = P.get<unsigned>(S_RMAX, S);
+    W.mmax = P.get<unsigned>(S_MMAX, 1);
+    W.bb = P.get<unsigned>(S_WBB, (size_t)S * 6);
+    W.hist = P.get<unsigned long long>(S_HIST, (size_t)S * kBins);
+    W.tab = P.get<float>(S_TAB, (size_t)S * kTab);
+    W.feat = wa->features_only;
+    W.prop = wa->proposal;
+    W.min_n = wa->min_n;
+    mem.mark(-1);
+    if (wa->features_only || !wa->proposal)
+    {
+      if (!W.feat)
+        W.feat = P.get<float>(S_FEAT, n1 * kFeat);
+      compute_features(R, W);
+      if (wa->features_only)
+      {
+        HBTG_CUDA(cudaStreamSynchronize(st));
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        H->stats.kernel_launches = R.launches;
+        return HBTG_OK;
+      }
+      float *prob = P.get<float>(S_PROB, n1);
+      uint8_t *prop = P.get<uint8_t>(S_PROP, n1);
+      if (N > 0)
+      {
+        const int mrc = hbtg_mlp_forward(P.get<float>(S_MODEL, HBTG_MLP_PARAMS), W.feat, prob, N, st);
+        if (mrc != HBTG_OK)
+          return mrc;
+        k_propose<<<blocks_for(N, 256), 256, 0, st>>>(prob, H->threshold, prop, N);
+        R.launches += 2;
+        R.check();
+      }
+      W.prop = prop;
+    }
+    warm_run(R, W, wc, !wa->proposal);
+    std::vector<int> warm(S);
+    HBTG_CUDA(cudaMemcpyAsync(warm.data(), D.warm, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+    HBTG_CUDA(cudaStreamSynchronize(st));
+    for (int s = 0; s < S; s++)
+    {
+      wc.warm_subhaloes += warm[s] != 0;
+      wc.restarts += warm[s] == 2;
+    }
+  }
 
   OutPtrs O;
   O.order = reinterpret_cast<long long *>(b->order);
@@ -360,8 +447,22 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   R.epilogue(O);
   HBTG_CUDA(cudaEventRecord(t1, st));
   HBTG_CUDA(cudaEventSynchronize(t1));
-  double phase_ms[6] = {0, 0, 0, 0, 0, 0};
+  H->last_S = S;
+  H->last_N = N;
+  H->last_ord = D.ord;
+  H->last_nlast = D.nlast;
+  H->last_state = D.state;
+  H->last_seg = D.seg_of;
+  H->last_off = off;
+  H->last_nb1 = D.nb1;
+  double phase_ms[7] = {0, 0, 0, 0, 0, 0, 0};
   mem.phase_totals(phase_ms);
+  H->stats.ms_propose = phase_ms[6];
+  H->stats.warm_subhaloes = wc.warm_subhaloes;
+  H->stats.excluded = wc.excluded;
+  H->stats.readmitted = wc.readmitted;
+  H->stats.cold_restarts = wc.restarts;
+  H->stats.readmit_rounds = wc.readmit_rounds;
   H->stats.ms_plan = phase_ms[0];
   H->stats.ms_walk = phase_ms[1];
   H->stats.ms_tree = phase_ms[2];
@@ -455,6 +556,8 @@ struct HostCall
   hbtg_handle *H;
   const hbtg_params *p;
   hbtg_batch *b;
+  bool learned = false;
+  const hbtg_prior *prior = nullptr; // host arrays
 };
 
 int host_call(void *arg)
@@ -495,7 +598,18 @@ int host_call(void *arg)
   d.potential = alloc_out(P, S_POT, b->potential, N);
   d.iterations = alloc_out(P, S_ITER, b->iterations, S);
   d.status = alloc_out(P, S_STAT, b->status, S);
-  rc = run_device(H, c.p, &d, st);
+  WarmArgs wa;
+  if (c.learned)
+  {
+    wa.min_n = H->min_particles;
+    if (c.prior && c.prior->nbound_prev)
+    {
+      wa.nb_prev = reinterpret_cast<const long long *>(upload(P, S_PNB, c.prior->nbound_prev, S, st, h2d));
+      if (c.prior->energy_prev)
+        wa.e_prev = upload(P, S_PEN, c.prior->energy_prev, N, st, h2d);
+    }
+  }
+  rc = run_device(H, c.p, &d, st, c.learned ? &wa : nullptr);
   if (rc != HBTG_OK && rc != HBTG_ERR_MAX_ITER)
     return rc;
   download(b->order, d.order, N, st, d2h);
@@ -527,15 +641,65 @@ struct DevCall
   const hbtg_params *p;
   hbtg_batch *b;
   cudaStream_t st;
+  const WarmArgs *wa = nullptr;
 };
 
 int dev_call(void *arg)
 {
   DevCall &c = *static_cast<DevCall *>(arg);
   HBTG_CUDA(cudaSetDevice(c.H->device));
-  const int rc = run_device(c.H, c.p, c.b, c.st);
+  const int rc = run_device(c.H, c.p, c.b, c.st, c.wa);
   HBTG_CUDA(cudaStreamSynchronize(c.st));
   return rc;
+}
+
+struct ModelCall
+{
+  hbtg_handle *H;
+  const hbtg_model *m;
+};
+
+int model_call(void *arg)
+{
+  ModelCall &c = *static_cast<ModelCall *>(arg);
+  HBTG_CUDA(cudaSetDevice(c.H->device));
+  float *d = c.H->pool.get<float>(S_MODEL, HBTG_MLP_PARAMS);
+  HBTG_CUDA(cudaMemcpy(d, c.m->weights, sizeof(float) * HBTG_MLP_PARAMS, cudaMemcpyHostToDevice));
+  c.H->has_model = true;
+  c.H->threshold = c.m->threshold;
+  c.H->min_particles = c.m->min_particles;
+  return HBTG_OK;
+}
+
+struct LabelCall
+{
+  hbtg_handle *H;
+  uint8_t *labels;
+  int which;
+  cudaStream_t st;
+};
+
+int label_call(void *arg)
+{
+  LabelCall &c = *static_cast<LabelCall *>(arg);
+  hbtg_handle *H = c.H;
+  if (!H->last_ord)
+    return HBTG_ERR_INVALID; // no unbinding call yet
+  HBTG_CUDA(cudaSetDevice(H->device));
+  DevState D;
+  D.S = H->last_S;
+  D.N = H->last_N;
+  D.off = H->last_off;
+  D.ord = H->last_ord;
+  D.nlast = H->last_nlast;
+  D.state = H->last_state;
+  D.seg_of = H->last_seg;
+  D.nb1 = H->last_nb1;
+  if (D.N > 0)
+    k_trace_labels<<<blocks_for(D.N, 256), 256, 0, c.st>>>(D, c.labels, c.which);
+  HBTG_CUDA(cudaGetLastError());
+  HBTG_CUDA(cudaStreamSynchronize(c.st));
+  return HBTG_OK;
 }
 
 } // namespace
@@ -610,6 +774,79 @@ int hbtg_unbind_batch_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b
     return HBTG_ERR_INVALID;
   DevCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream)};
   return guarded(dev_call, &c);
+}
+
+int hbtg_set_model(hbtg_handle *h, const hbtg_model *m)
+{
+  if (!h || !m || !m->weights || !(m->threshold == m->threshold) || m->min_particles < 0)
+    return HBTG_ERR_INVALID;
+  ModelCall c{h, m};
+  return guarded(model_call, &c);
+}
+
+int hbtg_unbind_batch_learned(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b, const hbtg_prior *prior)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  HostCall c{h, p, b, true, prior};
+  return guarded(host_call, &c);
+}
+
+int hbtg_unbind_batch_learned_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b, const hbtg_prior *prior,
+                                     void *cuda_stream)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  WarmArgs wa;
+  wa.min_n = h->min_particles;
+  if (prior && prior->nbound_prev)
+  {
+    wa.nb_prev = reinterpret_cast<const long long *>(prior->nbound_prev);
+    wa.e_prev = prior->energy_prev;
+  }
+  DevCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream), &wa};
+  return guarded(dev_call, &c);
+}
+
+int hbtg_unbind_batch_warm_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b, const uint8_t *proposal,
+                                  int64_t min_particles, void *cuda_stream)
+{
+  if (!h || !b || min_particles < 0)
+    return HBTG_ERR_INVALID;
+  static const uint8_t none = 0;
+  const bool empty = b->n_sub <= 0 || !b->offsets || b->offsets[b->n_sub] <= 0;
+  if (!proposal && !empty)
+    return HBTG_ERR_INVALID;
+  WarmArgs wa;
+  wa.proposal = proposal ? proposal : &none; // an empty batch never reads it
+  wa.min_n = min_particles;
+  DevCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream), &wa};
+  return guarded(dev_call, &c);
+}
+
+int hbtg_features_device(hbtg_handle *h, const hbtg_params *p, const hbtg_batch *b, const hbtg_prior *prior,
+                         float *features, void *cuda_stream)
+{
+  if (!h || !b || !features)
+    return HBTG_ERR_INVALID;
+  WarmArgs wa;
+  wa.features_only = features;
+  if (prior && prior->nbound_prev)
+  {
+    wa.nb_prev = reinterpret_cast<const long long *>(prior->nbound_prev);
+    wa.e_prev = prior->energy_prev;
+  }
+  hbtg_batch copy = *b; // a features-only call writes no output
+  DevCall c{h, p, &copy, static_cast<cudaStream_t>(cuda_stream), &wa};
+  return guarded(dev_call, &c);
+}
+
+int hbtg_trace_labels_device(hbtg_handle *h, uint8_t *labels, int which, void *cuda_stream)
+{
+  if (!h || !labels || which < 0 || which > 1)
+    return HBTG_ERR_INVALID;
+  LabelCall c{h, labels, which, static_cast<cudaStream_t>(cuda_stream)};
+  return guarded(label_call, &c);
 }
 
 int hbtg_prepare_subsampling(const hbtg_params *p, const hbtg_batch *b, int64_t *perm)

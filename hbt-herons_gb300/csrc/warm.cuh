@@ -1,0 +1,772 @@
+// warm.cuh - warm start of the batched unbinding iteration from a proposed
+// set, and the per-particle features of the learned proposer.
+//
+// No counterpart in the reference: Subhalo_t::Unbind always starts from every
+// particle of the subhalo (src/subhalo_unbind.cpp:505-507) and only ever
+// removes particles (stable_partition, src/subhalo_unbind.cpp:35-44).  Here
+// the iteration may start from a proposal and still ends at a verified fixed
+// point:
+//
+//   proposal     each warm subhalo's particles are partitioned proposal-first;
+//                the excluded ones are parked at the end of its segment and the
+//                iteration starts from the proposed set, in that set's
+//                centre-of-mass frame (the frame the reference uses for a set
+//                it evaluates, src/subhalo_unbind.cpp:687)
+//   iteration    the unchanged exact loop (driver.cuh) to convergence
+//   re-admission every particle outside the converged bound set (excluded by
+//                the proposal or removed by the iteration) is evaluated in the
+//                potential and frame that decided the bound set (those of the
+//                set the last iteration evaluated); bound ones join the bound
+//                set, which is checked again in its own potential, after one
+//                more exact iteration when they grow Nbound by more than
+//                BoundMassPrecision allows, until a check finds none (at most
+//                eight checks; the last one accepts what it finds)
+//   fallback     a warm subhalo that disrupts or stops at max_iterations is
+//                restarted cold from its inputs
+//
+// What a proposal should predict: the particles that survive the first exact
+// iteration (E < 0 in the potential of every particle, in the input frame).
+// The warm-started iteration then continues the plain method's own path from
+// its second iteration, in the frame that iteration uses (the centre of mass
+// of the survivors), and skips the most expensive iteration of all (every
+// particle against the tree of every particle).  A wrong proposal only
+// perturbs that path.
+//
+// Features (six per particle, about the input frame):
+//   f0 log(1 + r / r_half)            r_half of the subhalo's radial mass profile
+//   f1 min(|v - V| / v_c, 16)         v_c^2 = (G/a) (M/2) / r_half
+//   f2 E_mono / v_c^2 (clamped 16)    first-iteration energy with the tree replaced by
+//                                     the monopole of every particle: 1/2 |v - V|^2 + phi(r) (+ u)
+//   f3 E_prev / v_c^2 (clamped 16)    previous-output binding energy, 0 if unknown
+//   f4 +1 / -1 / 0                    bound / not bound at the previous output / unknown
+//   f5 species code                   gas 1, DM 0, star -0.5, black hole -1, other 0.25/0.5
+// The profile is 64 bins of a quarter octave below the largest radius,
+// summed in fixed point so that the features are bit-reproducible.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <vector>
+
+#include "common.cuh"
+#include "driver.cuh"
+#include "kernels.cuh"
+#include "primitives.cuh"
+
+namespace hbtg
+{
+namespace
+{
+
+constexpr int kBins = 64;               // quarter-octave bins: 16 octaves below r_max
+constexpr int kTab = 72;                // per subhalo: r_max, 1/r_half, 1/v_c^2, 1/v_c, phi at 65 edges
+constexpr int kFeat = 6;                // features per particle
+constexpr float kQScale = 1073741824.f; // 2^30: fixed-point mass unit = largest particle mass / 2^30
+
+struct WarmBufs
+{
+  const long long *nb_prev; // [S] previous-output Nbound, or null
+  const float *e_prev;      // [N] previous-output binding energies (first nb_prev of each subhalo), or null
+  unsigned *rmax;           // [S] float bits of the largest radius (radii are >= 0)
+  unsigned *mmax;           // [1] float bits of the largest particle mass
+  unsigned *bb;             // [6S] ordered-float bounding box of every particle (lo xyz, hi xyz)
+  unsigned long long *hist; // [64 S] fixed-point mass per radial bin
+  float *tab;               // [kTab S]
+  float *feat;              // [6 N]
+  const uint8_t *prop;      // [N] proposal (1 = start in the set)
+  long long min_n;          // subhaloes with fewer particles start cold
+};
+
+__device__ __forceinline__ bool has_prior(const WarmBufs &W, int s) { return W.nb_prev && W.nb_prev[s] > 0; }
+
+__device__ __forceinline__ float radius_about(float4 x, const float *c, const KParams &K)
+{
+  float d[3] = {__fsub_rn(x.x, c[0]), __fsub_rn(x.y, c[1]), __fsub_rn(x.z, c[2])};
+  if (K.periodic)
+    for (int q = 0; q < 3; q++)
+      d[q] = nearest_f(d[q], K.half, K.box);
+  return sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
+__global__ void k_feat_reset(DevState D, WarmBufs W)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0)
+    *W.mmax = 0u;
+  if (s >= D.S)
+    return;
+  W.rmax[s] = 0u;
+  for (int d = 0; d < 3; d++)
+  {
+    W.bb[6 * s + d] = 0xffffffffu;
+    W.bb[6 * s + 3 + d] = 0u;
+  }
+}
+
+// Largest radius about the input frame, bounding box, largest mass.
+__global__ void k_feat_extent(DevState D, KParams K, WarmBufs W)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < D.N;
+  const int s = valid ? D.seg_of[i] : -1;
+  unsigned r = 0u, m = 0u, lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  if (valid)
+  {
+    const float4 x = D.pm[i];
+    r = __float_as_uint(radius_about(x, D.ref_pos + 3 * s, K));
+    m = __float_as_uint(fmaxf(x.w, 0.f));
+    lo[0] = hi[0] = float_to_ordered(x.x);
+    lo[1] = hi[1] = float_to_ordered(x.y);
+    lo[2] = hi[2] = float_to_ordered(x.z);
+  }
+  const unsigned mm = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && mm)
+    atomicMax(W.mmax, mm);
+  const unsigned peers = __match_any_sync(0xffffffffu, s);
+  r = __reduce_max_sync(peers, r);
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+  {
+    lo[d] = __reduce_min_sync(peers, lo[d]);
+    hi[d] = __reduce_max_sync(peers, hi[d]);
+  }
+  if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+  {
+    atomicMax(&W.rmax[s], r);
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      atomicMin(&W.bb[6 * s + d], lo[d]);
+      atomicMax(&W.bb[6 * s + 3 + d], hi[d]);
+    }
+  }
+}
+
+__device__ __forceinline__ int radial_bin(float r, float rmax)
+{
+  if (!(r > 0.f) || !(rmax > 0.f))
+    return 0;
+  const float t = 4.f * __log2f(r / rmax) + (float)kBins;
+  const int b = (int)floorf(t);
+  return b < 0 ? 0 : (b > kBins - 1 ? kBins - 1 : b);
+}
+
+// Fixed-point mass histogram of every particle about the input centre.  A
+// block whose particles all belong to one subhalo sums in shared memory first.
+constexpr int kHistItems = 8;
+__global__ void __launch_bounds__(256) k_feat_hist(DevState D, KParams K, WarmBufs W)
+{
+  __shared__ unsigned long long sh[kBins];
+  __shared__ int s_one;
+  const long long b0 = (long long)blockIdx.x * blockDim.x * kHistItems;
+  const long long b1 = min(D.N, b0 + (long long)blockDim.x * kHistItems);
+  if (b0 >= D.N)
+    return;
+  if (threadIdx.x == 0)
+    s_one = (D.seg_of[b0] == D.seg_of[b1 - 1]) ? D.seg_of[b0] : -1;
+  if (threadIdx.x < kBins)
+    sh[threadIdx.x] = 0ull;
+  __syncthreads();
+  const float mmax = __uint_as_float(*W.mmax);
+  const int one = s_one;
+  for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+  {
+    const int s = D.seg_of[i];
+    const float4 x = D.pm[i];
+    if (!(x.w > 0.f) || !(mmax > 0.f))
+      continue;
+    const int b = radial_bin(radius_about(x, D.ref_pos + 3 * s, K), __uint_as_float(W.rmax[s]));
+    const unsigned long long q = (unsigned long long)__float2ull_rn(__fmul_rn(__fdiv_rn(x.w, mmax), kQScale));
+    if (one >= 0)
+      atomicAdd(&sh[b], q);
+    else
+      atomicAdd(&W.hist[(long long)kBins * s + b], q);
+  }
+  if (one >= 0)
+  {
+    __syncthreads();
+    if (threadIdx.x < kBins && sh[threadIdx.x])
+      atomicAdd(&W.hist[(long long)kBins * one + threadIdx.x], sh[threadIdx.x]);
+  }
+}
+
+// Per-subhalo profile: half-mass radius, circular speed and the monopole
+// potential at the 65 bin edges e_k = r_max 2^((k-64)/4):
+//   phi(e_k) = -(G/a) [ M(<e_k) / e_k + sum_{b>=k} m_b / (e_b 2^(1/8)) ]
+// One warp per subhalo, two bins per lane.
+__global__ void __launch_bounds__(256) k_feat_profile(DevState D, KParams K, WarmBufs W)
+{
+  const int s = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= D.S)
+    return;
+  float *tab = W.tab + (long long)kTab * s;
+  const double unit = (double)__uint_as_float(*W.mmax) / (double)kQScale;
+  const float rmax = __uint_as_float(W.rmax[s]);
+  const double m0 = (double)W.hist[(long long)kBins * s + 2 * lane] * unit;
+  const double m1 = (double)W.hist[(long long)kBins * s + 2 * lane + 1] * unit;
+  auto edge = [&](int k) { return (double)rmax * exp2((k - kBins) * 0.25); };
+  const double w0 = m0 / (edge(2 * lane) * 1.0905077326652577), w1 = m1 / (edge(2 * lane + 1) * 1.0905077326652577);
+  // inclusive scans of the pair sums
+  double cm = m0 + m1, cw = w0 + w1;
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const double a = __shfl_up_sync(0xffffffffu, cm, o), b = __shfl_up_sync(0xffffffffu, cw, o);
+    if (lane >= o)
+    {
+      cm += a;
+      cw += b;
+    }
+  }
+  const double M = __shfl_sync(0xffffffffu, cm, 31), Wt = __shfl_sync(0xffffffffu, cw, 31);
+  const double C0 = cm - m0 - m1, C1 = C0 + m0;       // M(<e_2l), M(<e_2l+1)
+  const double O0 = Wt - (cw - w0 - w1), O1 = O0 - w0; // outer sums from bins 2l and 2l+1
+  const double g = (double)K.G_over_a;
+  const double rr = (double)rmax;
+  if (rr > 0.)
+  {
+    tab[4 + 2 * lane] = (float)(-g * (C0 / edge(2 * lane) + O0));
+    tab[4 + 2 * lane + 1] = (float)(-g * (C1 / edge(2 * lane + 1) + O1));
+    if (lane == 31)
+      tab[4 + kBins] = (float)(-g * M / rr);
+  }
+  else
+  {
+    tab[4 + 2 * lane] = tab[4 + 2 * lane + 1] = 0.f;
+    if (lane == 31)
+      tab[4 + kBins] = 0.f;
+  }
+  // half-mass radius: the bin where the cumulative mass crosses M/2, log-interpolated
+  const double half = 0.5 * M;
+  double rh = -1.;
+  if (M > 0.)
+  {
+    if (C0 < half && half <= C1 && m0 > 0.)
+      rh = edge(2 * lane) * exp2(0.25 * (half - C0) / m0);
+    else if (C1 < half && half <= C1 + m1 && m1 > 0.)
+      rh = edge(2 * lane + 1) * exp2(0.25 * (half - C1) / m1);
+  }
+  const unsigned has = __ballot_sync(0xffffffffu, rh > 0.);
+  if (has)
+    rh = __shfl_sync(0xffffffffu, rh, __ffs(has) - 1);
+  if (lane == 0)
+  {
+    tab[0] = rmax;
+    if (!(rh > 0.))
+      rh = rr;
+    const double vc2 = (rh > 0.) ? g * half / rh : 0.;
+    tab[1] = rh > 0. ? (float)(1. / rh) : 0.f;
+    tab[2] = vc2 > 0. ? (float)(1. / vc2) : 0.f;
+    tab[3] = vc2 > 0. ? (float)(1. / sqrt(vc2)) : 0.f;
+  }
+}
+
+__device__ __forceinline__ float clamp16(float v) { return fminf(fmaxf(v, -16.f), 16.f); }
+
+// Monopole potential from a subhalo's table, linear in log radius between edges.
+__device__ __forceinline__ float mono_phi(const float *tab, float r)
+{
+  const float rmax = tab[0];
+  if (!(r > 0.f) || !(rmax > 0.f))
+    return tab[4];
+  const float t = 4.f * __log2f(r / rmax) + (float)kBins;
+  if (t <= 0.f)
+    return tab[4];
+  if (t >= (float)kBins)
+    return tab[4 + kBins];
+  const int k = (int)t;
+  const float f = t - (float)k;
+  return tab[4 + k] + f * (tab[5 + k] - tab[4 + k]);
+}
+
+__device__ __forceinline__ float species_code(int t)
+{
+  switch (t)
+  {
+  case 0:
+    return 1.f;
+  case 1:
+    return 0.f;
+  case 4:
+    return -0.5f;
+  case 5:
+    return -1.f;
+  case 2:
+    return 0.25f;
+  default:
+    return 0.5f;
+  }
+}
+
+__global__ void k_features(DevState D, KParams K, WarmBufs W)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
+  {
+    const int s = D.seg_of[i];
+    const float *tab = W.tab + (long long)kTab * s;
+    const float4 x = D.pm[i], v = D.vu[i];
+    const float r = radius_about(x, D.ref_pos + 3 * s, K);
+    float dv[3];
+    rel_vel(make_float3(x.x, x.y, x.z), make_float3(v.x, v.y, v.z), D.ref_pos + 3 * s, D.ref_vel + 3 * s, K, dv);
+    const float v2 = norm2_rn(dv);
+    float e = 0.5f * v2 + mono_phi(tab, r);
+    if (K.thermal)
+      e += v.w;
+    const long long k = i - D.off[s];
+    const int prior = has_prior(W, s) ? (k < W.nb_prev[s] ? 1 : -1) : 0;
+    float *f = W.feat + kFeat * i;
+    f[0] = log1pf(r * tab[1]);
+    f[1] = fminf(sqrtf(v2) * tab[3], 16.f);
+    f[2] = clamp16(e * tab[2]);
+    f[3] = (prior == 1 && W.e_prev) ? clamp16(W.e_prev[i] * tab[2]) : 0.f;
+    f[4] = (float)prior;
+    f[5] = species_code(D.ty[i] & 7);
+  }
+}
+
+__global__ void k_propose(const float *__restrict__ prob, float threshold, uint8_t *__restrict__ prop, long long n)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    prop[i] = prob[i] >= threshold ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Warm start from a proposal
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool warm_eligible(const DevState &D, const WarmBufs &W, int s)
+{
+  return D.state[s] == kActive && (long long)D.n_s[s] >= W.min_n;
+}
+
+__global__ void k_warm_flags(DevState D, WarmBufs W)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > D.N)
+    return;
+  if (i == D.N)
+  {
+    D.flags[i] = 0;
+    return;
+  }
+  const int s = D.seg_of[i];
+  D.flags[i] = (warm_eligible(D, W, s) && W.prop[i]) ? 1 : 0;
+}
+
+// Which subhaloes start warm (a proposal of at least MinNumPartOfSub particles
+// that leaves something out); the input frame is kept for a cold restart.
+__global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S)
+    return;
+  for (int q = 0; q < 3; q++)
+  {
+    D.ref0[6 * s + q] = D.ref_pos[3 * s + q];
+    D.ref0[6 * s + 3 + q] = D.ref_vel[3 * s + q];
+  }
+  D.iter_extra[s] = 0;
+  const int n = D.n_s[s];
+  const int npred = D.F[D.off[s + 1]] - D.F[D.off[s]];
+  const bool warm = warm_eligible(D, W, s) && npred >= max(K.min_part, 1) && npred < n;
+  D.warm[s] = warm ? 1 : 0;
+  D.flag_s[s] = warm ? 1 : 0;
+  D.nexcl[s] = warm ? n - npred : 0;
+  if (!warm)
+    return;
+  D.nbound[s] = npred;
+  D.nlast[s] = npred;
+  // the periodic wrap as a cold start decides it: from every particle's box
+  double len = 0.;
+  for (int d = 0; d < 3; d++)
+  {
+    const double l = (double)ordered_to_float(W.bb[6 * s + 3 + d]) - (double)ordered_to_float(W.bb[6 * s + d]);
+    len = l > len ? l : len;
+  }
+  D.wrap[s] = K.periodic && (len > (double)K.half);
+}
+
+__global__ void k_warm_scatter(DevState D)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.N)
+    return;
+  const int s = D.seg_of[i];
+  if (D.warm[s] != 1)
+    return;
+  const long long off = D.off[s];
+  const int rank = D.F[i] - D.F[off];
+  const int pos = D.flags[i] ? rank : D.nbound[s] + (int)(i - off) - rank;
+  D.ord[off + pos] = (int)i;
+  D.bnd[i] = (uint8_t)D.flags[i];
+}
+
+// Frame and mass of the flagged subhaloes from the k_com sums (no convergence
+// test); `clear` resets the flags.
+__global__ void k_frame_flagged(DevState D, KParams K, int clear)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || !D.flag_s[s])
+    return;
+  if (D.fin_off[s + 1] > D.fin_off[s])
+    frame_from_sums(D, K, s);
+  if (clear)
+    D.flag_s[s] = 0;
+}
+
+// Re-admission plan: each converged warm subhalo becomes active for one more
+// evaluation in the potential of the set its last iteration evaluated
+// (positions [0, Nlast): the sources), the potential that decided its bound
+// set, now for every particle outside the bound set (the targets: those the
+// last iteration removed, which are sources too and keep their self term, and
+// those the proposal excluded or earlier iterations removed).  The walk
+// treats it as a correction walk: targets from the tgt list.
+__global__ void k_plan_readmit(DevState D)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > D.S)
+    return;
+  if (s == D.S)
+  {
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tail_cnt[s] = 0;
+    return;
+  }
+  const bool check = D.warm[s] == 1 && D.state[s] == kConverged && D.nbound[s] < D.n_s[s];
+  D.flag_s[s] = check ? 1 : 0;
+  if (!check)
+  {
+    D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tail_cnt[s] = 0;
+    return;
+  }
+  const int ne = D.n_s[s] - D.nbound[s];
+  D.state[s] = kActive;
+  D.corr[s] = 1;
+  D.ngrav[s] = 0;
+  D.src_begin[s] = 0;
+  D.src_cnt[s] = D.nlast[s];
+  D.self_cnt[s] = D.nlast[s] - D.nbound[s];
+  D.tgt_cnt[s] = ne;
+  D.chunk_cnt[s] = (ne + kWarp - 1) / kWarp;
+  D.part_cnt[s] = ne;
+  D.tail_cnt[s] = ne;
+  D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
+  D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
+}
+
+__global__ void k_readmit_targets(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  const long long off = D.off[s];
+  D.tgt[off + (j - D.part_off[s])] = D.ord[off + D.nbound[s] + (j - D.part_off[s])];
+}
+
+// Binding energy of each target in that potential and frame; flags the bound ones.
+__global__ void k_readmit_energy(DevState D, KParams K, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > total)
+    return;
+  if (j == total)
+  {
+    D.flags[j] = 0;
+    return;
+  }
+  const int s = find_segment<int>(D.part_off, D.S, j);
+  const int p = D.tgt[D.off[s] + (j - D.part_off[s])];
+  const float4 x = D.pm[p], v = D.vu[p];
+  float dv[3];
+  rel_vel(make_float3(x.x, x.y, x.z), make_float3(v.x, v.y, v.z), D.ref_pos + 3 * s, D.ref_vel + 3 * s, K, dv);
+  float e = __fadd_rn(__fmul_rn(0.5f, norm2_rn(dv)), D.pot[p]);
+  if (K.thermal)
+    e = __fadd_rn(e, v.w);
+  D.Ep[p] = e;
+  D.flags[j] = e < 0.f ? 1 : 0;
+}
+
+// New order of positions [nbound, n): the re-admitted particles, then the
+// others, each group in its previous order.
+__global__ void k_readmit_scatter(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.tail_off, D.S, j);
+  const int q = j - D.tail_off[s];
+  const int nb = D.nbound[s];
+  const int base = D.part_off[s];
+  const int r = D.F[D.part_off[s + 1]] - D.F[base];
+  const int rank = D.F[base + q] - D.F[base];
+  const int pos = D.flags[base + q] ? nb + rank : nb + r + (q - rank);
+  const long long off = D.off[s];
+  D.ord_tmp[off + pos] = D.ord[off + nb + q];
+}
+
+__global__ void k_readmit_copy(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int s = find_segment<int>(D.tail_off, D.S, j);
+  const long long g = D.off[s] + D.nbound[s] + (j - D.tail_off[s]);
+  D.ord[g] = D.ord_tmp[g];
+}
+
+__global__ void k_readmit_bnd(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < total && D.flags[j])
+  {
+    const int s = find_segment<int>(D.part_off, D.S, j);
+    D.bnd[D.tgt[D.off[s] + (j - D.part_off[s])]] = 1;
+  }
+}
+
+// Applies the re-admission of the r particles found bound:
+//   r = 0 (or `accept`): verified, no further check;
+//   r grows Nbound by more than BoundMassPrecision allows ((float)Nbound_old <
+//     (float)Nbound_new * BoundMassPrecision, the convergence test read
+//     backwards): the exact iteration runs again, then another check;
+//   otherwise the grown set is checked again in its own potential (Nlast =
+//     Nbound), so that particles the missing ones had kept unbound get back too.
+// Flags every checked subhalo: the frame of its bound set is recomputed.
+__global__ void k_readmit_apply(DevState D, KParams K, int accept)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S || !D.flag_s[s])
+    return;
+  const int r = D.F[D.part_off[s + 1]] - D.F[D.part_off[s]];
+  const int nb = D.nbound[s];
+  D.corr[s] = 0;
+  D.nbound[s] = nb + r;
+  D.self_cnt[s] = 0;
+  D.flag_s[s] = 1;
+  if (r == 0 || accept)
+  {
+    D.state[s] = kConverged;
+    D.warm[s] = 3;
+    return;
+  }
+  const bool again = (float)nb < __fmul_rn((float)(nb + r), K.bmp);
+  D.state[s] = again ? kActive : kConverged;
+  if (!again)
+    D.nlast[s] = nb + r;
+}
+
+// Cold restart of the warm subhaloes that disrupted or stopped.
+__global__ void k_warm_fallback(DevState D)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S)
+    return;
+  const int st = D.state[s];
+  const bool restart = D.warm[s] == 1 && (st == kDisrupted || st == kMaxIter);
+  D.flag_s[s] = restart ? 1 : 0;
+  if (!restart)
+    return;
+  const int n = D.n_s[s];
+  D.warm[s] = 2;
+  D.iter_extra[s] += D.iter[s];
+  D.iter[s] = 0;
+  D.nbound[s] = n;
+  D.nlast[s] = n;
+  D.state[s] = kActive;
+  D.corr[s] = 0;
+  D.wrap[s] = 0;
+  D.tracers[s] = 0;
+  D.mbound[s] = 0.f;
+  D.ngrav[s] = 0;
+  for (int q = 0; q < 3; q++)
+  {
+    D.ref_pos[3 * s + q] = D.ref0[6 * s + q];
+    D.ref_vel[3 * s + q] = D.ref0[6 * s + 3 + q];
+  }
+}
+
+__global__ void k_warm_fallback_particles(DevState D)
+{
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= D.N)
+    return;
+  if (D.flag_s[D.seg_of[i]])
+  {
+    D.ord[i] = (int)i;
+    D.bnd[i] = 1;
+  }
+}
+
+// Training trace, in input order: which = 1 marks the survivors of the first
+// iteration (positions [0, Nbound after it): later iterations only reorder
+// inside that range); which = 0 marks the set whose potential decided the
+// final bound set (positions [0, Nlast) of the last iteration).
+__global__ void k_trace_labels(DevState D, uint8_t *__restrict__ label, int which)
+{
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < D.N; g += (long long)gridDim.x * blockDim.x)
+  {
+    const int s = D.seg_of[g];
+    const long long k = g - D.off[s];
+    const int st = D.state[s];
+    label[D.ord[g]] = (st != kEmpty && k < (which == 1 ? D.nb1[s] : D.nlast[s])) ? 1 : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host orchestration (templated on the driver's memory policy)
+// ---------------------------------------------------------------------------
+struct WarmCounters
+{
+  long long warm_subhaloes = 0, excluded = 0, readmitted = 0, restarts = 0, readmit_rounds = 0;
+};
+
+constexpr int kMaxReadmitRounds = 8; // the last round accepts without another check
+
+// Largest radius, bounding box of every particle and largest mass.
+template <class Mem>
+void compute_extent(IterationDriver<Mem> &R, const WarmBufs &W)
+{
+  DevState &D = R.D;
+  k_feat_reset<<<grid_for(D.S, 256), 256, 0, R.st>>>(D, W);
+  R.launches++;
+  if (D.N > 0)
+  {
+    k_feat_extent<<<grid_for(D.N, 256), 256, 0, R.st>>>(D, R.K, W);
+    R.launches++;
+  }
+  R.check();
+}
+
+template <class Mem>
+void compute_features(IterationDriver<Mem> &R, const WarmBufs &W)
+{
+  DevState &D = R.D;
+  cudaStream_t st = R.st;
+  compute_extent(R, W);
+  R.mem.check(cudaMemsetAsync(W.hist, 0, sizeof(unsigned long long) * kBins * (size_t)D.S, st));
+  if (D.N > 0)
+  {
+    k_feat_hist<<<grid_for(D.N, 256 * kHistItems), 256, 0, st>>>(D, R.K, W);
+    R.launches++;
+  }
+  k_feat_profile<<<grid_for((long long)D.S * 32, 256), 256, 0, st>>>(D, R.K, W);
+  R.launches++;
+  if (D.N > 0)
+  {
+    k_features<<<grid_for(D.N, 256), 256, 0, st>>>(D, R.K, W);
+    R.launches++;
+  }
+  R.check();
+}
+
+// Frame and mass of the subhaloes flagged in flag_s: of their bound sets
+// (mode 2, clears the flags) or of the sets their last iterations evaluated
+// (mode 3, keeps the flags).
+template <class Mem>
+void flagged_frames(IterationDriver<Mem> &R, int mode = 2)
+{
+  DevState &D = R.D;
+  cudaStream_t st = R.st;
+  k_plan_counts<<<grid_for(D.S + 1, 256), 256, 0, st>>>(D, mode);
+  R.launches++;
+  const int total = R.scan_counts(D.fin_cnt, D.fin_off, D.S);
+  if (total > 0)
+  {
+    k_com<<<grid_for((total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, R.K, total);
+    R.launches++;
+  }
+  k_frame_flagged<<<grid_for(D.S, 256), 256, 0, st>>>(D, R.K, mode == 2 ? 1 : 0);
+  R.launches++;
+  R.check();
+}
+
+// Warm start from W.prop, exact iteration, re-admission, cold restart, final
+// sort.  have_extent: compute_features already ran.
+template <class Mem>
+void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool have_extent)
+{
+  DevState &D = R.D;
+  cudaStream_t st = R.st;
+  const int S = D.S;
+  const unsigned sb = grid_for(S, 256);
+  if (!have_extent)
+    compute_extent(R, W); // the periodic-wrap decision of a cold start needs every particle's box
+  if (D.N > 0)
+  {
+    k_warm_flags<<<grid_for(D.N + 1, 256), 256, 0, st>>>(D, W);
+    R.launches++;
+    scan<int, false>(D.flags, D.F, D.N + 1, R.mem.scan_scratch(D.N + 1), st, &R.launches);
+    R.check();
+  }
+  else
+    R.mem.check(cudaMemsetAsync(D.F, 0, sizeof(int), st));
+  k_warm_setup<<<sb, 256, 0, st>>>(D, R.K, W);
+  R.launches++;
+  if (D.N > 0)
+  {
+    k_warm_scatter<<<grid_for(D.N, 256), 256, 0, st>>>(D);
+    R.launches++;
+  }
+  R.check();
+  {
+    std::vector<int> nex(S);
+    R.mem.check(cudaMemcpyAsync(nex.data(), D.nexcl, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+    R.mem.check(cudaStreamSynchronize(st));
+    for (int v : nex)
+      C.excluded += v;
+  }
+  flagged_frames(R); // the proposed set's own frame
+  R.mem.mark(6);
+  R.iterate();
+  for (int round = 0; round < kMaxReadmitRounds; round++)
+  {
+    k_plan_readmit<<<grid_for(S + 1, 256), 256, 0, st>>>(D);
+    R.launches++;
+    R.check();
+    const int src_total = R.scan_counts(D.src_cnt, D.src_off, S);
+    if (src_total == 0)
+      break;
+    const int chunk_total = R.scan_counts(D.chunk_cnt, D.chunk_off, S);
+    const int part_total = R.scan_counts(D.part_cnt, D.part_off, S);
+    const int tail_total = R.scan_counts(D.tail_cnt, D.tail_off, S);
+    C.readmit_rounds++;
+    flagged_frames(R, 3); // the frame that the last evaluation used
+    R.mem.mark(0);
+    R.build_tree(src_total);
+    k_readmit_targets<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+    R.launches++;
+    R.mem.mark(2);
+    R.walk(chunk_total);
+    R.mem.mark(1);
+    k_readmit_energy<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, R.K, part_total);
+    R.launches++;
+    scan<int, false>(D.flags, D.F, part_total + 1, R.mem.scan_scratch(part_total + 1), st, &R.launches);
+    R.check();
+    C.readmitted += R.read_int(D.F + part_total);
+    if (tail_total > 0)
+    {
+      k_readmit_scatter<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
+      k_readmit_copy<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
+      R.launches += 2;
+    }
+    k_readmit_bnd<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+    k_readmit_apply<<<sb, 256, 0, st>>>(D, R.K, round >= kMaxReadmitRounds - 1 ? 1 : 0);
+    R.launches += 2;
+    R.check();
+    flagged_frames(R);
+    R.mem.mark(3);
+    R.iterate();
+  }
+  k_warm_fallback<<<sb, 256, 0, st>>>(D);
+  R.launches++;
+  R.check();
+  if (D.N > 0)
+  {
+    k_warm_fallback_particles<<<grid_for(D.N, 256), 256, 0, st>>>(D);
+    R.launches++;
+  }
+  R.iterate();
+  R.finish();
+}
+
+} // namespace
+} // namespace hbtg

@@ -123,10 +123,26 @@ class CStats(C.Structure):
         ("ms_total", C.c_double), ("ms_walk", C.c_double), ("ms_plan", C.c_double), ("ms_tree", C.c_double),
         ("ms_part", C.c_double), ("ms_frame", C.c_double), ("ms_final", C.c_double), ("walk_launches", C.c_int64),
         ("kernel_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+        ("ms_propose", C.c_double), ("warm_subhaloes", C.c_int64), ("excluded", C.c_int64),
+        ("readmitted", C.c_int64), ("cold_restarts", C.c_int64), ("readmit_rounds", C.c_int64),
     ]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CPrior(C.Structure):
+    """hbtg_prior."""
+    _fields_ = [("nbound_prev", _P), ("energy_prev", _P)]
+
+
+class CModel(C.Structure):
+    """hbtg_model."""
+    _fields_ = [("weights", _P), ("threshold", C.c_float), ("min_particles", C.c_int64)]
+
+
+MLP_PARAMS = 4673
+NUM_FEATURES = 6
 
 
 def _ptr(a):
@@ -149,6 +165,10 @@ class Inputs:
     mostbound_vel: np.ndarray    # float32 [n_sub,3]
     most_bound_id: np.ndarray    # int64 [n_sub]
     meta: dict = field(default_factory=dict)
+    # previous-output knowledge for the warm start (hbtg_prior): particles
+    # [0, prior_nbound[s]) of each subhalo were bound, with energies prior_energy
+    prior_nbound: np.ndarray | None = None   # int64 [n_sub]
+    prior_energy: np.ndarray | None = None   # float32 [N]
 
     @property
     def n_sub(self):
@@ -170,7 +190,8 @@ class Inputs:
         return Inputs(offs, pick(self.pos), pick(self.vel), pick(self.mass), pick(self.id), pick(self.type),
                       pick(self.u), self.ref_pos[subs].copy(), self.ref_vel[subs].copy(),
                       self.mostbound_pos[subs].copy(), self.mostbound_vel[subs].copy(),
-                      self.most_bound_id[subs].copy(), dict(self.meta))
+                      self.most_bound_id[subs].copy(), dict(self.meta),
+                      None if self.prior_nbound is None else self.prior_nbound[subs].copy(), pick(self.prior_energy))
 
     def save(self, path):
         d = {k: getattr(self, k) for k in ("offsets", "pos", "vel", "mass", "id", "ref_pos", "ref_vel",
@@ -179,6 +200,10 @@ class Inputs:
             d["type"] = self.type
         if self.u is not None:
             d["u"] = self.u
+        if self.prior_nbound is not None:
+            d["prior_nbound"] = self.prior_nbound
+        if self.prior_energy is not None:
+            d["prior_energy"] = self.prior_energy
         np.savez_compressed(path, **d)
 
     @staticmethod
@@ -186,7 +211,8 @@ class Inputs:
         z = np.load(path_or_npz) if isinstance(path_or_npz, str) else path_or_npz
         g = lambda k: z[prefix + k] if (prefix + k) in z else None
         return Inputs(g("offsets"), g("pos"), g("vel"), g("mass"), g("id"), g("type"), g("u"), g("ref_pos"),
-                      g("ref_vel"), g("mostbound_pos"), g("mostbound_vel"), g("most_bound_id"))
+                      g("ref_vel"), g("mostbound_pos"), g("mostbound_vel"), g("most_bound_id"), {},
+                      g("prior_nbound"), g("prior_energy"))
 
 
 @dataclass

@@ -32,7 +32,7 @@ def build_library(force=False, verbose=False):
     if not force and not _stale(LIB, deps):
         return LIB
     nvcc = NVCC if os.path.exists(NVCC) else "nvcc"
-    units = [os.path.join(CSRC, f) for f in ("unbind.cu", "noalloc.cu", "probe.cu")]
+    units = [os.path.join(CSRC, f) for f in ("unbind.cu", "noalloc.cu", "probe.cu", "mlp.cu")]
     cmd = [nvcc, *ARCH, *FLAGS, "-I", os.path.join(REPO, "include"), *units, "-o", LIB + ".tmp"]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")

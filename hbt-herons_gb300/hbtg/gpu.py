@@ -11,7 +11,8 @@ import os
 
 import numpy as np
 
-from .abi import CallBuffers, CBatch, CStats, Inputs, Outputs, Params, STATUS_NAMES
+from .abi import (CallBuffers, CBatch, CModel, CPrior, CStats, Inputs, MLP_PARAMS, NUM_FEATURES, Outputs, Params,
+                  STATUS_NAMES)
 from .build import LIB
 
 _lib = None
@@ -42,8 +43,21 @@ def library(path=LIB):
         lib.hbtg_default_params.restype = None
         lib.hbtg_measure_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
         lib.hbtg_measure_fp32_peak.restype = C.c_int
+        P = C.c_void_p
+        lib.hbtg_set_model.argtypes = [P, P]
+        lib.hbtg_unbind_batch_learned.argtypes = [P, P, P, P]
+        lib.hbtg_unbind_batch_learned_device.argtypes = [P, P, P, P, P]
+        lib.hbtg_unbind_batch_warm_device.argtypes = [P, P, P, P, C.c_int64, P]
+        lib.hbtg_features_device.argtypes = [P, P, P, P, P, P]
+        lib.hbtg_trace_labels_device.argtypes = [P, P, C.c_int, P]
+        lib.hbtg_mlp_forward.argtypes = [P, P, P, C.c_int64, P]
+        lib.hbtg_mlp_backward.argtypes = [P, P, P, P, C.c_int64, P, P, P]
+        lib.hbtg_adam_step.argtypes = [P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                       C.c_int, P]
         for fn in ("hbtg_create", "hbtg_destroy", "hbtg_unbind_batch", "hbtg_unbind_batch_device", "hbtg_get_stats",
-                   "hbtg_set_count_interactions"):
+                   "hbtg_set_count_interactions", "hbtg_set_model", "hbtg_unbind_batch_learned",
+                   "hbtg_unbind_batch_learned_device", "hbtg_unbind_batch_warm_device", "hbtg_features_device",
+                   "hbtg_trace_labels_device", "hbtg_mlp_forward", "hbtg_mlp_backward", "hbtg_adam_step"):
             getattr(lib, fn).restype = C.c_int
         _lib = lib
     return _lib
@@ -109,6 +123,70 @@ class Unbinder:
         self.lib.hbtg_get_stats(self.h, C.byref(s))
         return s.as_dict()
 
+    # -- warm start ---------------------------------------------------------
+    def set_model(self, weights, threshold, min_particles=0):
+        """Loads the proposer network (hbtg_set_model)."""
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        if w.shape != (MLP_PARAMS,):
+            raise ValueError("expected %d weights" % MLP_PARAMS)
+        m = CModel(w.ctypes.data, float(threshold), int(min_particles))
+        rc = self.lib.hbtg_set_model(self.h, C.byref(m))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_set_model")
+
+    def unbind_learned(self, inp: Inputs, params: Params, want_energy=True, allow_max_iter=False):
+        """Host-pointer learned warm start (hbtg_unbind_batch_learned); the
+        prior comes from inp.prior_nbound / inp.prior_energy when present."""
+        buf = CallBuffers(inp, want_energy=want_energy)
+        nb = None if inp.prior_nbound is None else np.ascontiguousarray(inp.prior_nbound, dtype=np.int64)
+        en = None if inp.prior_energy is None else np.ascontiguousarray(inp.prior_energy, dtype=np.float32)
+        prior = CPrior(None if nb is None else nb.ctypes.data, None if en is None else en.ctypes.data)
+        rc = self.lib.hbtg_unbind_batch_learned(self.h, C.byref(params), C.byref(buf.c), C.byref(prior))
+        if rc != 0 and not (rc == 4 and allow_max_iter):
+            raise UnbindError(rc, "hbtg_unbind_batch_learned")
+        return buf.out
+
+    def unbind_learned_device(self, params: Params, db, stream_ptr=0, use_prior=True):
+        """Device-pointer learned warm start on a DeviceBatch."""
+        prior = db.cprior() if use_prior else CPrior(None, None)
+        rc = self.lib.hbtg_unbind_batch_learned_device(self.h, C.byref(params), C.byref(db.c), C.byref(prior),
+                                                       C.c_void_p(stream_ptr))
+        if rc != 0 and rc != 4:
+            raise UnbindError(rc, "hbtg_unbind_batch_learned_device")
+        return rc
+
+    def unbind_warm_device(self, params: Params, db, proposal, min_particles=0, stream_ptr=0):
+        """Warm start from an explicit proposal (torch uint8 tensor [N] on the device)."""
+        ptr = proposal.data_ptr() if proposal is not None and proposal.numel() else None
+        rc = self.lib.hbtg_unbind_batch_warm_device(self.h, C.byref(params), C.byref(db.c), ptr,
+                                                    int(min_particles), C.c_void_p(stream_ptr))
+        if rc != 0 and rc != 4:
+            raise UnbindError(rc, "hbtg_unbind_batch_warm_device")
+        return rc
+
+    def features_device(self, params: Params, db, use_prior=True, stream_ptr=0):
+        """The proposer's inputs for a DeviceBatch (in its current frame arrays):
+        a torch float32 tensor [N, 6]."""
+        import torch
+        n = db.inp.n_particles
+        f = torch.empty((max(n, 1), NUM_FEATURES), dtype=torch.float32, device=db.pos.device)
+        prior = db.cprior() if use_prior else CPrior(None, None)
+        rc = self.lib.hbtg_features_device(self.h, C.byref(params), C.byref(db.c), C.byref(prior), f.data_ptr(),
+                                           C.c_void_p(stream_ptr))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_features_device")
+        return f[:n]
+
+    def trace_labels_device(self, n, which=1, device="cuda:0", stream_ptr=0):
+        """Labels of the last call (hbtg_trace_labels_device): torch uint8 [n];
+        which=1 first-iteration survivors, which=0 the last evaluated set."""
+        import torch
+        lab = torch.zeros(max(n, 1), dtype=torch.uint8, device=device)
+        rc = self.lib.hbtg_trace_labels_device(self.h, lab.data_ptr(), int(which), C.c_void_p(stream_ptr))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_trace_labels_device")
+        return lab[:n]
+
 
 class DeviceBatch:
     """Device-resident copy of a batch (torch tensors) and the CBatch pointing at it."""
@@ -145,12 +223,18 @@ class DeviceBatch:
         self.energy = z(max(n, 1), torch.float32) if want_energy else None
         self.iterations = z(ns, torch.int32)
         self.status = z(ns, torch.int32)
+        self.prior_nbound = t(inp.prior_nbound.astype(np.int64)) if inp.prior_nbound is not None else None
+        self.prior_energy = t(inp.prior_energy.astype(np.float32)) if inp.prior_energy is not None else None
         p = lambda x: None if x is None else x.data_ptr()
         self.c = CBatch(ns, self.offsets.ctypes.data, p(self.pos), p(self.vel), p(self.mass), p(self.u), p(self.id),
                         p(self.type), p(self.ref_pos), p(self.ref_vel), p(self.mbp), p(self.mbv), p(self.mbid),
                         p(self.order), p(self.nbound), p(self.mbound), p(self.nbound_type), p(self.mbound_type),
                         p(self.tracer_index), p(self.kin), p(self.core), p(self.energy), None, p(self.iterations),
                         p(self.status))
+
+    def cprior(self):
+        p = lambda x: None if x is None else x.data_ptr()
+        return CPrior(p(self.prior_nbound), p(self.prior_energy))
 
     def reset_inout(self):
         """Restores the in/out frame arrays to the inputs (before each call)."""

@@ -18,6 +18,8 @@ Workloads
   hydro            55% DM, 35% gas (m=0.19, thermal u), 9.9% stars (Hernquist),
                    0.1% black holes (m=50) at the centre; N_p on [100, 2e5]
   precision_host   a 1e7 host (c=5) with satellites, straddling a box face
+  stripped         tidally stripped NFW subhaloes with a previous-output bound
+                   set (training and evaluation of the learned warm start)
 """
 from __future__ import annotations
 
@@ -301,6 +303,60 @@ def precision_host(n_host=10_000_000, n_sat=200, seed=0, box=100.0):
     counts = np.array([len(pos)], np.int64)
     return _finish(pos, vel, np.ones(len(pos)), counts, box, rng,
                    meta=dict(workload="precision_host", seed=seed, box=box, n=len(pos), r200=float(r200h)))
+
+
+def stripped(n_sub=20_000, seed=0, nmin=20, nmax=1_000_000, box=500.0, flip=0.05, with_prior=True):
+    """Tidally stripped NFW subhaloes with a previous-output bound set.
+
+    N_p ~ N^-1.9 on [nmin, nmax]; c ~ logN(ln 8, 0.3).  Each is truncated at a
+    radius U(0.2, 1.5) r_200 (the remnant keeps the Jeans velocities of the
+    untruncated halo), and a fraction U(0, 0.6) of its particles receives a
+    tidal kick of U(0.2, 1.5) v_esc in a random direction.  The previous
+    output's view is the un-kicked particle in the untruncated potential:
+    bound where 1/2 v^2 + phi_NFW(r) < 0, with a fraction `flip` of the
+    memberships flipped at random, and that energy as its binding energy.
+    As in HBT-HERONS, each subhalo lists its previously bound particles first
+    (prior_nbound of them, prior_energy their energies)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    T = _tables()
+    counts = _power_law_counts(rng, nmin, nmax, 1.9, count=n_sub)
+    nh = len(counts)
+    conc = np.exp(rng.normal(np.log(8.0), 0.3, nh))
+    rt_frac = rng.uniform(0.2, 1.5, nh)
+    fkick = rng.uniform(0.0, 0.6, nh)
+    seg = np.repeat(np.arange(nh), counts)
+    n = int(counts.sum())
+    m200 = counts / _m(conc * rt_frac) * _m(conc)  # unit-mass particles fill the truncated remnant
+    r200 = r200_of(m200)
+    rs = (r200 / conc)[seg]
+    xt = (conc * rt_frac)[seg]
+    x = T.inv_m(rng.random(n) * _m(xt)).clip(1e-7, None)
+    r = x * rs
+    pos = _random_dirs(rng, n) * r[:, None]
+    vscale2 = (m200 / (r200 / conc) / _m(conc))[seg]
+    vel = rng.standard_normal((n, 3)) * np.sqrt(vscale2 * T.sigma2_shape(x))[:, None]
+    phi = -vscale2 * np.log1p(x) / x
+    e_prev = 0.5 * np.sum(vel * vel, axis=1) + phi
+    prev = e_prev < 0
+    prev ^= rng.random(n) < flip
+    kicked = rng.random(n) < fkick[seg]
+    k = int(kicked.sum())
+    if k:
+        vesc = np.sqrt(2.0 * -phi[kicked])
+        vel[kicked] += _random_dirs(rng, k) * (rng.uniform(0.2, 1.5, k) * vesc)[:, None]
+    centres = rng.random((nh, 3)) * box
+    bulk = rng.standard_normal((nh, 3)) * 50.0
+    pos = _wrap(pos + centres[seg], box)
+    vel = vel + bulk[seg]
+    # previously bound particles first within each subhalo (stable)
+    order = np.lexsort((~prev, seg))
+    pos, vel, e_prev, prev = pos[order], vel[order], e_prev[order], prev[order]
+    inp = _finish(pos, vel, np.ones(n), counts, box, rng,
+                  meta=dict(workload="stripped", seed=seed, box=box, n_sub=nh, n=n))
+    if with_prior:
+        inp.prior_nbound = np.bincount(seg, weights=prev, minlength=nh).astype(np.int64)
+        inp.prior_energy = e_prev.astype(np.float32)
+    return inp
 
 
 def small_cases(seed=0, box=100.0):

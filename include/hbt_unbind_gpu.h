@@ -144,6 +144,13 @@ typedef struct hbtg_stats
   int64_t walk_launches;
   int64_t kernel_launches;    /* kernels launched by the last call */
   int64_t h2d_bytes, d2h_bytes;
+  /* warm-started calls only (zero otherwise) */
+  double ms_propose;          /* features, network, partition and first frame */
+  int64_t warm_subhaloes;     /* subhaloes started from a proposal */
+  int64_t excluded;           /* particles the proposal left out */
+  int64_t readmitted;         /* particles found bound by the re-admission checks */
+  int64_t cold_restarts;      /* warm subhaloes that disrupted or stopped and were restarted cold */
+  int64_t readmit_rounds;     /* re-admission checks (lock-step) */
 } hbtg_stats;
 
 typedef struct hbtg_handle hbtg_handle;
@@ -209,6 +216,91 @@ int hbtg_unbind_batch_noalloc(const hbtg_params *params, hbtg_batch *batch, void
 /* Measurement utility, no counterpart in the reference: FP32 FMA throughput
  * of the device in TFLOP/s (the roofline denominator of the tree walk). */
 int hbtg_measure_fp32_peak(int device, double *tflops);
+
+/* ------------------------------------------------------------------------
+ * Warm start (no counterpart in the reference, whose Unbind always starts
+ * from every particle, src/subhalo_unbind.cpp:505-507).  The iteration may
+ * start from a proposed set: the particles predicted to survive the first
+ * iteration.  It then runs the exact loop to its convergence test, evaluates
+ * every particle outside the bound set in the potential and frame that
+ * decided the bound set, re-admits the bound ones (checking the grown set
+ * again, after another exact iteration when they grow Nbound beyond
+ * BoundMassPrecision), and restarts cold any warm subhalo that disrupts or
+ * stops.  Outputs have the hbtg_unbind_batch layout.  Not combined with
+ * potential subsampling (max_sample_size must be 0).
+ * ------------------------------------------------------------------------ */
+#define HBTG_MLP_PARAMS 4673 /* weights of the 6-64-64-1 proposer network (layout at hbtg_mlp_forward) */
+#define HBTG_NUM_FEATURES 6  /* per-particle inputs of the proposer network */
+
+/* What the previous output knew about each subhalo.  The reference keeps it in
+ * Subhalo_t: the bound particles first in Particles, Nbound, and
+ * ParticleBindingEnergies (src/subhalo.h:95, src/subhalo_unbind.cpp:787-793). */
+typedef struct hbtg_prior
+{
+  const int64_t *nbound_prev; /* [n_sub] particles [0, nbound_prev[s]) were bound; NULL = unknown */
+  const float *energy_prev;   /* [N] their binding energies (entries past nbound_prev ignored); NULL = unknown */
+} hbtg_prior;
+
+/* The learned proposer: a particle starts in the set when the network's
+ * probability is >= threshold; subhaloes with fewer than min_particles
+ * particles start cold. */
+typedef struct hbtg_model
+{
+  const float *weights; /* [HBTG_MLP_PARAMS] host array */
+  float threshold;
+  int64_t min_particles;
+} hbtg_model;
+
+/* Copies the proposer network to the handle's device. */
+int hbtg_set_model(hbtg_handle *handle, const hbtg_model *model);
+
+/* Learned warm start: features, the network's proposal, then the
+ * warm-started iteration.  Host pointers (prior may be NULL), like
+ * hbtg_unbind_batch. */
+int hbtg_unbind_batch_learned(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
+                              const hbtg_prior *prior);
+
+/* The same with device pointers (offsets on the host, prior arrays on the
+ * device), like hbtg_unbind_batch_device. */
+int hbtg_unbind_batch_learned_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
+                                     const hbtg_prior *prior, void *cuda_stream);
+
+/* Warm start from an explicit proposal ([N] device array, 1 = start in the
+ * set) instead of the network; subhaloes with fewer than min_particles
+ * particles start cold. */
+int hbtg_unbind_batch_warm_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
+                                  const uint8_t *proposal, int64_t min_particles, void *cuda_stream);
+
+/* The proposer's inputs, features[6i..6i+5] of particle i (device array),
+ * computed exactly as the learned call computes them.  batch as for
+ * hbtg_unbind_batch_device; nothing is unbound and no output is written. */
+int hbtg_features_device(hbtg_handle *handle, const hbtg_params *params, const hbtg_batch *batch,
+                         const hbtg_prior *prior, float *features, void *cuda_stream);
+
+/* Training trace of the last unbinding call on this handle, labels[i] in
+ * {0, 1} (device array, input order).  which = 1: particle i survived its
+ * subhalo's first iteration (E < 0 in the potential of every particle; what
+ * the learned proposer predicts).  which = 0: particle i belonged to the set
+ * whose potential decided the final bound set (the tree sources of the last
+ * iteration). */
+int hbtg_trace_labels_device(hbtg_handle *handle, uint8_t *labels, int which, void *cuda_stream);
+
+/* The proposer network on the tensor cores (BF16 operands, FP32
+ * accumulation).  Weights (FP32, device): W1[6][64], b1[64], W2[64][64],
+ * b2[64], w3[64], b3 (matrices in x out);
+ * p = sigmoid(w3 . relu(W2^T relu(W1^T x + b1) + b2) + b3).
+ * prob[i] for features[6i..6i+5]; all device arrays. */
+int hbtg_mlp_forward(const float *weights, const float *features, float *prob, int64_t n, void *cuda_stream);
+
+/* Gradient of sum_i w_i BCE(p_i, y_i) over n rows (sample_weights may be
+ * NULL = 1): grad[HBTG_MLP_PARAMS] and loss[1] are overwritten (device). */
+int hbtg_mlp_backward(const float *weights, const float *features, const float *labels,
+                      const float *sample_weights, int64_t n, float *grad, float *loss, void *cuda_stream);
+
+/* One Adam step on the device: g = grad * grad_scale, bias-corrected moments
+ * at step `step` (>= 1). */
+int hbtg_adam_step(float *weights, const float *grad, float *m, float *v, int n_params, float lr, float beta1,
+                   float beta2, float eps, float grad_scale, int step, void *cuda_stream);
 
 #ifdef __cplusplus
 }
