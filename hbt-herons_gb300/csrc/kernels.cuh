@@ -1247,7 +1247,6 @@ __global__ void k_plan_counts(DevState D, int mode)
   // mode 1: fin_cnt = nbound of converged / stopped subhaloes (final sort)
   // mode 2: fin_cnt = nbound of the subhaloes flagged in flag_s (warm-start
   //         frames), whose frame sums are zeroed
-  // mode 3: as mode 2 with nlast (the set the last iteration evaluated)
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s > D.S)
     return;
@@ -1267,7 +1266,7 @@ __global__ void k_plan_counts(DevState D, int mode)
   }
   else
     take = mode == 0 ? (st == kActive) : (st == kConverged || st == kMaxIter);
-  D.fin_cnt[s] = take ? (mode == 3 ? D.nlast[s] : D.nbound[s]) : 0;
+  D.fin_cnt[s] = take ? D.nbound[s] : 0;
 }
 
 // ---------------------------------------------------------------------------

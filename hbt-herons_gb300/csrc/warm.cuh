@@ -2,35 +2,32 @@
 // set, and the per-particle features of the learned proposer.
 //
 // No counterpart in the reference: Subhalo_t::Unbind always starts from every
-// particle of the subhalo (src/subhalo_unbind.cpp:505-507) and only ever
-// removes particles (stable_partition, src/subhalo_unbind.cpp:35-44).  Here
-// the iteration may start from a proposal and still ends at a verified fixed
-// point:
+// particle of the subhalo (src/subhalo_unbind.cpp:505-507), and its first
+// iteration evaluates every particle against the tree of every particle, the
+// most expensive step of the method.  A proposal predicts that iteration's
+// survivors (E < 0 in the potential of every particle, in the input frame):
 //
-//   proposal     each warm subhalo's particles are partitioned proposal-first;
-//                the excluded ones are parked at the end of its segment and the
-//                iteration starts from the proposed set, in that set's
-//                centre-of-mass frame (the frame the reference uses for a set
-//                it evaluates, src/subhalo_unbind.cpp:687)
-//   iteration    the unchanged exact loop (driver.cuh) to convergence
-//   re-admission every particle outside the converged bound set (excluded by
-//                the proposal or removed by the iteration) is evaluated in the
-//                potential and frame that decided the bound set (those of the
-//                set the last iteration evaluated); bound ones join the bound
-//                set, which is checked again in its own potential, after one
-//                more exact iteration when they grow Nbound by more than
-//                BoundMassPrecision allows, until a check finds none (at most
-//                eight checks; the last one accepts what it finds)
-//   fallback     a warm subhalo that disrupts or stops at max_iterations is
-//                restarted cold from its inputs
-//
-// What a proposal should predict: the particles that survive the first exact
-// iteration (E < 0 in the potential of every particle, in the input frame).
-// The warm-started iteration then continues the plain method's own path from
-// its second iteration, in the frame that iteration uses (the centre of mass
-// of the survivors), and skips the most expensive iteration of all (every
-// particle against the tree of every particle).  A wrong proposal only
-// perturbs that path.
+//   proposal     the particles the proposer trusts start in the set; each warm
+//                subhalo's particles are partitioned trusted-first
+//   first test   every other particle gets the plain method's own first test:
+//                its energy against the tree of every particle, in the input
+//                frame; those with E < 0 join the set.  So nothing the first
+//                iteration would have kept is left out, whatever the proposal
+//   iteration    from that set, in its centre-of-mass frame (the frame the
+//                plain method's second iteration uses), the unchanged exact
+//                loop (driver.cuh) runs to its convergence test, so the path
+//                is the plain method's own from its second iteration on
+//   cold start   a subhalo whose first iteration would already have converged
+//                (the test leaves fewer than 1 - BoundMassPrecision of its
+//                particles out) is restarted cold from its inputs: the warm
+//                start has nothing to save there
+// Where the warm path can leave the plain one: a trusted particle that the
+// first iteration would have removed (the exact loop still removes it, later),
+// and the second iteration, which the plain method usually computes as a
+// correction (energies of the first minus the removed particles' potential,
+// src/subhalo_unbind.cpp:563-621) and the warm path from a new tree of the
+// same set: the two differ by the tree's approximation error, which moves
+// particles with |E| that small across E = 0.
 //
 // Features (six per particle, about the input frame):
 //   f0 log(1 + r / r_half)            r_half of the subhalo's radial mass profile
@@ -352,8 +349,10 @@ __global__ void k_warm_flags(DevState D, WarmBufs W)
   D.flags[i] = (warm_eligible(D, W, s) && W.prop[i]) ? 1 : 0;
 }
 
-// Which subhaloes start warm (a proposal of at least MinNumPartOfSub particles
-// that leaves something out); the input frame is kept for a cold restart.
+// Which subhaloes start warm (the proposal leaves more than 1 -
+// BoundMassPrecision of the particles out: otherwise the first iteration
+// would converge and a cold start costs no more); the input frame is kept for
+// a cold restart.
 __global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -367,7 +366,7 @@ __global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
   D.iter_extra[s] = 0;
   const int n = D.n_s[s];
   const int npred = D.F[D.off[s + 1]] - D.F[D.off[s]];
-  const bool warm = warm_eligible(D, W, s) && npred >= max(K.min_part, 1) && npred < n;
+  const bool warm = warm_eligible(D, W, s) && (float)npred < __fmul_rn((float)n, K.bmp);
   D.warm[s] = warm ? 1 : 0;
   D.flag_s[s] = warm ? 1 : 0;
   D.nexcl[s] = warm ? n - npred : 0;
@@ -413,14 +412,11 @@ __global__ void k_frame_flagged(DevState D, KParams K, int clear)
     D.flag_s[s] = 0;
 }
 
-// Re-admission plan: each converged warm subhalo becomes active for one more
-// evaluation in the potential of the set its last iteration evaluated
-// (positions [0, Nlast): the sources), the potential that decided its bound
-// set, now for every particle outside the bound set (the targets: those the
-// last iteration removed, which are sources too and keep their self term, and
-// those the proposal excluded or earlier iterations removed).  The walk
-// treats it as a correction walk: targets from the tgt list.
-__global__ void k_plan_readmit(DevState D)
+// Plan of the first test: for each warm subhalo, every particle is a tree
+// source (positions [0, n)) and the untrusted ones (positions [nbound, n))
+// are the targets, each keeping its self term.  The walk treats it as a
+// correction walk: targets from the tgt list.
+__global__ void k_plan_first(DevState D)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s > D.S)
@@ -430,20 +426,17 @@ __global__ void k_plan_readmit(DevState D)
     D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tail_cnt[s] = 0;
     return;
   }
-  const bool check = D.warm[s] == 1 && D.state[s] == kConverged && D.nbound[s] < D.n_s[s];
-  D.flag_s[s] = check ? 1 : 0;
-  if (!check)
+  if (D.warm[s] != 1)
   {
     D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tail_cnt[s] = 0;
     return;
   }
   const int ne = D.n_s[s] - D.nbound[s];
-  D.state[s] = kActive;
   D.corr[s] = 1;
   D.ngrav[s] = 0;
   D.src_begin[s] = 0;
-  D.src_cnt[s] = D.nlast[s];
-  D.self_cnt[s] = D.nlast[s] - D.nbound[s];
+  D.src_cnt[s] = D.n_s[s];
+  D.self_cnt[s] = ne;
   D.tgt_cnt[s] = ne;
   D.chunk_cnt[s] = (ne + kWarp - 1) / kWarp;
   D.part_cnt[s] = ne;
@@ -462,7 +455,8 @@ __global__ void k_readmit_targets(DevState D, int total)
   D.tgt[off + (j - D.part_off[s])] = D.ord[off + D.nbound[s] + (j - D.part_off[s])];
 }
 
-// Binding energy of each target in that potential and frame; flags the bound ones.
+// First-iteration energy of each target (the potential of every particle,
+// the input frame; src/subhalo_unbind.cpp:563-580); flags the bound ones.
 __global__ void k_readmit_energy(DevState D, KParams K, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -485,7 +479,7 @@ __global__ void k_readmit_energy(DevState D, KParams K, int total)
   D.flags[j] = e < 0.f ? 1 : 0;
 }
 
-// New order of positions [nbound, n): the re-admitted particles, then the
+// New order of positions [nbound, n): the particles the test keeps, then the
 // others, each group in its previous order.
 __global__ void k_readmit_scatter(DevState D, int total)
 {
@@ -523,45 +517,39 @@ __global__ void k_readmit_bnd(DevState D, int total)
   }
 }
 
-// Applies the re-admission of the r particles found bound:
-//   r = 0 (or `accept`): verified, no further check;
-//   r grows Nbound by more than BoundMassPrecision allows ((float)Nbound_old <
-//     (float)Nbound_new * BoundMassPrecision, the convergence test read
-//     backwards): the exact iteration runs again, then another check;
-//   otherwise the grown set is checked again in its own potential (Nlast =
-//     Nbound), so that particles the missing ones had kept unbound get back too.
-// Flags every checked subhalo: the frame of its bound set is recomputed.
-__global__ void k_readmit_apply(DevState D, KParams K, int accept)
+// After the first test: the set is the trusted particles plus the r the test
+// kept.  A subhalo whose first iteration would already have converged
+// ((float)Nbound >= (float)N * BoundMassPrecision, src/subhalo_unbind.cpp:690)
+// is marked for a cold restart; the others are flagged for their first frame.
+__global__ void k_first_apply(DevState D, KParams K)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.S || !D.flag_s[s])
+  if (s >= D.S)
+    return;
+  D.flag_s[s] = 0;
+  if (D.warm[s] != 1)
     return;
   const int r = D.F[D.part_off[s + 1]] - D.F[D.part_off[s]];
-  const int nb = D.nbound[s];
+  const int nb = D.nbound[s] + r;
+  D.nbound[s] = nb;
+  D.nlast[s] = nb;
   D.corr[s] = 0;
-  D.nbound[s] = nb + r;
   D.self_cnt[s] = 0;
-  D.flag_s[s] = 1;
-  if (r == 0 || accept)
-  {
-    D.state[s] = kConverged;
-    D.warm[s] = 3;
-    return;
-  }
-  const bool again = (float)nb < __fmul_rn((float)(nb + r), K.bmp);
-  D.state[s] = again ? kActive : kConverged;
-  if (!again)
-    D.nlast[s] = nb + r;
+  D.nexcl[s] = D.n_s[s] - nb;
+  D.iter_extra[s] = 1; // the first iteration, done by the proposal and the test
+  if ((float)nb >= __fmul_rn((float)D.n_s[s], K.bmp))
+    D.warm[s] = 4;
+  else
+    D.flag_s[s] = 1;
 }
 
-// Cold restart of the warm subhaloes that disrupted or stopped.
+// Cold restart of the warm subhaloes marked for it (warm = 4).
 __global__ void k_warm_fallback(DevState D)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= D.S)
     return;
-  const int st = D.state[s];
-  const bool restart = D.warm[s] == 1 && (st == kDisrupted || st == kMaxIter);
+  const bool restart = D.warm[s] == 4;
   D.flag_s[s] = restart ? 1 : 0;
   if (!restart)
     return;
@@ -619,8 +607,6 @@ struct WarmCounters
   long long warm_subhaloes = 0, excluded = 0, readmitted = 0, restarts = 0, readmit_rounds = 0;
 };
 
-constexpr int kMaxReadmitRounds = 8; // the last round accepts without another check
-
 // Largest radius, bounding box of every particle and largest mass.
 template <class Mem>
 void compute_extent(IterationDriver<Mem> &R, const WarmBufs &W)
@@ -658,15 +644,13 @@ void compute_features(IterationDriver<Mem> &R, const WarmBufs &W)
   R.check();
 }
 
-// Frame and mass of the subhaloes flagged in flag_s: of their bound sets
-// (mode 2, clears the flags) or of the sets their last iterations evaluated
-// (mode 3, keeps the flags).
+// Frame and mass of the bound sets of the subhaloes flagged in flag_s (clears the flags).
 template <class Mem>
-void flagged_frames(IterationDriver<Mem> &R, int mode = 2)
+void flagged_frames(IterationDriver<Mem> &R)
 {
   DevState &D = R.D;
   cudaStream_t st = R.st;
-  k_plan_counts<<<grid_for(D.S + 1, 256), 256, 0, st>>>(D, mode);
+  k_plan_counts<<<grid_for(D.S + 1, 256), 256, 0, st>>>(D, 2);
   R.launches++;
   const int total = R.scan_counts(D.fin_cnt, D.fin_off, D.S);
   if (total > 0)
@@ -674,13 +658,61 @@ void flagged_frames(IterationDriver<Mem> &R, int mode = 2)
     k_com<<<grid_for((total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, R.K, total);
     R.launches++;
   }
-  k_frame_flagged<<<grid_for(D.S, 256), 256, 0, st>>>(D, R.K, mode == 2 ? 1 : 0);
+  k_frame_flagged<<<grid_for(D.S, 256), 256, 0, st>>>(D, R.K, 1);
   R.launches++;
   R.check();
 }
 
-// Warm start from W.prop, exact iteration, re-admission, cold restart, final
-// sort.  have_extent: compute_features already ran.
+// The plain method's first test for the untrusted particles of the warm
+// subhaloes (see k_plan_first); returns how many it keeps.
+template <class Mem>
+long long first_test(IterationDriver<Mem> &R)
+{
+  DevState &D = R.D;
+  cudaStream_t st = R.st;
+  const int S = D.S;
+  k_plan_first<<<grid_for(S + 1, 256), 256, 0, st>>>(D);
+  R.launches++;
+  R.check();
+  const int src_total = R.scan_counts(D.src_cnt, D.src_off, S);
+  const int chunk_total = R.scan_counts(D.chunk_cnt, D.chunk_off, S);
+  const int part_total = R.scan_counts(D.part_cnt, D.part_off, S);
+  const int tail_total = R.scan_counts(D.tail_cnt, D.tail_off, S);
+  R.mem.mark(6);
+  if (src_total > 0)
+    R.build_tree(src_total);
+  if (part_total > 0)
+  {
+    k_readmit_targets<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+    R.launches++;
+  }
+  R.mem.mark(2);
+  R.walk(chunk_total);
+  R.mem.mark(1);
+  k_readmit_energy<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, R.K, part_total);
+  R.launches++;
+  scan<int, false>(D.flags, D.F, part_total + 1, R.mem.scan_scratch(part_total + 1), st, &R.launches);
+  R.check();
+  const long long kept = R.read_int(D.F + part_total);
+  if (tail_total > 0)
+  {
+    k_readmit_scatter<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
+    k_readmit_copy<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
+    R.launches += 2;
+  }
+  if (part_total > 0)
+  {
+    k_readmit_bnd<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+    R.launches++;
+  }
+  k_first_apply<<<grid_for(S, 256), 256, 0, st>>>(D, R.K);
+  R.launches++;
+  R.check();
+  return kept;
+}
+
+// Warm start from W.prop: partition, first test, cold restarts, first frame,
+// exact iteration, final sort.  have_extent: compute_features ran.
 template <class Mem>
 void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool have_extent)
 {
@@ -707,6 +739,8 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     R.launches++;
   }
   R.check();
+  C.readmitted += first_test(R);
+  C.readmit_rounds++;
   {
     std::vector<int> nex(S);
     R.mem.check(cudaMemcpyAsync(nex.data(), D.nexcl, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
@@ -714,56 +748,16 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     for (int v : nex)
       C.excluded += v;
   }
-  flagged_frames(R); // the proposed set's own frame
-  R.mem.mark(6);
-  R.iterate();
-  for (int round = 0; round < kMaxReadmitRounds; round++)
-  {
-    k_plan_readmit<<<grid_for(S + 1, 256), 256, 0, st>>>(D);
-    R.launches++;
-    R.check();
-    const int src_total = R.scan_counts(D.src_cnt, D.src_off, S);
-    if (src_total == 0)
-      break;
-    const int chunk_total = R.scan_counts(D.chunk_cnt, D.chunk_off, S);
-    const int part_total = R.scan_counts(D.part_cnt, D.part_off, S);
-    const int tail_total = R.scan_counts(D.tail_cnt, D.tail_off, S);
-    C.readmit_rounds++;
-    flagged_frames(R, 3); // the frame that the last evaluation used
-    R.mem.mark(0);
-    R.build_tree(src_total);
-    k_readmit_targets<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
-    R.launches++;
-    R.mem.mark(2);
-    R.walk(chunk_total);
-    R.mem.mark(1);
-    k_readmit_energy<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, R.K, part_total);
-    R.launches++;
-    scan<int, false>(D.flags, D.F, part_total + 1, R.mem.scan_scratch(part_total + 1), st, &R.launches);
-    R.check();
-    C.readmitted += R.read_int(D.F + part_total);
-    if (tail_total > 0)
-    {
-      k_readmit_scatter<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
-      k_readmit_copy<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
-      R.launches += 2;
-    }
-    k_readmit_bnd<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
-    k_readmit_apply<<<sb, 256, 0, st>>>(D, R.K, round >= kMaxReadmitRounds - 1 ? 1 : 0);
-    R.launches += 2;
-    R.check();
-    flagged_frames(R);
-    R.mem.mark(3);
-    R.iterate();
-  }
-  k_warm_fallback<<<sb, 256, 0, st>>>(D);
+  flagged_frames(R); // the frame of the set the second iteration evaluates
+  k_warm_fallback<<<sb, 256, 0, st>>>(D); // subhaloes whose first iteration converges run cold
   R.launches++;
-  R.check();
   if (D.N > 0)
   {
     k_warm_fallback_particles<<<grid_for(D.N, 256), 256, 0, st>>>(D);
     R.launches++;
   }
+  R.check();
+  R.mem.mark(3);
   R.iterate();
   R.finish();
 }

@@ -6,11 +6,11 @@ and proposes the set the iteration starts from.  It is trained here, on the
 GPU, by the library's own tensor-core kernels (hbtg_mlp_backward,
 hbtg_adam_step), on traces the plain method generates: the label of a
 particle is 1 when it survived its subhalo's first exact iteration
-(hbtg_trace_labels_device, which=1).  The warm-started iteration then takes
-the plain method's own path from its second iteration and skips the most
-expensive one (every particle against the tree of every particle); the
-re-admission checks and the cold restart inside the library keep the result
-a verified fixed point whatever the proposal.
+(hbtg_trace_labels_device, which=1).  Particles the network trusts skip that
+iteration, the most expensive one of the method (every particle against the
+tree of every particle); the library gives every other particle the
+iteration's own test, so nothing it would have kept is lost, and then takes
+the plain method's own path from its second iteration.
 
 Model files (.npz): weights (float32 [4673]), threshold, min_particles and a
 JSON description of the training run.
@@ -150,17 +150,18 @@ def traces(unbinder, inp, params, use_prior=True, device="cuda:0"):
     return feats, labels
 
 
-def choose_threshold(prob, labels, fn_weight=3.0):
-    """The probability cut minimising fn_weight * false negatives + false
-    positives (a member left out costs more than an extra one: it perturbs
-    the potential until a re-admission check finds it)."""
+def choose_threshold(prob, labels, fp_weight=50.0):
+    """The probability cut minimising fp_weight * false positives + false
+    negatives.  A survivor the network does not trust only costs one more
+    target in the first test; a trusted particle that the first iteration
+    would have removed moves the warm path off the plain one."""
     pos = labels > 0.5
     best, best_t, best_err = None, 0.5, 0.0
     for t in np.linspace(0.02, 0.98, 49):
         pred = prob >= float(t)
         fn = int((~pred & pos).sum().item())
         fp = int((pred & ~pos).sum().item())
-        cost = fn_weight * fn + fp
+        cost = fp_weight * fp + fn
         if best is None or cost < best:
             best, best_t, best_err = cost, float(t), (fn + fp) / max(len(labels), 1)
     return best_t, best_err

@@ -147,10 +147,10 @@ typedef struct hbtg_stats
   /* warm-started calls only (zero otherwise) */
   double ms_propose;          /* features, network, partition and first frame */
   int64_t warm_subhaloes;     /* subhaloes started from a proposal */
-  int64_t excluded;           /* particles the proposal left out */
-  int64_t readmitted;         /* particles found bound by the re-admission checks */
-  int64_t cold_restarts;      /* warm subhaloes that disrupted or stopped and were restarted cold */
-  int64_t readmit_rounds;     /* re-admission checks (lock-step) */
+  int64_t excluded;           /* particles left out after the first test */
+  int64_t readmitted;         /* untrusted particles the first test kept */
+  int64_t cold_restarts;      /* warm subhaloes restarted cold (their first iteration converges) */
+  int64_t readmit_rounds;     /* first tests run (lock-step) */
 } hbtg_stats;
 
 typedef struct hbtg_handle hbtg_handle;
@@ -219,15 +219,16 @@ int hbtg_measure_fp32_peak(int device, double *tflops);
 
 /* ------------------------------------------------------------------------
  * Warm start (no counterpart in the reference, whose Unbind always starts
- * from every particle, src/subhalo_unbind.cpp:505-507).  The iteration may
- * start from a proposed set: the particles predicted to survive the first
- * iteration.  It then runs the exact loop to its convergence test, evaluates
- * every particle outside the bound set in the potential and frame that
- * decided the bound set, re-admits the bound ones (checking the grown set
- * again, after another exact iteration when they grow Nbound beyond
- * BoundMassPrecision), and restarts cold any warm subhalo that disrupts or
- * stops.  Outputs have the hbtg_unbind_batch layout.  Not combined with
- * potential subsampling (max_sample_size must be 0).
+ * from every particle, src/subhalo_unbind.cpp:505-507, and spends most of its
+ * time on that first iteration).  A proposal marks the particles predicted
+ * to survive the first iteration.  Those are trusted; every other particle
+ * gets the first iteration's own test (its energy against the tree of every
+ * particle, in the input frame) and joins the set when bound.  From that set
+ * the exact loop runs to its convergence test, the plain method's own path
+ * from its second iteration on.  A subhalo whose first iteration would
+ * already converge runs cold.  Outputs have the hbtg_unbind_batch layout;
+ * `iterations` counts the first iteration.  Not combined with potential subsampling (max_sample_size
+ * must be 0).
  * ------------------------------------------------------------------------ */
 #define HBTG_MLP_PARAMS 4673 /* weights of the 6-64-64-1 proposer network (layout at hbtg_mlp_forward) */
 #define HBTG_NUM_FEATURES 6  /* per-particle inputs of the proposer network */
@@ -241,7 +242,7 @@ typedef struct hbtg_prior
   const float *energy_prev;   /* [N] their binding energies (entries past nbound_prev ignored); NULL = unknown */
 } hbtg_prior;
 
-/* The learned proposer: a particle starts in the set when the network's
+/* The learned proposer: a particle is trusted when the network's
  * probability is >= threshold; subhaloes with fewer than min_particles
  * particles start cold. */
 typedef struct hbtg_model
@@ -265,9 +266,9 @@ int hbtg_unbind_batch_learned(hbtg_handle *handle, const hbtg_params *params, hb
 int hbtg_unbind_batch_learned_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
                                      const hbtg_prior *prior, void *cuda_stream);
 
-/* Warm start from an explicit proposal ([N] device array, 1 = start in the
- * set) instead of the network; subhaloes with fewer than min_particles
- * particles start cold. */
+/* Warm start from an explicit proposal ([N] device array, 1 = trusted)
+ * instead of the network; subhaloes with fewer than min_particles particles
+ * start cold. */
 int hbtg_unbind_batch_warm_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
                                   const uint8_t *proposal, int64_t min_particles, void *cuda_stream);
 

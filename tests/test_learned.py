@@ -163,6 +163,21 @@ def _plain_and_trace(u, inp, params):
     return db, plain, u.trace_labels_device(inp.n_particles, which=1)
 
 
+# The warm path computes the second iteration from a new tree of the set the
+# plain method reaches by correcting its first-iteration energies; the two
+# differ by the tree's approximation error (opening angle 0.45), which moves
+# particles with |E| that small across E = 0.  On these small, marginal test
+# batches that is a few 1e-4 of the bound mass, of either sign.
+PATH_NOISE = 6e-4
+
+
+def _statuses_agree(inp, got, ref, params):
+    from parity import near_disruption
+    bad = [s for s in np.nonzero(got.status != ref.status)[0]
+           if not (near_disruption(inp, got, s, params) or near_disruption(inp, ref, s, params))]
+    assert not bad, bad
+
+
 @pytest.mark.gpu
 def test_warm_start_from_first_iteration_trace_keeps_the_plain_fixed_point(unbinder):
     """The ideal proposal (the plain run's own first-iteration survivors): the
@@ -182,17 +197,17 @@ def test_warm_start_from_first_iteration_trace_keeps_the_plain_fixed_point(unbin
         unbinder.count_interactions(False)
     check_invariants(inp, plain)
     check_invariants(inp, warm)
+    _statuses_agree(inp, warm, plain, params)
     m = compare(inp, warm, plain)
-    assert np.array_equal(warm.status, plain.status)
-    assert m["mass_rel"] <= 1e-4 and m["membership"] <= 1e-3, m
-    assert st["warm_subhaloes"] > 0
+    assert m["mass_rel"] <= PATH_NOISE and m["membership"] <= 2 * PATH_NOISE, m
+    assert st["warm_subhaloes"] > 0 and st["readmitted"] == 0
     assert st["interactions"] < work_plain, (st["interactions"], work_plain)
 
 
 @pytest.mark.gpu
-def test_warm_start_readmits_wrongly_excluded_particles(unbinder):
-    """A proposal that misses a tenth of the survivors: the re-admission
-    checks bring them back."""
+def test_first_test_keeps_wrongly_excluded_particles(unbinder):
+    """A proposal that misses a tenth of the survivors: the first test finds
+    every one of them, and the result stays at the plain fixed point."""
     import torch
     inp = synthetic.stripped(n_sub=120, seed=12, nmax=20_000)
     params = _params()
@@ -206,35 +221,31 @@ def test_warm_start_readmits_wrongly_excluded_particles(unbinder):
     warm = db.outputs()
     st = unbinder.stats()
     check_invariants(inp, warm)
-    assert st["readmitted"] > 0.05 * int(plain.nbound.sum())
+    dropped = int((labels.bool() & drop).sum().item())
+    assert st["readmitted"] >= 0.9 * dropped, (st["readmitted"], dropped)
+    _statuses_agree(inp, warm, plain, params)
     m = compare(inp, warm, plain)
-    assert m["mass_rel"] <= 1e-2 and m["membership"] <= 2e-2, m
+    assert m["mass_rel"] <= PATH_NOISE and m["membership"] <= 2 * PATH_NOISE, m
 
 
 @pytest.mark.gpu
-def test_warm_start_restarts_cold_when_the_proposal_disrupts(unbinder):
-    """A proposal of MinNumPartOfSub unbound particles disrupts at once; the
-    cold restart then gives the plain result."""
+def test_empty_proposal_is_the_plain_method(unbinder):
+    """Trusting nothing, the first test is the plain first iteration itself;
+    subhaloes whose first iteration converges restart cold."""
     import torch
-    inp = synthetic.stripped(n_sub=40, seed=13, nmax=5_000)
+    inp = synthetic.batched(total=300_000, seed=16, nmax=50_000)
     params = _params()
     db, plain, _ = _plain_and_trace(unbinder, inp, params)
-    # in every converged subhalo, propose the particles the plain run removed
-    # first (the end of its order); the others start cold
-    prop = torch.zeros(inp.n_particles, dtype=torch.uint8)
-    for s in range(inp.n_sub):
-        off, end = inp.offsets[s], inp.offsets[s + 1]
-        tail = plain.order[off:end][int(plain.nbound[s]):]
-        if plain.status[s] == 0 and len(tail) >= params.min_num_part:
-            prop[off + tail[-params.min_num_part:]] = 1
     db.reset_inout()
-    unbinder.unbind_warm_device(params, db, prop.cuda(), min_particles=0)
+    unbinder.unbind_warm_device(params, db, torch.zeros(inp.n_particles, dtype=torch.uint8, device="cuda"))
     warm = db.outputs()
     st = unbinder.stats()
-    assert st["cold_restarts"] > 0
-    assert np.array_equal(warm.status, plain.status)
+    check_invariants(inp, warm)
+    _statuses_agree(inp, warm, plain, params)
     m = compare(inp, warm, plain)
-    assert m["membership"] <= 1e-4 and m["mass_rel"] <= 1e-5, m
+    assert m["mass_rel"] <= PATH_NOISE and m["membership"] <= 2 * PATH_NOISE, m
+    one = int(np.sum((plain.iterations == 1) & (np.diff(inp.offsets) > 0)))
+    assert st["cold_restarts"] >= (1 if one else 0)
 
 
 @pytest.mark.gpu
@@ -274,13 +285,14 @@ def test_features_are_deterministic_and_finite(unbinder):
 def test_trained_network_gains_over_the_plain_method(unbinder):
     """Train on the GPU from scratch on a small trace set; on held-out
     subhaloes the learned warm start does less tree work than the cold start
-    and stays at its fixed point (bound mass within 1e-3 here; the bench
-    reports the full-size figure)."""
+    and stays at its fixed point (bound mass within 2e-4 on this batch of
+    1500; the benchmark reports the full-size figure)."""
     from hbtg.gpu import DeviceBatch
     params = _params()
     train_set = [(synthetic.stripped(n_sub=3000, seed=21, nmax=100_000), True)]
     model = learned.train(unbinder, train_set, params, steps=1500, batch=32768, min_particles=100)
     assert model.meta["train_error"] < 0.02
+    assert 0.0 < model.threshold < 1.0
     test = synthetic.stripped(n_sub=1500, seed=22, nmax=100_000)
     db = DeviceBatch(test)
     unbinder.count_interactions(True)
@@ -298,6 +310,6 @@ def test_trained_network_gains_over_the_plain_method(unbinder):
         unbinder.count_interactions(False)
     check_invariants(test, warm)
     m = compare(test, warm, plain)
-    assert m["mass_rel"] <= 1e-3, m
+    assert m["mass_rel"] <= 2e-4 and m["membership"] <= 2 * PATH_NOISE, m
     assert st["warm_subhaloes"] > 0
-    assert st["interactions"] < 0.8 * work_plain, (st["interactions"], work_plain)
+    assert st["interactions"] < 0.85 * work_plain, (st["interactions"], work_plain)
