@@ -7,10 +7,16 @@ in a 500-unit periodic box, drawn until the batch holds >= 5e7 particles.
 All subhaloes are unbound in one call.  Inputs are far larger than L2.
 
 Arms
-  (default)          this library.  `value`: device-resident inputs
-                     (hbtg_unbind_batch_device); `e2e`: the host-pointer C-ABI
-                     call (hbtg_unbind_batch) from pinned host buffers, copies
-                     inside the timed region.
+  (default)          this library, learned warm start + batching.  `value`:
+                     device-resident inputs (hbtg_unbind_batch_learned_device
+                     with the shipped proposer); the plain batched GPU path
+                     (hbtg_unbind_batch_device) is timed beside it on the same
+                     batch ("plain", "learned_vs_plain") and judges its bound
+                     mass ("dM_bound") and membership; `e2e`: the host-pointer
+                     C-ABI call (hbtg_unbind_batch_learned) from pinned host
+                     buffers, copies inside the timed region.
+  --workload stripped  the learned warm start's evaluation set: held-out
+                     tidally stripped subhaloes with a previous-output bound set.
   --impl reference   the reference CPU algorithm on the host cores: the
                      reference's own Unbind (oracle/_ref) where it was built,
                      else the project's bit-identical restatement (oracle/),
@@ -35,9 +41,20 @@ UNIT = "bound particles/s"
 FLOPS_PER_INTERACTION = 13  # 3 sub, 5 for r^2, 2 opening test, 1 rsqrt, 2 accumulate
 
 
-def workload(total, seed):
+WORKLOADS = {
+    "batched": "batched method: NFW subhaloes N_p~N^-1.9 on [20,1e6] drawn to >=%.0e particles, "
+               "f_unbound~U(0,0.5) heated to 1.5-4 v_esc, 500-unit periodic box",
+    "stripped": "learned warm start evaluation: %d held-out tidally stripped NFW subhaloes (N_p~N^-1.9 on "
+                "[20,1e6]) with a previous-output bound set, 500-unit periodic box",
+}
+
+
+def workload(total, seed, kind="batched"):
     from hbtg import abi, synthetic
-    inp = synthetic.batched(total=total, seed=seed)
+    if kind == "stripped":
+        inp = synthetic.stripped(n_sub=int(total), seed=424242 + seed)  # seeds disjoint from the training traces
+    else:
+        inp = synthetic.batched(total=total, seed=seed)
     prm = abi.parity_params(dm_only=1, box_size=500.0)
     return inp, prm
 
@@ -133,7 +150,7 @@ def bench_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    inp, prm = workload(args.total, args.seed)
+    inp, prm = workload(args.total, args.seed, args.workload)
     threads = os.cpu_count() or 1
     sample, stride = cpu_sample(inp, args.ref_sample)
     for _ in range(args.warmup):
@@ -148,7 +165,7 @@ def bench_reference(args):
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(times)), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
-        "config": {"workload": "batched NFW subhaloes, N_p~N^-1.9 on [20,1e6], 500-unit box",
+        "config": {"workload": WORKLOADS[args.workload] % args.total,
                    "particles": inp.n_particles, "subhaloes": inp.n_sub},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
                          "sample": "every %d-th subhalo of the size-sorted batch: %d subhaloes, %d particles" %
@@ -160,8 +177,12 @@ def bench_reference(args):
 
 
 def bench_gpu(args):
+    import ctypes
+
     import torch
 
+    from hbtg import learned
+    from hbtg.abi import CallBuffers, CPrior, Inputs, _ptr
     from hbtg.build import build_library
     from hbtg.gpu import DeviceBatch, Unbinder, measure_fp32_peak
 
@@ -171,22 +192,21 @@ def bench_gpu(args):
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local)
     build_library()
-    inp, prm = workload(args.total, args.seed + rank)  # weak scaling: one full batch per GPU
+    inp, prm = workload(args.total, args.seed + rank, args.workload)  # weak scaling: one full batch per GPU
+    use_prior = inp.prior_nbound is not None
+    model = learned.Model.load()
     u = Unbinder(local)
+    u.set_model(model.weights, model.threshold, model.min_particles)
     db = DeviceBatch(inp, device="cuda:%d" % local)
     stream = torch.cuda.current_stream()
 
-    def step():
+    def plain_step():
         db.reset_inout()
         u.unbind_device(prm, db.c, stream.cuda_stream)
 
-    for _ in range(max(3, args.warmup)):
-        step()
-    # interactions of one step (counted in an untimed pass)
-    u.count_interactions(True)
-    step()
-    counted = u.stats()
-    u.count_interactions(False)
+    def learned_step():
+        db.reset_inout()
+        u.unbind_learned_device(prm, db, stream.cuda_stream, use_prior=use_prior)
 
     def barrier():
         if world > 1:
@@ -194,37 +214,47 @@ def bench_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    ms_walk, walk_launches, launches, bound = 0.0, 0, 0, 0
-    with Clocks(local) as clk:
-        barrier()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(args.steps):
+    def timed(step):
+        """W warm-up steps, one untimed counted pass, K timed steps (CUDA events)."""
+        for _ in range(max(3, args.warmup)):
             step()
-            s = u.stats()
-            ms_walk += s["ms_walk"]
-            walk_launches += s["walk_launches"]
-            launches += s["kernel_launches"]
-            bound += s["total_bound"]
-        ev1.record(stream)
-        barrier()
-    ms = ev0.elapsed_time(ev1)
-    clocks = clk.summary()
-    t_max = ms
-    bound_all = bound
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-        b = torch.tensor([bound], device="cuda", dtype=torch.float64)
-        dist.all_reduce(b)
-        bound_all = float(b.item())
-    value = bound_all / (t_max * 1e-3)
+        u.count_interactions(True)
+        step()
+        counted = u.stats()
+        u.count_interactions(False)
+        acc = dict(ms_walk=0.0, walk_launches=0, kernel_launches=0, total_bound=0)
+        st = None
+        with Clocks(local) as clk:
+            barrier()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            for _ in range(args.steps):
+                step()
+                st = u.stats()
+                for k in acc:
+                    acc[k] += st[k]
+            ev1.record(stream)
+            barrier()
+        ms = ev0.elapsed_time(ev1)
+        t_max, bound_all = ms, acc["total_bound"]
+        if world > 1:
+            t_max = _max_over_ranks(ms)
+            bound_all = _sum_over_ranks(bound_all)
+        return dict(ms=ms, t_max=t_max, bound_all=bound_all, value=bound_all / (t_max * 1e-3), counted=counted,
+                    clocks=clk.summary(), last=st, **acc)
 
-    # end to end: host buffers (pinned), copies inside the timed region
-    from hbtg.abi import CallBuffers
+    plain = timed(plain_step)
+    plain_out = db.outputs()
+    warm = timed(learned_step)
+    warm_out = db.outputs()
+    m_plain = float(np.sum(plain_out.mbound.astype(np.float64)))
+    m_warm = float(np.sum(warm_out.mbound.astype(np.float64)))
+    dm = abs(m_warm - m_plain) / max(m_plain, 1e-30)
+    memb = _membership(inp, warm_out, plain_out)
+
+    # end to end through the learned host-pointer C-ABI call: pinned host
+    # buffers, host<->device copies inside the timed region
     pinned = {}
 
     def pin(a):
@@ -236,36 +266,42 @@ def bench_gpu(args):
         pinned[id(arr)] = t
         return arr
 
-    from hbtg.abi import Inputs
     hin = Inputs(inp.offsets, pin(inp.pos), pin(inp.vel), pin(inp.mass), pin(inp.id), None, None,
                  pin(inp.ref_pos), pin(inp.ref_vel), pin(inp.mostbound_pos), pin(inp.mostbound_vel),
-                 pin(inp.most_bound_id))
+                 pin(inp.most_bound_id), {}, pin(inp.prior_nbound), pin(inp.prior_energy))
     buf = CallBuffers(hin, want_energy=True)
     for name in ("order", "energy", "nbound", "mbound", "tracer_index", "iterations", "status", "kinematics", "core",
                  "nbound_type", "mbound_type"):
         setattr(buf.out, name, pin(getattr(buf.out, name)))
     buf = _rebind(buf)
-    u.unbind_raw(prm, buf.c)  # warm the host path once
+    prior = CPrior(_ptr(hin.prior_nbound), _ptr(hin.prior_energy))
+
+    def e2e_call():
+        rc = u.lib.hbtg_unbind_batch_learned(u.h, ctypes.byref(prm), ctypes.byref(buf.c), ctypes.byref(prior))
+        assert rc in (0, 4), rc
+
+    e2e_call()  # warm the host path once
     e2e_times, h2d, d2h = [], 0, 0
     for _ in range(args.steps):
         _reset_frames(buf, hin)
         barrier()
         t0 = time.perf_counter()
-        u.unbind_raw(prm, buf.c)
+        e2e_call()
         e2e_times.append(time.perf_counter() - t0)
-        s = u.stats()
-        h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
+        st = u.stats()
+        h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
     t_e2e = float(np.mean(e2e_times))
     if world > 1:
         t_e2e = _max_over_ranks(t_e2e)
-    e2e_value = (bound_all / args.steps) / t_e2e
+    e2e_value = (warm["bound_all"] / args.steps) / t_e2e
 
-    # roofline of the dominant kernel (the tree walk)
+    # roofline of the dominant kernel (the tree walk) in the learned arm
     peak = measure_fp32_peak(local)
-    walk_ms_per_launch = ms_walk / max(1, walk_launches)
-    flops_per_launch = counted["interactions"] * FLOPS_PER_INTERACTION / max(1, counted["walk_launches"])
+    walk_ms_per_launch = warm["ms_walk"] / max(1, warm["walk_launches"])
+    cw = warm["counted"]
+    flops_per_launch = cw["interactions"] * FLOPS_PER_INTERACTION / max(1, cw["walk_launches"])
     achieved = flops_per_launch / (walk_ms_per_launch * 1e-3) / 1e12
-    traffic = _walk_traffic(counted)
+    traffic = _walk_traffic(cw)
 
     cpu = None
     if rank == 0 and not args.skip_cpu:
@@ -277,28 +313,44 @@ def bench_gpu(args):
                          (stride, sample.n_sub, sample.n_particles, dt)}
 
     if rank == 0:
+        last = warm["last"]
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": max(3, args.warmup), "ms_per_step": t_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (walk) / f64 (reductions)",
+            "metric": METRIC, "value": warm["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": warm["t_max"] / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (walk) / f64 (reductions) / bf16 (proposer)",
             "data": "synthetic (seeded NFW subhaloes)",
-            "config": {"workload": "batched plain method: NFW subhaloes N_p~N^-1.9 on [20,1e6] drawn to >=%.0e "
-                                   "particles, 500-unit periodic box" % args.total,
+            "config": {"workload": WORKLOADS[args.workload] % args.total,
                        "particles_per_gpu": inp.n_particles, "subhaloes_per_gpu": inp.n_sub,
-                       "bound_per_gpu_step": bound / args.steps, "open_angle": 0.45, "softening": 0.005,
-                       "bound_mass_precision": 0.995, "max_sample_size": 0,
+                       "bound_per_gpu_step": warm["total_bound"] / args.steps, "open_angle": 0.45,
+                       "softening": 0.005, "bound_mass_precision": 0.995, "max_sample_size": 0,
                        "l2": "inputs larger than L2 (%.1f GB of particle data)" % (inp.n_particles * 44 / 1e9),
-                       "global_iterations": counted["global_iterations"],
-                       "interactions_per_step": counted["interactions"], "parallelism": "dp%d" % world},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches // args.steps,
+                       "proposer": {"threshold": model.threshold, "min_particles": model.min_particles,
+                                    "trained_on": {k: model.meta.get(k) for k in ("n_sub_stripped", "n_batched",
+                                                                                  "rows", "steps")}},
+                       "global_iterations": {"learned": cw["global_iterations"],
+                                             "plain": plain["counted"]["global_iterations"]},
+                       "interactions_per_step": {"learned": cw["interactions"],
+                                                 "plain": plain["counted"]["interactions"]},
+                       "parallelism": "dp%d" % world},
+            "plain": {"value": plain["value"], "ms_per_step": plain["t_max"] / args.steps,
+                      "bound_per_step": plain["total_bound"] / args.steps,
+                      "ms_walk_per_step": plain["ms_walk"] / args.steps},
+            "learned_vs_plain": warm["value"] / plain["value"],
+            "dM_bound": dm, "membership_vs_plain": memb,
+            "warm_start": {k: last[k] for k in ("warm_subhaloes", "excluded", "readmitted", "cold_restarts",
+                                                "ms_propose", "ms_walk", "ms_tree", "ms_part", "ms_frame",
+                                                "ms_plan", "ms_final")},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "call": "hbtg_unbind_batch_learned (host pointers, pinned)"},
+            "gpu_launches": warm["kernel_launches"] // args.steps,
             "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "FP32 FMA throughput measured in-process (hbtg_measure_fp32_peak)",
                          "flops_per_launch": flops_per_launch, "ms_per_launch": walk_ms_per_launch,
-                         "walk_share_of_step": ms_walk / max(ms, 1e-9)},
+                         "walk_share_of_step": warm["ms_walk"] / max(warm["ms"], 1e-9)},
             "cpu_baseline": cpu,
-            "clocks": clocks,
+            "clocks": warm["clocks"],
+            "clocks_plain": plain["clocks"],
         }
         print(json.dumps(line))
     if world > 1:
@@ -306,6 +358,20 @@ def bench_gpu(args):
         dist.destroy_process_group()
     u.close()
     return 0
+
+
+def _membership(inp, got, ref):
+    """Bound-membership mismatch sum_s |B xor B'| / sum_s |B'| (vectorised)."""
+    seg = np.repeat(np.arange(inp.n_sub), np.diff(inp.offsets))
+    local = np.arange(inp.n_particles) - inp.offsets[seg]
+
+    def bound_mask(out):
+        pos = np.empty(inp.n_particles, np.int64)
+        pos[inp.offsets[seg] + out.order] = local  # position of each input particle
+        return pos < out.nbound[seg]
+
+    a, b = bound_mask(got), bound_mask(ref)
+    return float(np.sum(a ^ b) / max(1, np.sum(b)))
 
 
 def _rebind(buf):
@@ -325,6 +391,14 @@ def _reset_frames(buf, hin):
     buf.out.mostbound_pos[...] = hin.mostbound_pos
     buf.out.mostbound_vel[...] = hin.mostbound_vel
     buf.out.most_bound_id[...] = hin.most_bound_id
+
+
+def _sum_over_ranks(x):
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t)
+    return float(t.item())
 
 
 def _max_over_ranks(x):
@@ -353,12 +427,16 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--total", type=float, default=5e7, help="particles per batch")
+    ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS))
+    ap.add_argument("--total", type=float, default=None,
+                    help="particles per batch (batched; default 5e7) or subhaloes (stripped; default 20000)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--cpu-sample", type=float, default=1e6, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=float, default=4e5, help="particles per reference-arm step")
     ap.add_argument("--skip-cpu", action="store_true")
     args = ap.parse_args()
+    if args.total is None:
+        args.total = 20000 if args.workload == "stripped" else 5e7
     args.total = int(args.total)
     args.cpu_sample = int(args.cpu_sample)
     args.ref_sample = int(args.ref_sample)
