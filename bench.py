@@ -196,7 +196,7 @@ def bench_gpu(args):
     use_prior = inp.prior_nbound is not None
     model = learned.Model.load()
     u = Unbinder(local)
-    u.set_model(model.weights, model.threshold, model.min_particles)
+    model.install(u)
     db = DeviceBatch(inp, device="cuda:%d" % local)
     stream = torch.cuda.current_stream()
 
@@ -324,7 +324,8 @@ def bench_gpu(args):
                        "bound_per_gpu_step": warm["total_bound"] / args.steps, "open_angle": 0.45,
                        "softening": 0.005, "bound_mass_precision": 0.995, "max_sample_size": 0,
                        "l2": "inputs larger than L2 (%.1f GB of particle data)" % (inp.n_particles * 44 / 1e9),
-                       "proposer": {"threshold": model.threshold, "min_particles": model.min_particles,
+                       "proposer": {"threshold": model.threshold, "exclude_below": model.exclude_below,
+                                    "min_particles": model.min_particles,
                                     "trained_on": {k: model.meta.get(k) for k in ("n_sub_stripped", "n_batched",
                                                                                   "rows", "steps")}},
                        "global_iterations": {"learned": cw["global_iterations"],

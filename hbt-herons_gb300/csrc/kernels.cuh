@@ -109,6 +109,7 @@ struct DevState
   int *iter_extra = nullptr; // iterations spent before a cold restart
   int *flag_s = nullptr;     // per-subhalo scratch flag of the warm-start stages
   int *self_cnt = nullptr;   // leading targets of a correction-type walk that are also sources
+  int *ntest = nullptr;      // particles the first test evaluates
   float *ref0 = nullptr;     // [6S] input frame, restored for a cold restart
 };
 

@@ -121,6 +121,7 @@ struct hbtg_handle
   // learned warm start (hbtg_set_model)
   bool has_model = false;
   float threshold = 0.5f;
+  float exclude_below = 0.f;
   long long min_particles = 0;
   // state of the last unbinding call, for hbtg_trace_labels_device
   int last_S = 0;
@@ -373,12 +374,13 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
     R.run();
   else
   {
-    int *wi = P.get<int>(S_WARMI, (size_t)(S + 1) * 5);
+    int *wi = P.get<int>(S_WARMI, (size_t)(S + 1) * 6);
     D.warm = wi;
     D.nexcl = wi + (S + 1);
     D.iter_extra = wi + 2 * (size_t)(S + 1);
     D.flag_s = wi + 3 * (size_t)(S + 1);
     D.self_cnt = wi + 4 * (size_t)(S + 1);
+    D.ntest = wi + 5 * (size_t)(S + 1);
     HBTG_CUDA(cudaMemsetAsync(D.self_cnt, 0, sizeof(int) * (S + 1), st));
     D.ref0 = P.get<float>(S_REF0, (size_t)S * 6);
     WarmBufs W;
@@ -413,7 +415,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
         const int mrc = hbtg_mlp_forward(P.get<float>(S_MODEL, HBTG_MLP_PARAMS), W.feat, prob, N, st);
         if (mrc != HBTG_OK)
           return mrc;
-        k_propose<<<blocks_for(N, 256), 256, 0, st>>>(prob, H->threshold, prop, N);
+        k_propose<<<blocks_for(N, 256), 256, 0, st>>>(prob, H->threshold, H->exclude_below, prop, N);
         R.launches += 2;
         R.check();
       }
@@ -667,6 +669,7 @@ int model_call(void *arg)
   HBTG_CUDA(cudaMemcpy(d, c.m->weights, sizeof(float) * HBTG_MLP_PARAMS, cudaMemcpyHostToDevice));
   c.H->has_model = true;
   c.H->threshold = c.m->threshold;
+  c.H->exclude_below = c.m->exclude_below;
   c.H->min_particles = c.m->min_particles;
   return HBTG_OK;
 }
@@ -778,7 +781,8 @@ int hbtg_unbind_batch_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b
 
 int hbtg_set_model(hbtg_handle *h, const hbtg_model *m)
 {
-  if (!h || !m || !m->weights || !(m->threshold == m->threshold) || m->min_particles < 0)
+  if (!h || !m || !m->weights || !(m->threshold == m->threshold) || !(m->exclude_below <= m->threshold) ||
+      m->min_particles < 0)
     return HBTG_ERR_INVALID;
   ModelCall c{h, m};
   return guarded(model_call, &c);

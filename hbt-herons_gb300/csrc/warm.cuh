@@ -7,12 +7,14 @@
 // most expensive step of the method.  A proposal predicts that iteration's
 // survivors (E < 0 in the potential of every particle, in the input frame):
 //
-//   proposal     the particles the proposer trusts start in the set; each warm
-//                subhalo's particles are partitioned trusted-first
-//   first test   every other particle gets the plain method's own first test:
-//                its energy against the tree of every particle, in the input
-//                frame; those with E < 0 join the set.  So nothing the first
-//                iteration would have kept is left out, whatever the proposal
+//   proposal     per particle: trusted (1: starts in the set), to test (0), or
+//                left out (2: the proposer is sure the first iteration removes
+//                it); each warm subhalo's particles are partitioned in that
+//                order: trusted, tested, left out
+//   first test   every particle to test gets the plain method's own first
+//                test: its energy against the tree of every particle, in the
+//                input frame; those with E < 0 join the set.  The targets walk
+//                in the tree's key order, so a warp's 32 are neighbours
 //   iteration    from that set, in its centre-of-mass frame (the frame the
 //                plain method's second iteration uses), the unchanged exact
 //                loop (driver.cuh) runs to its convergence test, so the path
@@ -23,7 +25,7 @@
 //                start has nothing to save there
 // Where the warm path can leave the plain one: a trusted particle that the
 // first iteration would have removed (the exact loop still removes it, later),
-// and the second iteration, which the plain method usually computes as a
+// a left-out particle that it would have kept, and the second iteration, which the plain method usually computes as a
 // correction (energies of the first minus the removed particles' potential,
 // src/subhalo_unbind.cpp:563-621) and the warm path from a new tree of the
 // same set: the two differ by the tree's approximation error, which moves
@@ -70,7 +72,7 @@ struct WarmBufs
   unsigned long long *hist; // [64 S] fixed-point mass per radial bin
   float *tab;               // [kTab S]
   float *feat;              // [6 N]
-  const uint8_t *prop;      // [N] proposal (1 = start in the set)
+  const uint8_t *prop;      // [N] proposal: 1 trusted, 0 to test, 2 left out
   long long min_n;          // subhaloes with fewer particles start cold
 };
 
@@ -321,10 +323,16 @@ __global__ void k_features(DevState D, KParams K, WarmBufs W)
   }
 }
 
-__global__ void k_propose(const float *__restrict__ prob, float threshold, uint8_t *__restrict__ prop, long long n)
+// Proposal from the network's probabilities: trusted at or above `trust`,
+// left out below `leave_out`, tested in between.
+__global__ void k_propose(const float *__restrict__ prob, float trust, float leave_out, uint8_t *__restrict__ prop,
+                          long long n)
 {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    prop[i] = prob[i] >= threshold ? 1 : 0;
+  {
+    const float p = prob[i];
+    prop[i] = p >= trust ? 1 : (p < leave_out ? 2 : 0);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -335,6 +343,7 @@ __device__ __forceinline__ bool warm_eligible(const DevState &D, const WarmBufs 
   return D.state[s] == kActive && (long long)D.n_s[s] >= W.min_n;
 }
 
+// flags: trusted; cnt: to test (eligible subhaloes only; scanned into F and X)
 __global__ void k_warm_flags(DevState D, WarmBufs W)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -343,10 +352,13 @@ __global__ void k_warm_flags(DevState D, WarmBufs W)
   if (i == D.N)
   {
     D.flags[i] = 0;
+    D.cnt[i] = 0;
     return;
   }
-  const int s = D.seg_of[i];
-  D.flags[i] = (warm_eligible(D, W, s) && W.prop[i]) ? 1 : 0;
+  const bool ok = warm_eligible(D, W, D.seg_of[i]);
+  const uint8_t q = W.prop[i];
+  D.flags[i] = (ok && q == 1) ? 1 : 0;
+  D.cnt[i] = (ok && q == 0) ? 1 : 0;
 }
 
 // Which subhaloes start warm (the proposal leaves more than 1 -
@@ -366,10 +378,12 @@ __global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
   D.iter_extra[s] = 0;
   const int n = D.n_s[s];
   const int npred = D.F[D.off[s + 1]] - D.F[D.off[s]];
+  const int ntest = D.X[D.off[s + 1]] - D.X[D.off[s]];
   const bool warm = warm_eligible(D, W, s) && (float)npred < __fmul_rn((float)n, K.bmp);
   D.warm[s] = warm ? 1 : 0;
   D.flag_s[s] = warm ? 1 : 0;
   D.nexcl[s] = warm ? n - npred : 0;
+  D.ntest[s] = warm ? ntest : 0;
   if (!warm)
     return;
   D.nbound[s] = npred;
@@ -393,8 +407,9 @@ __global__ void k_warm_scatter(DevState D)
   if (D.warm[s] != 1)
     return;
   const long long off = D.off[s];
-  const int rank = D.F[i] - D.F[off];
-  const int pos = D.flags[i] ? rank : D.nbound[s] + (int)(i - off) - rank;
+  const int rt = D.F[i] - D.F[off], ru = D.X[i] - D.X[off];
+  const int nt = D.nbound[s], nu = D.ntest[s];
+  const int pos = D.flags[i] ? rt : (D.cnt[i] ? nt + ru : nt + nu + (int)(i - off) - rt - ru);
   D.ord[off + pos] = (int)i;
   D.bnd[i] = (uint8_t)D.flags[i];
 }
@@ -413,9 +428,9 @@ __global__ void k_frame_flagged(DevState D, KParams K, int clear)
 }
 
 // Plan of the first test: for each warm subhalo, every particle is a tree
-// source (positions [0, n)) and the untrusted ones (positions [nbound, n))
-// are the targets, each keeping its self term.  The walk treats it as a
-// correction walk: targets from the tgt list.
+// source (positions [0, n)) and the particles to test (positions [nbound,
+// nbound + ntest)) are the targets, each keeping its self term.  The walk
+// treats it as a correction walk: targets from the tgt list.
 __global__ void k_plan_first(DevState D)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -431,11 +446,11 @@ __global__ void k_plan_first(DevState D)
     D.src_cnt[s] = D.chunk_cnt[s] = D.part_cnt[s] = D.tail_cnt[s] = 0;
     return;
   }
-  const int ne = D.n_s[s] - D.nbound[s];
+  const int ne = D.ntest[s];
   D.corr[s] = 1;
   D.ngrav[s] = 0;
   D.src_begin[s] = 0;
-  D.src_cnt[s] = D.n_s[s];
+  D.src_cnt[s] = ne > 0 ? D.n_s[s] : 0; // no tree where nothing is tested
   D.self_cnt[s] = ne;
   D.tgt_cnt[s] = ne;
   D.chunk_cnt[s] = (ne + kWarp - 1) / kWarp;
@@ -445,18 +460,27 @@ __global__ void k_plan_first(DevState D)
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
 }
 
-__global__ void k_readmit_targets(DevState D, int total)
+// Targets of the first test in the tree's key order: the sources (packed by
+// src_off, key-sorted in val) that are to be tested (flag, scan, scatter).
+__global__ void k_first_tgt_flags(DevState D, WarmBufs W, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= total)
+  if (j > total)
     return;
-  const int s = find_segment<int>(D.part_off, D.S, j);
-  const long long off = D.off[s];
-  D.tgt[off + (j - D.part_off[s])] = D.ord[off + D.nbound[s] + (j - D.part_off[s])];
+  D.flags[j] = (j < total && W.prop[D.val[j]] == 0) ? 1 : 0;
+}
+
+__global__ void k_first_tgt_scatter(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total || !D.flags[j])
+    return;
+  const int s = find_segment<int>(D.src_off, D.S, j);
+  D.tgt[D.off[s] + (D.F[j] - D.F[D.src_off[s]])] = (int)D.val[j];
 }
 
 // First-iteration energy of each target (the potential of every particle,
-// the input frame; src/subhalo_unbind.cpp:563-580); flags the bound ones.
+// the input frame; src/subhalo_unbind.cpp:563-580).
 __global__ void k_readmit_energy(DevState D, KParams K, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -479,8 +503,8 @@ __global__ void k_readmit_energy(DevState D, KParams K, int total)
   D.flags[j] = e < 0.f ? 1 : 0;
 }
 
-// New order of positions [nbound, n): the particles the test keeps, then the
-// others, each group in its previous order.
+// New order of positions [nbound, nbound + ntest): the particles the test
+// keeps, then the others, each group in its previous order.
 __global__ void k_readmit_scatter(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,14 +531,23 @@ __global__ void k_readmit_copy(DevState D, int total)
   D.ord[g] = D.ord_tmp[g];
 }
 
-__global__ void k_readmit_bnd(DevState D, int total)
+// Outcome of the first test by position ([nbound, nbound + ntest), packed
+// like the targets): flags the kept particles and marks them bound.
+__global__ void k_first_flags(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < total && D.flags[j])
+  if (j > total)
+    return;
+  if (j == total)
   {
-    const int s = find_segment<int>(D.part_off, D.S, j);
-    D.bnd[D.tgt[D.off[s] + (j - D.part_off[s])]] = 1;
+    D.flags[j] = 0;
+    return;
   }
+  const int s = find_segment<int>(D.tail_off, D.S, j);
+  const int p = D.ord[D.off[s] + D.nbound[s] + (j - D.tail_off[s])];
+  const bool kept = D.Ep[p] < 0.f;
+  D.flags[j] = kept ? 1 : 0;
+  D.bnd[p] = kept ? 1 : 0;
 }
 
 // After the first test: the set is the trusted particles plus the r the test
@@ -663,10 +696,10 @@ void flagged_frames(IterationDriver<Mem> &R)
   R.check();
 }
 
-// The plain method's first test for the untrusted particles of the warm
+// The plain method's first test for the particles to test of the warm
 // subhaloes (see k_plan_first); returns how many it keeps.
 template <class Mem>
-long long first_test(IterationDriver<Mem> &R)
+long long first_test(IterationDriver<Mem> &R, const WarmBufs &W)
 {
   DevState &D = R.D;
   cudaStream_t st = R.st;
@@ -680,31 +713,33 @@ long long first_test(IterationDriver<Mem> &R)
   const int tail_total = R.scan_counts(D.tail_cnt, D.tail_off, S);
   R.mem.mark(6);
   if (src_total > 0)
-    R.build_tree(src_total);
-  if (part_total > 0)
   {
-    k_readmit_targets<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
+    R.build_tree(src_total);
+    k_first_tgt_flags<<<grid_for(src_total + 1, 256), 256, 0, st>>>(D, W, src_total);
     R.launches++;
+    scan<int, false>(D.flags, D.F, src_total + 1, R.mem.scan_scratch(src_total + 1), st, &R.launches);
+    k_first_tgt_scatter<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    R.launches++;
+    R.check();
   }
   R.mem.mark(2);
   R.walk(chunk_total);
   R.mem.mark(1);
-  k_readmit_energy<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, R.K, part_total);
-  R.launches++;
-  scan<int, false>(D.flags, D.F, part_total + 1, R.mem.scan_scratch(part_total + 1), st, &R.launches);
-  R.check();
-  const long long kept = R.read_int(D.F + part_total);
-  if (tail_total > 0)
+  long long kept = 0;
+  if (part_total > 0)
   {
+    k_readmit_energy<<<grid_for(part_total + 1, 256), 256, 0, st>>>(D, R.K, part_total);
+    k_first_flags<<<grid_for(tail_total + 1, 256), 256, 0, st>>>(D, tail_total);
+    R.launches += 2;
+    scan<int, false>(D.flags, D.F, tail_total + 1, R.mem.scan_scratch(tail_total + 1), st, &R.launches);
+    R.check();
+    kept = R.read_int(D.F + tail_total);
     k_readmit_scatter<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
     k_readmit_copy<<<grid_for(tail_total, 256), 256, 0, st>>>(D, tail_total);
     R.launches += 2;
   }
-  if (part_total > 0)
-  {
-    k_readmit_bnd<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
-    R.launches++;
-  }
+  else
+    R.mem.check(cudaMemsetAsync(D.F, 0, sizeof(int), st)); // k_first_apply reads F[part_off[s]]
   k_first_apply<<<grid_for(S, 256), 256, 0, st>>>(D, R.K);
   R.launches++;
   R.check();
@@ -727,10 +762,14 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     k_warm_flags<<<grid_for(D.N + 1, 256), 256, 0, st>>>(D, W);
     R.launches++;
     scan<int, false>(D.flags, D.F, D.N + 1, R.mem.scan_scratch(D.N + 1), st, &R.launches);
+    scan<int, false>(D.cnt, D.X, D.N + 1, R.mem.scan_scratch(D.N + 1), st, &R.launches);
     R.check();
   }
   else
+  {
     R.mem.check(cudaMemsetAsync(D.F, 0, sizeof(int), st));
+    R.mem.check(cudaMemsetAsync(D.X, 0, sizeof(int), st));
+  }
   k_warm_setup<<<sb, 256, 0, st>>>(D, R.K, W);
   R.launches++;
   if (D.N > 0)
@@ -739,7 +778,7 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     R.launches++;
   }
   R.check();
-  C.readmitted += first_test(R);
+  C.readmitted += first_test(R, W);
   C.readmit_rounds++;
   {
     std::vector<int> nex(S);

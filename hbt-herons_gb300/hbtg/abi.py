@@ -138,7 +138,8 @@ class CPrior(C.Structure):
 
 class CModel(C.Structure):
     """hbtg_model."""
-    _fields_ = [("weights", _P), ("threshold", C.c_float), ("min_particles", C.c_int64)]
+    _fields_ = [("weights", _P), ("threshold", C.c_float), ("min_particles", C.c_int64),
+                ("exclude_below", C.c_float)]
 
 
 MLP_PARAMS = 4673

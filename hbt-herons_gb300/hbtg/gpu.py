@@ -124,12 +124,12 @@ class Unbinder:
         return s.as_dict()
 
     # -- warm start ---------------------------------------------------------
-    def set_model(self, weights, threshold, min_particles=0):
+    def set_model(self, weights, threshold, min_particles=0, exclude_below=0.0):
         """Loads the proposer network (hbtg_set_model)."""
         w = np.ascontiguousarray(weights, dtype=np.float32)
         if w.shape != (MLP_PARAMS,):
             raise ValueError("expected %d weights" % MLP_PARAMS)
-        m = CModel(w.ctypes.data, float(threshold), int(min_particles))
+        m = CModel(w.ctypes.data, float(threshold), int(min_particles), float(exclude_below))
         rc = self.lib.hbtg_set_model(self.h, C.byref(m))
         if rc != 0:
             raise UnbindError(rc, "hbtg_set_model")
@@ -156,7 +156,8 @@ class Unbinder:
         return rc
 
     def unbind_warm_device(self, params: Params, db, proposal, min_particles=0, stream_ptr=0):
-        """Warm start from an explicit proposal (torch uint8 tensor [N] on the device)."""
+        """Warm start from an explicit proposal (torch uint8 tensor [N] on the
+        device: 1 trusted, 0 to test, 2 left out without the test)."""
         ptr = proposal.data_ptr() if proposal is not None and proposal.numel() else None
         rc = self.lib.hbtg_unbind_batch_warm_device(self.h, C.byref(params), C.byref(db.c), ptr,
                                                     int(min_particles), C.c_void_p(stream_ptr))

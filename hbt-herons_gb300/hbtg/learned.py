@@ -12,8 +12,9 @@ tree of every particle); the library gives every other particle the
 iteration's own test, so nothing it would have kept is lost, and then takes
 the plain method's own path from its second iteration.
 
-Model files (.npz): weights (float32 [4673]), threshold, min_particles and a
-JSON description of the training run.
+Model files (.npz): weights (float32 [4673]), threshold (trusted at or
+above), exclude_below (left out untested below), min_particles and a JSON
+description of the training run.
 """
 from __future__ import annotations
 
@@ -34,19 +35,25 @@ LAYERS = [("W1", NUM_FEATURES * 64), ("b1", 64), ("W2", 64 * 64), ("b2", 64), ("
 @dataclass
 class Model:
     weights: np.ndarray
-    threshold: float = 0.5
-    min_particles: int = 100
+    threshold: float = 0.5      # trusted at or above
+    min_particles: int = 100    # smaller subhaloes start cold
     meta: dict = field(default_factory=dict)
+    exclude_below: float = 0.0  # left out without the first test below
 
     def save(self, path):
         np.savez(path, weights=np.asarray(self.weights, np.float32), threshold=np.float32(self.threshold),
-                 min_particles=np.int64(self.min_particles), meta=np.array(json.dumps(self.meta)))
+                 min_particles=np.int64(self.min_particles), exclude_below=np.float32(self.exclude_below),
+                 meta=np.array(json.dumps(self.meta)))
 
     @staticmethod
     def load(path=MODEL_FILE):
         z = np.load(path)
+        lo = float(z["exclude_below"]) if "exclude_below" in z else 0.0
         return Model(z["weights"].astype(np.float32), float(z["threshold"]), int(z["min_particles"]),
-                     json.loads(str(z["meta"])))
+                     json.loads(str(z["meta"])), lo)
+
+    def install(self, unbinder):
+        unbinder.set_model(self.weights, self.threshold, self.min_particles, self.exclude_below)
 
 
 def initial_weights(seed=0):
@@ -167,6 +174,21 @@ def choose_threshold(prob, labels, fp_weight=50.0):
     return best_t, best_err
 
 
+def choose_exclusion(prob, labels, max_missed=1e-6):
+    """The largest probability below which leaving particles out untested
+    loses at most max_missed of the survivors."""
+    pos = labels > 0.5
+    npos = max(int(pos.sum().item()), 1)
+    best = 0.0
+    for t in np.concatenate([[1e-7, 3e-7], np.logspace(-6, np.log10(0.5), 40)]):
+        missed = int(((prob < float(t)) & pos).sum().item())
+        if missed <= max_missed * npos:
+            best = float(t)
+        else:
+            break
+    return best
+
+
 def training_batches(n_sub_stripped=100_000, n_batched=2_000_000, seed=1000, nmax=1_000_000):
     """The inputs of the training traces: tidally stripped subhaloes with a
     previous bound set, and (without a prior) subhaloes of the batched workload."""
@@ -192,9 +214,14 @@ def train(unbinder, batches, params, steps=3000, batch=65536, seed=0, min_partic
     history = tr.fit(feats, labels, steps=steps, batch=batch, seed=seed, log_every=log_every)
     prob = mlp_forward(tr.w, feats)
     thr, err = choose_threshold(prob, labels)
+    lo = min(choose_exclusion(prob, labels), thr)
+    pos = labels > 0.5
     meta = dict(rows=int(feats.shape[0]), positive=float(labels.mean().item()), steps=steps, batch=batch,
-                train_error=err, history=history)
-    return Model(tr.weights(), thr, min_particles, meta)
+                train_error=err, history=history,
+                left_out=float((prob < lo).float().mean().item()),
+                left_out_survivors=int(((prob < lo) & pos).sum().item()),
+                tested=float(((prob >= lo) & (prob < thr)).float().mean().item()))
+    return Model(tr.weights(), thr, min_particles, meta, lo)
 
 
 def main(argv=None):
@@ -218,7 +245,7 @@ def main(argv=None):
     model.meta.update(dict(n_sub_stripped=n_str, n_batched=n_bat, generate_s=t1 - t0, train_s=t2 - t1,
                            params=dict(softening=float(params.softening), box_size=500.0, G=1.0)))
     model.save(out)
-    print(json.dumps(dict(out=out, threshold=model.threshold,
+    print(json.dumps(dict(out=out, threshold=model.threshold, exclude_below=model.exclude_below,
                           **{k: v for k, v in model.meta.items() if k != "history"})))
     for k, l in model.meta["history"]:
         print("step %5d loss %.5f" % (k, l))

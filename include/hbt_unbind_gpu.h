@@ -221,9 +221,10 @@ int hbtg_measure_fp32_peak(int device, double *tflops);
  * Warm start (no counterpart in the reference, whose Unbind always starts
  * from every particle, src/subhalo_unbind.cpp:505-507, and spends most of its
  * time on that first iteration).  A proposal marks the particles predicted
- * to survive the first iteration.  Those are trusted; every other particle
- * gets the first iteration's own test (its energy against the tree of every
- * particle, in the input frame) and joins the set when bound.  From that set
+ * to survive the first iteration (trusted), those it is sure the iteration
+ * removes (left out), and the rest, which get the first iteration's own test
+ * (their energy against the tree of every particle, in the input frame) and
+ * join the trusted ones when bound.  From that set
  * the exact loop runs to its convergence test, the plain method's own path
  * from its second iteration on.  A subhalo whose first iteration would
  * already converge runs cold.  Outputs have the hbtg_unbind_batch layout;
@@ -243,13 +244,15 @@ typedef struct hbtg_prior
 } hbtg_prior;
 
 /* The learned proposer: a particle is trusted when the network's
- * probability is >= threshold; subhaloes with fewer than min_particles
- * particles start cold. */
+ * probability is >= threshold, left out without the first test when it is
+ * below exclude_below (0 = test every untrusted particle), tested otherwise;
+ * subhaloes with fewer than min_particles particles start cold. */
 typedef struct hbtg_model
 {
   const float *weights; /* [HBTG_MLP_PARAMS] host array */
   float threshold;
   int64_t min_particles;
+  float exclude_below;  /* <= threshold */
 } hbtg_model;
 
 /* Copies the proposer network to the handle's device. */
@@ -266,9 +269,9 @@ int hbtg_unbind_batch_learned(hbtg_handle *handle, const hbtg_params *params, hb
 int hbtg_unbind_batch_learned_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
                                      const hbtg_prior *prior, void *cuda_stream);
 
-/* Warm start from an explicit proposal ([N] device array, 1 = trusted)
- * instead of the network; subhaloes with fewer than min_particles particles
- * start cold. */
+/* Warm start from an explicit proposal ([N] device array: 1 = trusted,
+ * 0 = to test, 2 = left out without the test) instead of the network;
+ * subhaloes with fewer than min_particles particles start cold. */
 int hbtg_unbind_batch_warm_device(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch,
                                   const uint8_t *proposal, int64_t min_particles, void *cuda_stream);
 

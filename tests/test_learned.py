@@ -205,6 +205,26 @@ def test_warm_start_from_first_iteration_trace_keeps_the_plain_fixed_point(unbin
 
 
 @pytest.mark.gpu
+def test_three_state_trace_proposal_skips_the_first_test(unbinder):
+    """Trusting the survivors and leaving the rest out untested: no first test
+    at all, and the plain path from its second iteration."""
+    import torch
+    inp = synthetic.stripped(n_sub=300, seed=17, nmax=30_000)
+    params = _params()
+    db, plain, labels = _plain_and_trace(unbinder, inp, params)
+    prop = torch.where(labels.bool(), torch.ones_like(labels), torch.full_like(labels, 2))
+    db.reset_inout()
+    unbinder.unbind_warm_device(params, db, prop, min_particles=100)
+    warm = db.outputs()
+    st = unbinder.stats()
+    check_invariants(inp, warm)
+    _statuses_agree(inp, warm, plain, params)
+    assert st["warm_subhaloes"] > 0 and st["readmitted"] == 0
+    m = compare(inp, warm, plain)
+    assert m["mass_rel"] <= PATH_NOISE and m["membership"] <= 2 * PATH_NOISE, m
+
+
+@pytest.mark.gpu
 def test_first_test_keeps_wrongly_excluded_particles(unbinder):
     """A proposal that misses a tenth of the survivors: the first test finds
     every one of them, and the result stays at the plain fixed point."""
@@ -301,7 +321,7 @@ def test_trained_network_gains_over_the_plain_method(unbinder):
         unbinder.unbind_device(params, db.c)
         plain = db.outputs()
         work_plain = unbinder.stats()["interactions"]
-        unbinder.set_model(model.weights, model.threshold, model.min_particles)
+        model.install(unbinder)
         db.reset_inout()
         unbinder.unbind_learned_device(params, db)
         warm = db.outputs()
