@@ -244,14 +244,19 @@ def bench_gpu(args):
         return dict(ms=ms, t_max=t_max, bound_all=bound_all, value=bound_all / (t_max * 1e-3), counted=counted,
                     clocks=clk.summary(), last=st, **acc)
 
-    plain = timed(plain_step)
-    plain_out = db.outputs()
-    warm = timed(learned_step)
-    warm_out = db.outputs()
-    m_plain = float(np.sum(plain_out.mbound.astype(np.float64)))
-    m_warm = float(np.sum(warm_out.mbound.astype(np.float64)))
-    dm = abs(m_warm - m_plain) / max(m_plain, 1e-30)
-    memb = _membership(inp, warm_out, plain_out)
+    plain = timed(plain_step) if args.arm in ("both", "plain") else None
+    plain_out = db.outputs() if plain else None
+    if args.arm == "plain":  # profile the plain arm alone: report it as the line's value
+        warm, warm_out = plain, plain_out
+    else:
+        warm = timed(learned_step)
+        warm_out = db.outputs()
+    dm = memb = None
+    if plain and args.arm == "both":
+        m_plain = float(np.sum(plain_out.mbound.astype(np.float64)))
+        m_warm = float(np.sum(warm_out.mbound.astype(np.float64)))
+        dm = abs(m_warm - m_plain) / max(m_plain, 1e-30)
+        memb = _membership(inp, warm_out, plain_out)
 
     # end to end through the learned host-pointer C-ABI call: pinned host
     # buffers, host<->device copies inside the timed region
@@ -329,14 +334,15 @@ def bench_gpu(args):
                                     "trained_on": {k: model.meta.get(k) for k in ("n_sub_stripped", "n_batched",
                                                                                   "rows", "steps")}},
                        "global_iterations": {"learned": cw["global_iterations"],
-                                             "plain": plain["counted"]["global_iterations"]},
+                                             "plain": plain and plain["counted"]["global_iterations"]},
                        "interactions_per_step": {"learned": cw["interactions"],
-                                                 "plain": plain["counted"]["interactions"]},
-                       "parallelism": "dp%d" % world},
-            "plain": {"value": plain["value"], "ms_per_step": plain["t_max"] / args.steps,
-                      "bound_per_step": plain["total_bound"] / args.steps,
-                      "ms_walk_per_step": plain["ms_walk"] / args.steps},
-            "learned_vs_plain": warm["value"] / plain["value"],
+                                                 "plain": plain and plain["counted"]["interactions"]},
+                       "arm": args.arm, "parallelism": "dp%d" % world},
+            "plain": plain and {"value": plain["value"], "ms_per_step": plain["t_max"] / args.steps,
+                                "bound_per_step": plain["total_bound"] / args.steps,
+                                "ms_walk_per_step": plain["ms_walk"] / args.steps,
+                                "gpu_launches": plain["kernel_launches"] // args.steps},
+            "learned_vs_plain": (warm["value"] / plain["value"]) if plain and args.arm == "both" else None,
             "dM_bound": dm, "membership_vs_plain": memb,
             "warm_start": {k: last[k] for k in ("warm_subhaloes", "excluded", "readmitted", "cold_restarts",
                                                 "ms_propose", "ms_walk", "ms_tree", "ms_part", "ms_frame",
@@ -351,7 +357,7 @@ def bench_gpu(args):
                          "walk_share_of_step": warm["ms_walk"] / max(warm["ms"], 1e-9)},
             "cpu_baseline": cpu,
             "clocks": warm["clocks"],
-            "clocks_plain": plain["clocks"],
+            "clocks_plain": plain and plain["clocks"],
         }
         print(json.dumps(line))
     if world > 1:
@@ -429,6 +435,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="batched", choices=sorted(WORKLOADS))
+    ap.add_argument("--arm", default="both", choices=["both", "learned", "plain"],
+                    help="time both GPU arms (default) or one alone (for profiling)")
     ap.add_argument("--total", type=float, default=None,
                     help="particles per batch (batched; default 5e7) or subhaloes (stripped; default 20000)")
     ap.add_argument("--seed", type=int, default=0)
