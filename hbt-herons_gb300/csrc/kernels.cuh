@@ -712,10 +712,10 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
 
 // ---------------------------------------------------------------------------
 // Tree walk: one warp evaluates 32 neighbouring targets (key order) of one
-// subhalo; each lane's interaction list is that of the reference's stackless
-// walk for its target (open: next slot; accept: interact, jump to the skip
-// slot), and the warp visits the union of those lists together (walk_warp).
-// FP32 with Kahan-compensated accumulation.
+// subhalo; each lane walks the slots for its own target exactly as the
+// reference's stackless walk (open: next slot; accept: interact, jump to the
+// skip slot), so its interaction list is the reference's.  FP32 with
+// Kahan-compensated accumulation.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float spline_w(float u)
 {
@@ -725,42 +725,17 @@ __device__ __forceinline__ float spline_w(float u)
                         u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
 }
 
-// Warp-coherent walk: the 32 lanes (neighbouring targets of one subhalo)
-// step through the slots together, one slot per step, reading it from a
-// window of 32 slots that the warp loads with one coalesced load.  A lane that accepts a cell takes its
-// monopole and sits out the cell's subtree (until the skip slot); the warp
-// descends into a cell when any lane opens it and jumps over it otherwise.
-// Each lane therefore sums exactly the interactions of its own stackless
-// walk, in the same (preorder) order.  Every lane of the warp must call this.
 template <bool Wrap>
-__device__ __forceinline__ void walk_warp(const float4 *__restrict__ T, int root, float4 x, bool valid,
+__device__ __forceinline__ void walk_lane(const float4 *__restrict__ T, int root, float4 x, bool valid,
                                           float self_mass, const KParams &K, float &out, unsigned long long &cnt)
 {
   float sum = valid ? self_mass / K.soft : 0.f, comp = 0.f;
-  const int lane = threadIdx.x & 31;
-  const int end = __float_as_int(__ldg(&T[root + 1]).y); // the root's skip: the same for the whole warp
+  const int end = valid ? __float_as_int(__ldg(&T[root + 1]).y) : root;
   const float h2 = K.h * K.h;
-  int resume = valid ? root : 0x7fffffff; // the lane takes part from this slot on
   int idx = root;
-  // window of 32 consecutive slots, slot wbase + l held by lane l: one
-  // coalesced load serves the steps until the walk leaves it
-  int wbase = -64;
-  float4 win = make_float4(0.f, 0.f, 0.f, 0.f);
   while (idx < end)
   {
-    int k = idx - wbase;
-    if (k < 0 || k >= 31) // a cell needs its second slot in the window too
-    {
-      wbase = idx;
-      k = 0;
-      win = (idx + lane < end) ? __ldg(&T[idx + lane]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    float4 a;
-    a.x = __shfl_sync(0xffffffffu, win.x, k);
-    a.y = __shfl_sync(0xffffffffu, win.y, k);
-    a.z = __shfl_sync(0xffffffffu, win.z, k);
-    a.w = __shfl_sync(0xffffffffu, win.w, k);
-    const bool active = idx >= resume;
+    const float4 a = __ldg(&T[idx]);
     float dx = a.x - x.x, dy = a.y - x.y, dz = a.z - x.z;
     if (Wrap)
     {
@@ -769,40 +744,35 @@ __device__ __forceinline__ void walk_warp(const float4 *__restrict__ T, int root
       dz = nearest_f(dz, K.half, K.box);
     }
     const float r2 = dx * dx + dy * dy + dz * dz;
-    float m = a.w;
-    bool take = active;
-    int next = idx + 1;
+    float m;
+    int next;
     if (slot_is_cell(a.w))
     {
-      const bool open = active && r2 < -a.w; // the first child follows the cell's two slots
-      take = active && !open;
-      const bool any_open = __any_sync(0xffffffffu, open);
-      if (any_open && !__any_sync(0xffffffffu, take))
+      if (r2 < -a.w) // open: the first child follows the cell's two slots
       {
         idx += 2;
         continue;
       }
-      const float bm = __shfl_sync(0xffffffffu, win.x, k + 1), bs = __shfl_sync(0xffffffffu, win.y, k + 1);
-      m = bm;
-      const int skip = __float_as_int(bs);
-      if (take)
-        resume = skip;
-      next = any_open ? idx + 2 : skip;
+      const float2 b = __ldg(reinterpret_cast<const float2 *>(&T[idx + 1]));
+      m = b.x;
+      next = __float_as_int(b.y);
     }
-    if (take)
+    else
     {
-      float term;
-      if (r2 >= h2)
-        term = -m * rsqrtf(r2);
-      else
-        term = m * K.h_inv * spline_w(sqrtf(r2) * K.h_inv);
-      const float y = term - comp;
-      const float t = sum + y;
-      comp = (t - sum) - y;
-      sum = t;
-      cnt++;
+      m = a.w;
+      next = idx + 1;
     }
-    idx = next;
+    float term;
+    if (r2 >= h2)
+      term = -m * rsqrtf(r2);
+    else
+      term = m * K.h_inv * spline_w(sqrtf(r2) * K.h_inv);
+    const float y = term - comp;
+    const float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+    cnt++;
+    idx = max(next, idx + 1); // strictly increasing
   }
   out = sum - comp;
 }
@@ -834,9 +804,9 @@ __global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_c
     if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
       ;
     else if (D.wrap[s])
-      walk_warp<true>(D.nodes, root, x, valid, self, K, phi, cnt);
+      walk_lane<true>(D.nodes, root, x, valid, self, K, phi, cnt);
     else
-      walk_warp<false>(D.nodes, root, x, valid, self, K, phi, cnt);
+      walk_lane<false>(D.nodes, root, x, valid, self, K, phi, cnt);
     if (valid)
       D.pot[p] = phi * K.G_over_a;
   }
