@@ -23,6 +23,83 @@
 
 using namespace hbtg;
 
+namespace hbtg
+{
+namespace
+{
+__global__ void k_pot_repack(DevState D, const float *__restrict__ pos, const float *__restrict__ mass)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
+  {
+    D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
+    D.vu[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    D.ty[i] = 1;
+    D.seg_of[i] = 0;
+    D.ord[i] = (int)i;
+  }
+}
+
+// One "subhalo" whose every particle is a source; the walk takes the
+// requested particles as targets (tgt list) with their self terms.
+__global__ void k_pot_plan(DevState D, int n_tgt, int phase)
+{
+  if (blockIdx.x != 0 || threadIdx.x != 0)
+    return;
+  const int n = (int)D.N;
+  if (phase == 0)
+  {
+    D.state[0] = kActive;
+    D.iter[0] = 1;
+    D.corr[0] = 0; // the build decides the periodic wrap as a first iteration does
+    D.wrap[0] = 0;
+    D.ngrav[0] = 0;
+    D.src_begin[0] = 0;
+    D.src_cnt[0] = n;
+    D.src_cnt[1] = 0;
+    D.tgt_cnt[0] = n_tgt;
+    D.chunk_cnt[0] = (n_tgt + kWarp - 1) / kWarp;
+    D.chunk_cnt[1] = 0;
+    D.sp_len[0] = n;
+    for (int d = 0; d < 3; d++)
+    {
+      D.bb_lo[d] = 0xffffffffu;
+      D.bb_hi[d] = 0u;
+    }
+    for (int t = 0; t < 6; t++)
+      D.factor[t] = 1.f;
+  }
+  else
+  {
+    D.corr[0] = 1;
+    D.self_cnt[0] = n_tgt;
+  }
+}
+
+__global__ void k_pot_targets(DevState D, const long long *__restrict__ tgt, int n_tgt, int *__restrict__ bad)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tgt)
+    return;
+  const long long i = tgt[t];
+  if (i < 0 || i >= D.N)
+  {
+    atomicExch(bad, 1);
+    D.tgt[t] = 0;
+    return;
+  }
+  D.tgt[t] = (int)i;
+}
+
+__global__ void k_pot_out(DevState D, int n_tgt, float *__restrict__ out)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n_tgt)
+    out[t] = D.pot[D.tgt[t]];
+}
+
+} // namespace
+} // namespace hbtg
+
 namespace
 {
 
@@ -57,6 +134,7 @@ enum Slot
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
   S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
+  S_POTI,
   S_NUM
 };
 
@@ -637,6 +715,96 @@ int host_call(void *arg)
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Tree potential of one particle set (GravityTree_t::Build + EvaluatePotential)
+// ---------------------------------------------------------------------------
+struct PotCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  long long ns, nt;
+  const float *pos, *mass;
+  const long long *tgt;
+  float *out;
+  cudaStream_t st;
+};
+
+int pot_call(void *arg)
+{
+  PotCall &c = *static_cast<PotCall *>(arg);
+  hbtg_handle *H = c.H;
+  HBTG_CUDA(cudaSetDevice(H->device));
+  cudaStream_t st = c.st;
+  Pool &P = H->pool;
+  PoolMem mem{H, st, {}};
+  IterationDriver<PoolMem> R(mem, st);
+  R.K = make_kparams(c.p, false);
+  R.S = 1;
+  R.seg_bits = 0;
+  R.sm_count = H->sm_count;
+  DevState &D = R.D;
+  D.S = 1;
+  D.N = c.ns;
+  const size_t n1 = (size_t)c.ns;
+  long long *off = P.get<long long>(S_OFF, 2);
+  const long long hoff[2] = {0, c.ns};
+  HBTG_CUDA(cudaMemcpyAsync(off, hoff, sizeof(hoff), cudaMemcpyHostToDevice, st));
+  D.off = off;
+  D.pm = P.get<float4>(S_PM, n1);
+  D.vu = P.get<float4>(S_VU, n1);
+  D.ty = P.get<uint8_t>(S_TY, n1);
+  D.seg_of = P.get<int>(S_SEG, n1);
+  D.ord = P.get<int>(S_ORD, n1);
+  D.sp = P.get<int>(S_SP, n1);
+  D.tgt = P.get<int>(S_TGT, std::max<size_t>(n1, (size_t)c.nt));
+  D.pot = P.get<float>(S_PHI, n1);
+  int *subi = P.get<int>(S_SUBI, (size_t)2 * 28);
+  int q = 0;
+  auto nexti = [&]() { return subi + (size_t)2 * (q++); };
+  D.n_s = nexti(); D.nbound = nexti(); D.nlast = nexti(); D.state = nexti(); D.corr = nexti(); D.iter = nexti();
+  D.wrap = nexti(); D.tracers = nexti(); D.nb_new = nexti(); D.src_begin = nexti(); D.src_cnt = nexti();
+  D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
+  D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
+  D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti(); D.nunsample = nexti(); D.ngrav = nexti();
+  D.self_cnt = nexti();
+  int *bad = nexti();
+  D.factor = P.get<float>(S_FACTOR, 6);
+  unsigned *bb = P.get<unsigned>(S_BB, 6);
+  D.bb_lo = bb;
+  D.bb_hi = bb + 3;
+  D.root = P.get<double>(S_ROOT, 4);
+  D.keyp = P.get<float>(S_KEYP, 12);
+  D.key = P.get<unsigned long long>(S_KEY, n1);
+  D.key_alt = P.get<unsigned long long>(S_KEYA, n1);
+  D.val = P.get<uint32_t>(S_VAL, n1);
+  D.val_alt = P.get<uint32_t>(S_VALA, n1);
+  D.k32 = P.get<uint32_t>(S_K32, n1);
+  D.k32_alt = P.get<uint32_t>(S_K32A, n1);
+  D.perm = P.get<uint32_t>(S_PERM, n1);
+  D.perm_alt = P.get<uint32_t>(S_PERMA, n1);
+  D.fb_list = P.get<int>(S_FBL, n1);
+  D.fb_count = P.get<int>(S_FBC, 1);
+  D.cnt = P.get<int>(S_CNT, n1 + 1);
+  D.X = P.get<int>(S_X, n1 + 1);
+  D.P = P.get<D4>(S_P, n1);
+  D.nodes = P.get<float4>(S_NODES, n1 * 3);
+  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  HBTG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  k_pot_repack<<<blocks_for(c.ns, 256), 256, 0, st>>>(D, c.pos, c.mass);
+  k_pot_plan<<<1, 32, 0, st>>>(D, (int)c.nt, 0);
+  R.check();
+  const int src_total = R.scan_counts(D.src_cnt, D.src_off, 1);
+  const int chunk_total = R.scan_counts(D.chunk_cnt, D.chunk_off, 1);
+  R.build_tree(src_total);
+  k_pot_targets<<<blocks_for(c.nt, 256), 256, 0, st>>>(D, c.tgt, (int)c.nt, bad);
+  k_pot_plan<<<1, 32, 0, st>>>(D, (int)c.nt, 1);
+  R.check();
+  R.walk(chunk_total);
+  k_pot_out<<<blocks_for(c.nt, 256), 256, 0, st>>>(D, (int)c.nt, c.out);
+  R.check();
+  return read_int(bad, st) ? HBTG_ERR_INVALID : HBTG_OK;
+}
+
 struct DevCall
 {
   hbtg_handle *H;
@@ -843,6 +1011,21 @@ int hbtg_features_device(hbtg_handle *h, const hbtg_params *p, const hbtg_batch 
   hbtg_batch copy = *b; // a features-only call writes no output
   DevCall c{h, p, &copy, static_cast<cudaStream_t>(cuda_stream), &wa};
   return guarded(dev_call, &c);
+}
+
+int hbtg_tree_potential_device(hbtg_handle *h, const hbtg_params *p, int64_t n_src, const float *pos,
+                               const float *mass, int64_t n_tgt, const int64_t *tgt_index, float *potential,
+                               void *cuda_stream)
+{
+  if (!h || !p || n_src <= 0 || n_src >= (1LL << 30) || n_tgt < 0 || n_tgt >= (1LL << 30) || !pos || !mass ||
+      (n_tgt > 0 && (!tgt_index || !potential)) || !(p->softening > 0) || !(p->open_angle > 0) ||
+      !(p->box_size > 0))
+    return HBTG_ERR_INVALID;
+  if (n_tgt == 0)
+    return HBTG_OK;
+  PotCall c{h, p, n_src, n_tgt, pos, mass, reinterpret_cast<const long long *>(tgt_index), potential,
+            static_cast<cudaStream_t>(cuda_stream)};
+  return guarded(pot_call, &c);
 }
 
 int hbtg_trace_labels_device(hbtg_handle *h, uint8_t *labels, int which, void *cuda_stream)

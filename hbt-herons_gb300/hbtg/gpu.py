@@ -50,6 +50,7 @@ def library(path=LIB):
         lib.hbtg_unbind_batch_warm_device.argtypes = [P, P, P, P, C.c_int64, P]
         lib.hbtg_features_device.argtypes = [P, P, P, P, P, P]
         lib.hbtg_trace_labels_device.argtypes = [P, P, C.c_int, P]
+        lib.hbtg_tree_potential_device.argtypes = [P, P, C.c_int64, P, P, C.c_int64, P, P, P]
         lib.hbtg_mlp_forward.argtypes = [P, P, P, C.c_int64, P]
         lib.hbtg_mlp_backward.argtypes = [P, P, P, P, C.c_int64, P, P, P]
         lib.hbtg_adam_step.argtypes = [P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
@@ -57,7 +58,8 @@ def library(path=LIB):
         for fn in ("hbtg_create", "hbtg_destroy", "hbtg_unbind_batch", "hbtg_unbind_batch_device", "hbtg_get_stats",
                    "hbtg_set_count_interactions", "hbtg_set_model", "hbtg_unbind_batch_learned",
                    "hbtg_unbind_batch_learned_device", "hbtg_unbind_batch_warm_device", "hbtg_features_device",
-                   "hbtg_trace_labels_device", "hbtg_mlp_forward", "hbtg_mlp_backward", "hbtg_adam_step"):
+                   "hbtg_trace_labels_device", "hbtg_mlp_forward", "hbtg_mlp_backward", "hbtg_adam_step",
+                   "hbtg_tree_potential_device"):
             getattr(lib, fn).restype = C.c_int
         _lib = lib
     return _lib
@@ -177,6 +179,22 @@ class Unbinder:
         if rc != 0:
             raise UnbindError(rc, "hbtg_features_device")
         return f[:n]
+
+    def tree_potential(self, params: Params, pos, mass, targets, device="cuda:0"):
+        """G/a * tree potential at the listed particles of one set
+        (hbtg_tree_potential_device); numpy in, numpy float32 out."""
+        import torch
+        t = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a, dtype=dt)).to(device)
+        dpos, dmass = t(pos, np.float32), t(mass, np.float32)
+        dtgt = t(targets, np.int64)
+        out = torch.empty(max(len(targets), 1), dtype=torch.float32, device=device)
+        rc = self.lib.hbtg_tree_potential_device(self.h, C.byref(params), len(mass), dpos.data_ptr(),
+                                                 dmass.data_ptr(), len(targets), dtgt.data_ptr(), out.data_ptr(),
+                                                 None)
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_tree_potential_device")
+        torch.cuda.synchronize()
+        return out[:len(targets)].cpu().numpy()
 
     def trace_labels_device(self, n, which=1, device="cuda:0", stream_ptr=0):
         """Labels of the last call (hbtg_trace_labels_device): torch uint8 [n];

@@ -213,6 +213,17 @@ void hbtg_default_params(hbtg_params *params);
  * capture.  All calls share the reserve: calls that overlap on the GPU race. */
 int hbtg_unbind_batch_noalloc(const hbtg_params *params, hbtg_batch *batch, void *cuda_stream);
 
+/* The tree potential of one particle set: GravityTree_t::Build over the n_src
+ * sources (src/gravity_tree.cpp:25-80, src/oct_tree.tpp:12-142) and
+ * EvaluatePotential (src/gravity_tree.cpp:82-166) at the sources listed in
+ * tgt_index, each with its self term cancelled (as Unbind evaluates its
+ * particles).  potential[t] = G/a * phi, in the geometry and FP32 arithmetic
+ * of the unbinding walk.  Device arrays: pos [3 n_src], mass [n_src],
+ * tgt_index [n_tgt] (int64 indices into the sources), potential [n_tgt]. */
+int hbtg_tree_potential_device(hbtg_handle *handle, const hbtg_params *params, int64_t n_src, const float *pos,
+                               const float *mass, int64_t n_tgt, const int64_t *tgt_index, float *potential,
+                               void *cuda_stream);
+
 /* Measurement utility, no counterpart in the reference: FP32 FMA throughput
  * of the device in TFLOP/s (the roofline denominator of the tree walk). */
 int hbtg_measure_fp32_peak(int device, double *tflops);

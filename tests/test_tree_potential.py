@@ -1,0 +1,103 @@
+"""The tree potential of the unbinding walk (hbtg_tree_potential_device, the
+GPU counterpart of GravityTree_t::Build + EvaluatePotential) against closed
+forms and against the oracle's FP64 tree: the known-answer tests the
+reference lacks for this path (two-particle spline kernel in its three
+regimes, a uniform sphere's central potential, periodic wrap across the box
+faces)."""
+import numpy as np
+import pytest
+
+from hbtg import abi, oracle, synthetic
+
+
+def spline_potential(r, m, soft, G=1.0):
+    """Gadget cubic-spline softened potential of a point mass (h = 2.8 soft)."""
+    h = 2.8 * soft
+    u = r / h
+    if u >= 1.0:
+        return -G * m / r
+    if u < 0.5:
+        w = -2.8 + u * u * (16.0 / 3.0 + u * u * (6.4 * u - 9.6))
+    else:
+        w = -3.2 + 1.0 / (15.0 * u) + u * u * (32.0 / 3.0 + u * (-16.0 + u * (9.6 - 32.0 / 15.0 * u)))
+    return G * m / h * w
+
+
+def _params(**kw):
+    base = dict(dm_only=1, box_size=100.0, softening=0.01, G=1.0)
+    base.update(kw)
+    return abi.parity_params(**base)
+
+
+def test_oracle_two_particle_kernel():
+    """The oracle restates the reference's kernel: pinned to the closed form."""
+    prm = _params()
+    for u in (0.2, 0.7, 1.5):
+        r = u * 2.8 * prm.softening
+        pos = np.array([[50.0, 50.0, 50.0], [50.0 + r, 50.0, 50.0]], np.float32)
+        mass = np.array([1.0, 2.0], np.float32)
+        got = oracle.tree_potential(prm, pos, mass, pos[:1], mass[:1])[0]
+        r32 = float(np.float32(50.0 + r) - np.float32(50.0))
+        assert got == pytest.approx(spline_potential(r32, 2.0, prm.softening), rel=1e-6)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("u", [0.2, 0.45, 0.7, 0.99, 1.5, 40.0])
+def test_two_particle_spline_kernel(unbinder, u):
+    prm = _params()
+    r = u * 2.8 * prm.softening
+    pos = np.array([[50.0, 50.0, 50.0], [50.0 + r, 50.0, 50.0]], np.float32)
+    mass = np.array([1.0, 2.0], np.float32)
+    got = unbinder.tree_potential(prm, pos, mass, [0, 1])
+    r32 = float(np.float32(50.0 + r) - np.float32(50.0))
+    assert got[0] == pytest.approx(spline_potential(r32, 2.0, prm.softening), rel=2e-6)
+    assert got[1] == pytest.approx(spline_potential(r32, 1.0, prm.softening), rel=2e-6)
+
+
+@pytest.mark.gpu
+def test_uniform_sphere_central_potential(unbinder):
+    """phi(0) = -3 G M / (2 R) for a uniform sphere (Monte Carlo scatter ~0.1%
+    at 2e5 points, softening and tree error below that)."""
+    rng = np.random.default_rng(3)
+    n, R = 200_000, 1.0
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    pos = d * (R * rng.random(n) ** (1.0 / 3.0))[:, None] + 50.0
+    pos = np.vstack([pos, [[50.0, 50.0, 50.0]]]).astype(np.float32)
+    mass = np.full(n + 1, 1.0 / n, np.float32)
+    mass[-1] = 1e-12  # a test particle at the centre
+    prm = _params(softening=0.001)
+    got = unbinder.tree_potential(prm, pos, mass, [n])[0]
+    assert got == pytest.approx(-1.5, rel=1e-2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("x", [-3.0, -0.1, 0.1, 50.0, 99.9, 100.1, 103.0])
+def test_periodic_wrap_across_box_faces(unbinder, x):
+    """Two particles; the separation is the nearest periodic image (NEAREST)."""
+    prm = _params(box_size=100.0, softening=0.001)
+    x0 = 0.2
+    pos = np.array([[x0, 10.0, 10.0], [x, 10.0, 10.0]], np.float32)
+    mass = np.array([1.0, 1.0], np.float32)
+    got = unbinder.tree_potential(prm, pos, mass, [0])[0]
+    dx = float(np.float32(x) - np.float32(x0))
+    half = 50.0
+    dx = dx - 100.0 if dx > half else (dx + 100.0 if dx < -half else dx)
+    assert got == pytest.approx(spline_potential(abs(dx), 1.0, prm.softening), rel=2e-6)
+
+
+@pytest.mark.gpu
+def test_tree_potential_matches_oracle_tree(unbinder):
+    """Same tree geometry and opening criterion as the oracle's FP64 tree: the
+    FP32 walk differs by rounding, and by the rare cell whose opening test sits
+    on the boundary in one precision and not the other."""
+    inp = synthetic.nfw_single(n=20_000, seed=5)
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    rng = np.random.default_rng(0)
+    tgt = np.sort(rng.choice(inp.n_particles, 3000, replace=False))
+    got = unbinder.tree_potential(prm, inp.pos, inp.mass, tgt).astype(np.float64)
+    ref = oracle.tree_potential(prm, inp.pos, inp.mass, inp.pos[tgt], inp.mass[tgt])
+    rel = np.abs(got - ref) / np.abs(ref)
+    assert np.median(rel) <= 2e-6, np.median(rel)
+    assert np.percentile(rel, 99) <= 1e-4, np.percentile(rel, 99)
+    assert rel.max() <= 5e-3, rel.max()
