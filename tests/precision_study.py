@@ -81,10 +81,10 @@ def run(unbinder, n_host=10_000_000, n_sat=200, n_subset=100_000, seed=0, n_subs
         pot_gpu[inside] = unbinder.tree_potential(prm, bpos, bmass, src_index[esub[inside]])
         pot_dir[inside] = oracle.tree_potential(prm, bpos, bmass, inp.pos[esub[inside]], inp.mass[esub[inside]],
                                                 direct=True)
-    if (~inside).any():  # massless copies appended as extra sources stand for outside particles
+    if (~inside).any():  # copies of negligible mass appended as extra sources stand for outside particles
         outs = esub[~inside]
         pos2 = np.vstack([bpos, inp.pos[outs]])
-        mass2 = np.concatenate([bmass, np.zeros(len(outs), np.float32)])
+        mass2 = np.concatenate([bmass, np.full(len(outs), 1e-30, np.float32)])
         pot_gpu[~inside] = unbinder.tree_potential(prm, pos2, mass2, nb + np.arange(len(outs)))
         pot_dir[~inside] = oracle.tree_potential(prm, bpos, bmass, inp.pos[outs], None, direct=True)
     dv = inp.vel[esub].astype(np.float64) - out.ref_vel[0].astype(np.float64)
