@@ -23,6 +23,13 @@ def spline_potential(r, m, soft, G=1.0):
     return G * m / h * w
 
 
+def self_term_ulp(m, soft):
+    """The walk cancels a particle's self-interaction by starting its sum at
+    +m/soft against its own leaf's -m/soft; in FP32 that leaves about one ulp
+    of m/soft, which dominates the error of a potential made of few particles."""
+    return float(np.spacing(np.float32(m / soft)))
+
+
 def _params(**kw):
     base = dict(dm_only=1, box_size=100.0, softening=0.01, G=1.0)
     base.update(kw)
@@ -50,8 +57,9 @@ def test_two_particle_spline_kernel(unbinder, u):
     mass = np.array([1.0, 2.0], np.float32)
     got = unbinder.tree_potential(prm, pos, mass, [0, 1])
     r32 = float(np.float32(50.0 + r) - np.float32(50.0))
-    assert got[0] == pytest.approx(spline_potential(r32, 2.0, prm.softening), rel=2e-6)
-    assert got[1] == pytest.approx(spline_potential(r32, 1.0, prm.softening), rel=2e-6)
+    for k, (m_self, m_other) in enumerate(((1.0, 2.0), (2.0, 1.0))):
+        tol = 3 * self_term_ulp(m_self, prm.softening)
+        assert got[k] == pytest.approx(spline_potential(r32, m_other, prm.softening), rel=2e-6, abs=tol)
 
 
 @pytest.mark.gpu
@@ -83,7 +91,8 @@ def test_periodic_wrap_across_box_faces(unbinder, x):
     dx = float(np.float32(x) - np.float32(x0))
     half = 50.0
     dx = dx - 100.0 if dx > half else (dx + 100.0 if dx < -half else dx)
-    assert got == pytest.approx(spline_potential(abs(dx), 1.0, prm.softening), rel=2e-6)
+    tol = 3 * self_term_ulp(1.0, prm.softening)
+    assert got == pytest.approx(spline_potential(abs(dx), 1.0, prm.softening), rel=2e-6, abs=tol)
 
 
 @pytest.mark.gpu
