@@ -68,9 +68,37 @@ public:
   Unbinder(const Unbinder &) = delete;
   Unbinder &operator=(const Unbinder &) = delete;
 
+  // Loads the learned warm start's proposer (weights of hbtg_mlp_forward's layout).
+  void set_model(const std::vector<float> &weights, float threshold, float exclude_below, int64_t min_particles)
+  {
+    if (weights.size() != HBTG_MLP_PARAMS)
+      throw std::runtime_error("hbtg_set_model: wrong number of weights");
+    hbtg_model m{weights.data(), threshold, min_particles, exclude_below};
+    const int rc = hbtg_set_model(h_, &m);
+    if (rc != HBTG_OK)
+      throw std::runtime_error(std::string("hbtg_set_model: ") + hbtg_status_string(rc));
+  }
+
   // Unbinds every subhalo pointed to by `subs` in one GPU call.
   template <class Subhalo>
   void unbind(const hbtg_params &params_in, const std::vector<Subhalo *> &subs, const Options &opt)
+  {
+    run(params_in, subs, opt, false);
+  }
+
+  // The same with the learned warm start (set_model first).  The previous
+  // output's knowledge comes from the Subhalo_t members as Unbind finds them:
+  // Nbound (its bound particles lead Particles) and ParticleBindingEnergies
+  // when the previous output saved them.  No potential subsampling.
+  template <class Subhalo>
+  void unbind_learned(const hbtg_params &params_in, const std::vector<Subhalo *> &subs, const Options &opt)
+  {
+    run(params_in, subs, opt, true);
+  }
+
+private:
+  template <class Subhalo>
+  void run(const hbtg_params &params_in, const std::vector<Subhalo *> &subs, const Options &opt, bool learned)
   {
     hbtg_params params = params_in;
     if (params.max_sample_size > 0 && !params.prepared_subsample)
@@ -148,14 +176,34 @@ public:
     b.potential = opt.save_potential ? potential.data() : nullptr;
     b.iterations = iters.data();
     b.status = status.data();
-    const int rc = hbtg_unbind_batch(h_, &params, &b);
+    int rc;
+    if (learned)
+    {
+      std::vector<int64_t> nb_prev(ns);
+      std::vector<float> e_prev(n, 0.f);
+      bool have_e = false;
+      for (int64_t s = 0; s < ns; s++)
+      {
+        const Subhalo &sub = *subs[s];
+        nb_prev[s] = std::min<int64_t>((int64_t)sub.Nbound, (int64_t)sub.Particles.size());
+        const auto &E = sub.ParticleBindingEnergies;
+        for (int64_t k = 0; k < nb_prev[s] && k < (int64_t)E.size(); k++)
+        {
+          e_prev[offsets[s] + k] = E[k];
+          have_e = true;
+        }
+      }
+      hbtg_prior prior{nb_prev.data(), have_e ? e_prev.data() : nullptr};
+      rc = hbtg_unbind_batch_learned(h_, &params, &b, &prior);
+    }
+    else
+      rc = hbtg_unbind_batch(h_, &params, &b);
     if (rc != HBTG_OK && rc != HBTG_ERR_MAX_ITER)
       throw std::runtime_error(std::string("hbtg_unbind_batch: ") + hbtg_status_string(rc));
     for (int64_t s = 0; s < ns; s++)
       apply(*subs[s], s, offsets, b, opt);
   }
 
-private:
   template <class P>
   static auto exempt(const P &p, const hbtg_params &prm, const Options &opt) -> decltype((void)p.Type, bool())
   {
