@@ -169,10 +169,16 @@ struct IterationDriver
   {
     if (chunk_total <= 0)
       return;
+    unsigned grid = grid_for(chunk_total, 8);
+    if (D.walk_ctr)
+    { // one resident wave (8 blocks of 8 warps per SM) over per-SM chunk ranges
+      mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)sm_count, st));
+      grid = std::min<unsigned>(grid, (unsigned)sm_count * 8u);
+    }
     if (K.count_interactions)
-      k_walk<true><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+      k_walk<true><<<grid, 256, 0, st>>>(D, K, chunk_total, sm_count);
     else
-      k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+      k_walk<false><<<grid, 256, 0, st>>>(D, K, chunk_total, sm_count);
     launches++;
     walk_launches++;
     check();
@@ -291,9 +297,9 @@ struct IterationDriver
     if (src_total == 0)
       return;
     build_tree(src_total);
-    k_walk<false><<<grid_for(chunk_total, 8), 256, 0, st>>>(D, K, chunk_total);
+    walk(chunk_total);
     k_refine_keys<<<grid_for(src_total, 256), 256, 0, st>>>(D, K, src_total);
-    launches += 2;
+    launches++;
     check();
     uint32_t *sorted = sort_energy_keys(src_total);
     k_refine_write<<<grid_for(src_total, 256), 256, 0, st>>>(D, sorted, src_total);

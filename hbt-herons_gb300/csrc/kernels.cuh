@@ -103,6 +103,7 @@ struct DevState
   float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
   int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
+  unsigned *walk_ctr = nullptr; // per-SM chunk counters of the walk (zeroed before each walk), or null
   // warm start (null on the plain path)
   int *warm = nullptr;       // 1 = started from a proposal, 2 = restarted cold, 3 = warm start verified
   int *nexcl = nullptr;      // particles the proposal excluded (parked at the end of the segment at the start)
@@ -777,38 +778,74 @@ __device__ __forceinline__ void walk_lane(const float4 *__restrict__ T, int root
   out = sum - comp;
 }
 
+// One 32-target chunk of the walk (a warp).
 template <bool Count>
-__global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_chunks)
+__device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, int c, int lane,
+                                           unsigned long long &cnt)
 {
-  const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int s = find_segment<int>(D.chunk_off, D.S, c);
+  const int t = (c - D.chunk_off[s]) * kWarp + lane;
+  const bool valid = t < D.tgt_cnt[s];
+  const bool corr = D.corr[s] != 0;
+  const int ngrav = D.ngrav[s];
+  int p = 0;
+  if (valid) // correction: key-ordered bound set; subsampled: every candidate; else the sources
+    p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
+  const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  // self term: only targets that are tree sources (with their upscaled mass)
+  const int nself = (corr && D.self_cnt) ? D.self_cnt[s] : 0;
+  const float self =
+    !valid ? 0.f : (corr ? (t < nself ? x.w : 0.f) : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w));
+  const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
+  float phi = 0.f;
+  if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
+    ;
+  else if (D.wrap[s])
+    walk_lane<true>(D.nodes, root, x, valid, self, K, phi, cnt);
+  else
+    walk_lane<false>(D.nodes, root, x, valid, self, K, phi, cnt);
+  if (valid)
+    D.pot[p] = phi * K.G_over_a;
+}
+
+// With walk counters, the chunks (key order) are split into `nranges`
+// contiguous ranges, one per SM: the warps resident on an SM take the chunks
+// of their own range in order, so they walk neighbouring targets and share
+// the tree slots in L1; a warp whose range is used up moves on to the next
+// ranges (each tried once).  Without counters, a grid-stride loop.
+template <bool Count>
+__global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_chunks, int nranges)
+{
   const int lane = threadIdx.x & 31;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
   unsigned long long cnt = 0;
-  for (int c = warp_global; c < total_chunks; c += nwarps)
+  if (D.walk_ctr)
   {
-    const int s = find_segment<int>(D.chunk_off, D.S, c);
-    const int t = (c - D.chunk_off[s]) * kWarp + lane;
-    const bool valid = t < D.tgt_cnt[s];
-    const bool corr = D.corr[s] != 0;
-    const int ngrav = D.ngrav[s];
-    int p = 0;
-    if (valid) // correction: key-ordered bound set; subsampled: every candidate; else the sources
-      p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
-    const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-    // self term: only targets that are tree sources (with their upscaled mass)
-    const int nself = (corr && D.self_cnt) ? D.self_cnt[s] : 0;
-    const float self =
-      !valid ? 0.f : (corr ? (t < nself ? x.w : 0.f) : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w));
-    const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
-    float phi = 0.f;
-    if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
-      ;
-    else if (D.wrap[s])
-      walk_lane<true>(D.nodes, root, x, valid, self, K, phi, cnt);
-    else
-      walk_lane<false>(D.nodes, root, x, valid, self, K, phi, cnt);
-    if (valid)
-      D.pot[p] = phi * K.G_over_a;
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const int per = (total_chunks + nranges - 1) / nranges;
+    int r = (int)(smid % (unsigned)nranges);
+    for (int tries = 0; tries < nranges;)
+    {
+      int got = 0;
+      if (lane == 0)
+        got = (int)atomicAdd(&D.walk_ctr[r], 1u);
+      got = __shfl_sync(0xffffffffu, got, 0);
+      const long long c = (long long)r * per + got;
+      if (got >= per || c >= total_chunks)
+      {
+        r = (r + 1 == nranges) ? 0 : r + 1;
+        tries++;
+        continue;
+      }
+      walk_chunk<Count>(D, K, (int)c, lane, cnt);
+    }
+  }
+  else
+  {
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int c = warp_global; c < total_chunks; c += nwarps)
+      walk_chunk<Count>(D, K, c, lane, cnt);
   }
   if (Count)
   {

@@ -134,7 +134,7 @@ enum Slot
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
   S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
-  S_POTI,
+  S_POTI, S_WCTR,
   S_NUM
 };
 
@@ -402,6 +402,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
   D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti(); D.nunsample = nexti(); D.ngrav = nexti();
   D.nb1 = P.get<int>(S_NB1, (size_t)S + 1);
+  D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));
   D.factor = P.get<float>(S_FACTOR, (size_t)S * 6);
   float *subf = P.get<float>(S_SUBF, (size_t)S * 8);
   D.old_pos = subf;
@@ -789,6 +790,7 @@ int pot_call(void *arg)
   D.P = P.get<D4>(S_P, n1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));
   HBTG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
   k_pot_repack<<<blocks_for(c.ns, 256), 256, 0, st>>>(D, c.pos, c.mass);
   k_pot_plan<<<1, 32, 0, st>>>(D, (int)c.nt, 0);
