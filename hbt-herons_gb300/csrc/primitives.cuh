@@ -199,34 +199,77 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const K *__restric
   table[(long long)threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
+// Stable scatter of one tile: the tile's items are first ranked by digit
+// into shared memory (so that each digit's items are contiguous there, in
+// their input order), then written out in that order, so consecutive threads
+// store to consecutive addresses of a digit's output run.
 template <typename K>
 __global__ void __launch_bounds__(kRadixThreads)
   k_radix_scatter(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
                   uint32_t *__restrict__ vout, long long n, int shift, uint32_t mask, const int *__restrict__ table,
                   int tiles)
 {
-  __shared__ int s_off[256];
-  __shared__ int s_base[256];
+  __shared__ K s_key[kRadixTile];
+  __shared__ uint32_t s_val[kRadixTile];
+  __shared__ int s_off[256];   // this tile's first output slot per digit (scanned table)
+  __shared__ int s_start[256]; // first shared-memory slot per digit
+  __shared__ int s_base[256];  // items of the digit ranked so far
   __shared__ int s_warp[kRadixThreads / kWarp][256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  s_off[threadIdx.x] = table[(long long)threadIdx.x * tiles + blockIdx.x];
-  s_base[threadIdx.x] = 0;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long base = (long long)blockIdx.x * kRadixTile;
+  const int count = (int)min((long long)kRadixTile, n - base);
+  s_off[tid] = table[(long long)tid * tiles + blockIdx.x];
+  s_base[tid] = 0;
+  s_start[tid] = 0;
+  __syncthreads();
+  K key[kRadixItems];
+  uint32_t val[kRadixItems];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; r++)
+  {
+    const int k = r * kRadixThreads + tid;
+    key[r] = k < count ? kin[base + k] : K(0);
+    val[r] = k < count ? vin[base + k] : 0u;
+    if (k < count)
+      atomicAdd(&s_start[(uint32_t)(key[r] >> shift) & mask], 1);
+  }
+  __syncthreads();
+  if (warp == 0)
+  { // exclusive scan of the 256 digit counts, 8 per lane
+    int v[8], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      v[q] = s_start[8 * lane + q];
+      sum += v[q];
+    }
+    int incl = sum;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o)
+        incl += y;
+    }
+    int run = incl - sum;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+    {
+      s_start[8 * lane + q] = run;
+      run += v[q];
+    }
+  }
   const uint32_t lt_mask = (1u << lane) - 1u;
+#pragma unroll
   for (int r = 0; r < kRadixItems; r++)
   {
 #pragma unroll
     for (int w = 0; w < kRadixThreads / kWarp; w++)
-      s_warp[w][threadIdx.x] = 0;
+      s_warp[w][tid] = 0;
     __syncthreads();
-    const long long i = base + r * kRadixThreads + threadIdx.x;
-    const bool valid = i < n;
-    K key = valid ? kin[i] : K(0);
-    uint32_t val = valid ? vin[i] : 0u;
-    const uint32_t d = valid ? ((uint32_t)(key >> shift) & mask) : (256u + lane);
+    const bool valid = r * kRadixThreads + tid < count;
+    const uint32_t d = valid ? ((uint32_t)(key[r] >> shift) & mask) : (256u + lane);
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const int leader = __ffs(peers) - 1;
-    if (valid && lane == leader)
+    if (valid && lane == __ffs(peers) - 1)
       s_warp[warp][d] = __popc(peers);
     __syncthreads();
     if (valid)
@@ -234,16 +277,24 @@ __global__ void __launch_bounds__(kRadixThreads)
       int rank = s_base[d] + __popc(peers & lt_mask);
       for (int w = 0; w < warp; w++)
         rank += s_warp[w][d];
-      const int dst = s_off[d] + rank;
-      kout[dst] = key;
-      vout[dst] = val;
+      s_key[s_start[d] + rank] = key[r];
+      s_val[s_start[d] + rank] = val[r];
     }
     __syncthreads();
     int add = 0;
 #pragma unroll
     for (int w = 0; w < kRadixThreads / kWarp; w++)
-      add += s_warp[w][threadIdx.x];
-    s_base[threadIdx.x] += add;
+      add += s_warp[w][tid];
+    s_base[tid] += add;
+  }
+  __syncthreads();
+  for (int k = tid; k < count; k += kRadixThreads)
+  {
+    const K kk = s_key[k];
+    const uint32_t d = (uint32_t)(kk >> shift) & mask;
+    const int dst = s_off[d] + (k - s_start[d]);
+    kout[dst] = kk;
+    vout[dst] = s_val[k];
   }
 }
 
