@@ -359,6 +359,54 @@ def stripped(n_sub=20_000, seed=0, nmin=20, nmax=1_000_000, box=500.0, flip=0.05
     return inp
 
 
+def nested_system(seed=0, n_host=20_000, n_sat=6, n_subsat=3, box=100.0):
+    """A FoF-like subhalo tree for nested unbinding: a host NFW halo (c=6),
+    n_sat satellites (NFW, 300-3000 particles, 20 % heated) on orbits inside it,
+    and n_subsat sub-satellites (NFW, 60-300 particles) inside the first
+    satellites.  Every subhalo's source is its own particles; the host centre
+    sits near a box corner so the system straddles the periodic boundary.
+    Returns (nested.Particles, members, parent, frames)."""
+    from .nested import Particles
+    rng = np.random.Generator(np.random.PCG64(seed))
+    comps, parent = [], []
+    m200 = n_host * _m(6.0) / _m(12.0)
+    r200h = r200_of(m200)
+    centre = np.array([[0.2 * r200h, box - 0.1 * r200h, box / 2]])
+    hp, hv, _, _ = _nfw_halo_particles(rng, np.array([n_host]), np.array([6.0]), 1.0, np.array([0.1]), 1.5, 3.0,
+                                       False, box, centre, np.zeros((1, 3)), do_wrap=False)
+    comps.append((hp, hv))
+    parent.append(-1)
+    sat_centres = []
+    for i in range(n_sat):
+        n = int(rng.integers(300, 3000))
+        rr = r200h * rng.uniform(0.2, 0.8)
+        c = centre + _random_dirs(rng, 1) * rr
+        vc = np.sqrt(m200 * _m(6.0 * rr / r200h) / _m(6.0) / rr)
+        v = _random_dirs(rng, 1) * 0.7 * vc
+        p, vel, _, _ = _nfw_halo_particles(rng, np.array([n]), np.array([10.0]), 1.0, np.array([0.2]), 1.5, 3.0,
+                                           False, box, c, v, do_wrap=False)
+        comps.append((p, vel))
+        parent.append(0)
+        sat_centres.append((c, v, r200_of(n * _m(10.0) / _m(20.0))))
+    for j in range(n_subsat):
+        c0, v0, r0 = sat_centres[j % len(sat_centres)]
+        n = int(rng.integers(60, 300))
+        c = c0 + _random_dirs(rng, 1) * r0 * rng.uniform(0.2, 0.6)
+        p, vel, _, _ = _nfw_halo_particles(rng, np.array([n]), np.array([10.0]), 1.0, np.array([0.2]), 1.5, 3.0,
+                                           False, box, c, v0, do_wrap=False)
+        comps.append((p, vel))
+        parent.append(1 + (j % len(sat_centres)))
+    counts = np.array([len(p) for p, _ in comps], np.int64)
+    pos = _wrap(np.concatenate([p for p, _ in comps]), box)
+    vel = np.concatenate([v for _, v in comps])
+    inp = _finish(pos, vel, np.ones(len(pos)), counts, box, rng)
+    parts = Particles(inp.pos, inp.vel, inp.mass, inp.id)
+    members = [np.arange(inp.offsets[s], inp.offsets[s + 1], dtype=np.int64) for s in range(len(counts))]
+    frames = dict(ref_pos=inp.ref_pos, ref_vel=inp.ref_vel, mostbound_pos=inp.mostbound_pos,
+                  mostbound_vel=inp.mostbound_vel, most_bound_id=inp.most_bound_id)
+    return parts, members, np.array(parent, np.int64), frames
+
+
 def small_cases(seed=0, box=100.0):
     """A small mixed batch for parity tests: NFW haloes of 20-3000 particles,
     one empty subhalo, one single-particle subhalo, a halo straddling the box
