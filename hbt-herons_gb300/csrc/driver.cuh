@@ -141,9 +141,7 @@ struct IterationDriver
     const int internal = scan_counts(D.cnt, D.X, src_total);
     D.nodes = mem.tree_slots((long long)src_total + 2LL * internal);
     tree_nodes += internal;
-    k_prefix_prep<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
-    launches++;
-    scan<D4, true>(D.P, D.P, src_total, mem.d4_scratch(src_total), st, &launches);
+    scan_load<D4, true>(PrefixLoad{D}, D.P, src_total, mem.d4_scratch(src_total), st, &launches);
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
     k_record_key_order<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
     launches += 2;

@@ -637,19 +637,21 @@ __global__ void k_tree_count(DevState D, int total)
   D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
 }
 
-// Double prefix sums of mass and mass-weighted offset from the root centre.
-__global__ void k_prefix_prep(DevState D, int total)
+// Item j of the double prefix sums of mass and mass-weighted offset from the
+// root centre (scanned by scan_load straight into D.P).
+struct PrefixLoad
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= total)
-    return;
-  const int p = (int)D.val[j];
-  const int s = D.seg_of[p];
-  const double *r = D.root + 4 * s;
-  const float4 x = D.pm[p];
-  const double m = source_mass(D, s, p);
-  D.P[j] = D4{m, m * ((double)x.x - r[0]), m * ((double)x.y - r[1]), m * ((double)x.z - r[2])};
-}
+  DevState D;
+  __device__ __forceinline__ D4 operator()(long long j) const
+  {
+    const int p = (int)D.val[j];
+    const int s = D.seg_of[p];
+    const double *r = D.root + 4 * s;
+    const float4 x = D.pm[p];
+    const double m = source_mass(D, s, p);
+    return D4{m, m * ((double)x.x - r[0]), m * ((double)x.y - r[1]), m * ((double)x.z - r[2])};
+  }
+};
 
 // Writes the particle leaf and the cells that start at item j, in preorder.
 // Slot index: cell (j, level lo+t) = j + 2 X[j] + 2t; leaf of item j =
@@ -674,7 +676,10 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   const int kstar = __float_as_int(D.keyp[12 * s + 8]);
   const unsigned long long kj = D.key[j];
   const D4 before = (j > 0) ? D.P[j - 1] : D4{0., 0., 0., 0.};
-  for (int t = 0; t < c; t++)
+  // Deepest cell first: a shallower cell ends at or after a deeper one, so
+  // each search gallops forward from the previous cell's last item.
+  int a = j; // key[a] shares the current prefix with item j
+  for (int t = c - 1; t >= 0; t--)
   {
     const int L = lo + t;
     // last item whose first L digits equal those of item j
@@ -685,8 +690,19 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
     {
       const int shift = 63 - 3 * L;
       const unsigned long long pref = kj >> shift;
-      int a = j, e = seg_end; // invariant: key[a] has the prefix; answer in [a, e)
-      while (e - a > 1)
+      int e, step = 1;
+      for (;;)
+      {
+        const int probe = a + step;
+        if (probe >= seg_end || (D.key[probe] >> shift) != pref)
+        {
+          e = min(probe, seg_end);
+          break;
+        }
+        a = probe;
+        step <<= 1;
+      }
+      while (e - a > 1) // key[a] has the prefix; answer in [a, e)
       {
         const int mid = (a + e) >> 1;
         if ((D.key[mid] >> shift) == pref)

@@ -1,7 +1,8 @@
 // primitives.cuh - hand-written device-wide scan and LSD radix sort.
 //
-// Both are tile-based (2048 items per 256-thread block): a per-tile pass,
-// a scan of the per-tile totals (recursive) and a fix-up pass.  The radix
+// Both are tile-based (2048 items per 256-thread block).  The scan is
+// reduce-then-scan: per-tile sums, a scan of them (recursive), then a pass
+// that scans each tile with its offset.  The radix
 // sort is stable, with 8-bit digits; segmented sorting is done by sorting on
 // the key and then, stably, on the segment id (see unbind.cu).
 #pragma once
@@ -56,84 +57,113 @@ __device__ __forceinline__ D4 shfl_up<D4>(D4 v, int d)
             __shfl_up_sync(0xffffffffu, v.y, d), __shfl_up_sync(0xffffffffu, v.z, d)};
 }
 
-// Block-wide exclusive scan of one value per thread; returns the block total.
 template <typename T>
-__device__ __forceinline__ T block_exclusive_scan(T v, T &total)
+__device__ __forceinline__ T shfl_idx(T v, int src)
 {
-  __shared__ T warp_tot[kScanThreads / kWarp];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T inc = v;
+  return __shfl_sync(0xffffffffu, v, src);
+}
+template <>
+__device__ __forceinline__ D4 shfl_idx<D4>(D4 v, int src)
+{
+  return D4{__shfl_sync(0xffffffffu, v.m, src), __shfl_sync(0xffffffffu, v.x, src),
+            __shfl_sync(0xffffffffu, v.y, src), __shfl_sync(0xffffffffu, v.z, src)};
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_inclusive_scan(T v, int lane)
+{
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1)
   {
-    T o = shfl_up(inc, d);
+    const T o = shfl_up(v, d);
     if (lane >= d)
-      inc = inc + o;
+      v = v + o;
   }
-  if (lane == 31)
-    warp_tot[warp] = inc;
-  __syncthreads();
-  T warp_off = zero_of<T>();
-  T tot = zero_of<T>();
-#pragma unroll
-  for (int w = 0; w < kScanThreads / kWarp; w++)
-  {
-    if (w < warp)
-      warp_off = warp_off + warp_tot[w];
-    tot = tot + warp_tot[w];
-  }
-  __syncthreads();
-  total = tot;
-  // exclusive = inclusive - v, written without subtraction (exact for doubles)
-  T excl = shfl_up(inc, 1);
-  if (lane == 0)
-    excl = zero_of<T>();
-  return warp_off + excl;
+  return v;
 }
 
-// Scans each tile; writes tile totals when `tile_sums` is non-null.
-template <typename T, bool Inclusive>
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const T *__restrict__ in, T *__restrict__ out,
-                                                             T *__restrict__ tile_sums, long long n)
+// Scan input read straight from an array.
+template <typename T>
+struct ArrayLoad
 {
-  constexpr int kTile = scan_tile<T>();
-  constexpr int kScanItems = scan_items<T>();
-  __shared__ T s[kTile];
-  const long long base = (long long)blockIdx.x * kTile;
-  for (int i = threadIdx.x; i < kTile; i += kScanThreads)
-    s[i] = (base + i < n) ? in[base + i] : zero_of<T>();
-  __syncthreads();
-  T local[kScanItems];
+  const T *in;
+  __device__ __forceinline__ T operator()(long long i) const { return in[i]; }
+};
+
+// Reduce-then-scan.  A tile is 8 warps x 32 lanes x scan_items<T>() rows;
+// warp w owns the contiguous items [w*32*rows, (w+1)*32*rows) of its tile and
+// reads them one coalesced row of 32 at a time.  Pass 1 sums each tile, the
+// tile sums are scanned (recursively), pass 2 scans each tile row by row with
+// warp shuffles and adds the tile's offset.  `Load` supplies item i, so an
+// input that is a function of other arrays needs no array of its own.
+template <typename T, typename Load>
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Load load, T *__restrict__ tile_sums, long long n)
+{
+  constexpr int kTile = scan_tile<T>(), kRows = scan_items<T>();
+  __shared__ T warp_tot[kScanThreads / kWarp];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long wbase = (long long)blockIdx.x * kTile + (long long)warp * kWarp * kRows;
   T acc = zero_of<T>();
 #pragma unroll
-  for (int k = 0; k < kScanItems; k++)
+  for (int k = 0; k < kRows; k++)
   {
-    local[k] = acc;
-    acc = acc + s[threadIdx.x * kScanItems + k];
+    const long long i = wbase + k * kWarp + lane;
+    if (i < n)
+      acc = acc + load(i);
   }
-  T total;
-  const T off = block_exclusive_scan(acc, total);
-#pragma unroll
-  for (int k = 0; k < kScanItems; k++)
-  {
-    const T v = s[threadIdx.x * kScanItems + k];
-    s[threadIdx.x * kScanItems + k] = Inclusive ? (off + local[k]) + v : off + local[k];
-  }
+  acc = warp_inclusive_scan(acc, lane);
+  if (lane == 31)
+    warp_tot[warp] = acc;
   __syncthreads();
-  for (int i = threadIdx.x; i < kTile; i += kScanThreads)
-    if (base + i < n)
-      out[base + i] = s[i];
-  if (tile_sums && threadIdx.x == 0)
-    tile_sums[blockIdx.x] = total;
+  if (threadIdx.x == 0)
+  {
+    T tot = zero_of<T>();
+#pragma unroll
+    for (int w = 0; w < kScanThreads / kWarp; w++)
+      tot = tot + warp_tot[w];
+    tile_sums[blockIdx.x] = tot;
+  }
 }
 
-template <typename T>
-__global__ void k_add_tile_offsets(T *__restrict__ out, const T *__restrict__ tile_off, long long n)
+template <typename T, bool Inclusive, typename Load>
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(Load load, T *out, const T *__restrict__ tile_off,
+                                                             long long n)
 {
-  constexpr int kTile = scan_tile<T>();
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && i >= kTile)
-    out[i] = tile_off[i / kTile] + out[i];
+  constexpr int kTile = scan_tile<T>(), kRows = scan_items<T>();
+  __shared__ T warp_tot[kScanThreads / kWarp];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long wbase = (long long)blockIdx.x * kTile + (long long)warp * kWarp * kRows;
+  T v[kRows];
+  T carry = zero_of<T>();
+#pragma unroll
+  for (int k = 0; k < kRows; k++)
+  {
+    const long long i = wbase + k * kWarp + lane;
+    const T x = (i < n) ? load(i) : zero_of<T>();
+    const T inc = warp_inclusive_scan(x, lane);
+    T part = inc;
+    if (!Inclusive)
+    { // exclusive = the previous lane's inclusive value (no subtraction: exact for doubles)
+      part = shfl_up(inc, 1);
+      if (lane == 0)
+        part = zero_of<T>();
+    }
+    v[k] = carry + part;
+    carry = carry + shfl_idx(inc, 31);
+  }
+  if (lane == 0)
+    warp_tot[warp] = carry;
+  __syncthreads(); // every item of the tile is read before any is written (in == out allowed)
+  T off = tile_off ? tile_off[blockIdx.x] : zero_of<T>();
+  for (int w = 0; w < warp; w++)
+    off = off + warp_tot[w];
+#pragma unroll
+  for (int k = 0; k < kRows; k++)
+  {
+    const long long i = wbase + k * kWarp + lane;
+    if (i < n)
+      out[i] = off + v[k];
+  }
 }
 
 // Scratch needed by scan<T>(n): sum over recursion levels of the tile counts.
@@ -150,10 +180,10 @@ inline size_t scan_scratch_elems(long long n)
   return tot + 2;
 }
 
-// Device-wide scan of n items (in may equal out).  `scratch` must hold
+// Device-wide scan of the n items load(0..n-1) into out.  `scratch` must hold
 // scan_scratch_elems(n) items of T.
-template <typename T, bool Inclusive>
-void scan(const T *in, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
+template <typename T, bool Inclusive, typename Load>
+void scan_load(Load load, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
 {
   constexpr int kTile = scan_tile<T>();
   if (n <= 0)
@@ -161,15 +191,22 @@ void scan(const T *in, T *out, long long n, T *scratch, cudaStream_t st, int64_t
   const long long tiles = (n + kTile - 1) / kTile;
   if (tiles == 1)
   {
-    k_scan_tiles<T, Inclusive><<<1, kScanThreads, 0, st>>>(in, out, nullptr, n);
+    k_scan_apply<T, Inclusive, Load><<<1, kScanThreads, 0, st>>>(load, out, nullptr, n);
     (*launches)++;
     return;
   }
   T *sums = scratch, *sums_scanned = scratch + tiles;
-  k_scan_tiles<T, Inclusive><<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, sums, n);
-  scan<T, false>(sums, sums_scanned, tiles, scratch + 2 * tiles, st, launches);
-  k_add_tile_offsets<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, sums_scanned, n);
+  k_scan_reduce<T, Load><<<(unsigned)tiles, kScanThreads, 0, st>>>(load, sums, n);
+  scan_load<T, false>(ArrayLoad<T>{sums}, sums_scanned, tiles, scratch + 2 * tiles, st, launches);
+  k_scan_apply<T, Inclusive, Load><<<(unsigned)tiles, kScanThreads, 0, st>>>(load, out, sums_scanned, n);
   *launches += 2;
+}
+
+// Device-wide scan of n items (in may equal out).
+template <typename T, bool Inclusive>
+void scan(const T *in, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
+{
+  scan_load<T, Inclusive>(ArrayLoad<T>{in}, out, n, scratch, st, launches);
 }
 
 // ---------------------------------------------------------------------------
