@@ -12,7 +12,7 @@
 //   int *scan_scratch(long long n)               scratch for scan<int>(n)
 //   int *radix_table(long long n)                table for radix_sort_pairs(n)
 //   int *radix_scan_scratch(long long n)
-//   D4 *d4_scratch(long long n)                  scratch for scan<D4>(n)
+//   I4 *prefix_scratch(long long n)              scratch for scan<I4>(n)
 //   float4 *tree_slots(long long slots)          tree storage (may throw when too large)
 //   void mark(int phase)                         phase boundary for timing (may be a no-op)
 #pragma once
@@ -141,7 +141,7 @@ struct IterationDriver
     const int internal = scan_counts(D.cnt, D.X, src_total);
     D.nodes = mem.tree_slots((long long)src_total + 2LL * internal);
     tree_nodes += internal;
-    scan_load<D4, true>(PrefixLoad{D}, D.P, src_total, mem.d4_scratch(src_total), st, &launches);
+    scan_load<I4, true>(PrefixLoad{D}, D.P, src_total, mem.prefix_scratch(src_total), st, &launches);
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
     k_record_key_order<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
     launches += 2;

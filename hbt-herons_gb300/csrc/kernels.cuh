@@ -99,7 +99,8 @@ struct DevState
   unsigned long long *key, *key_alt;
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
   int *cnt, *X, *flags, *F;
-  D4 *P;
+  I4 *P;          // fixed-point prefix sums of source mass and mass x offset (k_tree_emit)
+  unsigned *pmax; // [1] float bits of the largest |particle mass| of the call
   float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
   int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
@@ -135,12 +136,23 @@ __device__ __forceinline__ float source_mass(const DevState &D, int s, int p)
 // ---------------------------------------------------------------------------
 // Set-up
 // ---------------------------------------------------------------------------
+// Largest |mass| of the call (D.pmax, zeroed before the repack): bounds the
+// fixed-point prefix sums of the tree build.  Every thread of the block calls it.
+__device__ __forceinline__ void note_mass_bound(const DevState &D, unsigned mbits)
+{
+  mbits = __reduce_max_sync(0xffffffffu, mbits);
+  if ((threadIdx.x & 31) == 0 && mbits)
+    atomicMax(D.pmax, mbits);
+}
+
 __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, const float *__restrict__ vel,
                          const float *__restrict__ mass, const float *__restrict__ u, const uint8_t *__restrict__ type)
 {
+  unsigned mbits = 0u;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
   {
     D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
+    mbits = max(mbits, __float_as_uint(fabsf(mass[i])));
     D.vu[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], (K.thermal && u) ? u[i] : 0.f);
     int t = K.dm_only ? 1 : (type ? (int)type[i] : 1);
     t = t < 0 ? 0 : (t > 5 ? 5 : t);
@@ -152,6 +164,7 @@ __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, c
     D.ord[i] = (int)i;
     D.bnd[i] = 1;
   }
+  note_mass_bound(D, mbits);
 }
 
 __global__ void k_init_subs(DevState D, KParams K)
@@ -278,10 +291,12 @@ __global__ void k_bbox(DevState D, int total)
 }
 
 // Root cube (src/oct_tree.tpp:44-65): centre of the box, side = largest extent.
+// Built for every subhalo with sources: the active ones, and the converged
+// ones whose most-bound prefix gets its own tree (RefineBindingEnergyOrder).
 __global__ void k_root(DevState D, KParams K)
 {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= D.S || D.state[s] != kActive || D.src_cnt[s] == 0)
+  if (s >= D.S || D.src_cnt[s] == 0 || (D.state[s] != kActive && D.state[s] != kConverged))
     return;
   double lo[3], hi[3];
   for (int d = 0; d < 3; d++)
@@ -320,9 +335,38 @@ __global__ void k_root(DevState D, KParams K)
   for (double l = len; l >= (double)K.res && kstar < 1000; l *= 0.5)
     kstar++;
   kp[8] = __int_as_float(kstar);
+  // fixed-point scales of the prefix sums (PrefixLoad): 2^em per mass unit and
+  // 2^ex per mass x length unit.  The subhalo's source mass is below count x
+  // largest mass x largest upscale factor, and offsets from the float origin
+  // kp[0..2] are below side + |origin| 2^-23, so every partial sum of the
+  // subhalo stays below 2^61.
+  float fup = 1.f;
+  for (int t = 0; t < 6; t++)
+    fup = fmaxf(fup, D.factor[6 * s + t]);
+  const double mtot = (double)D.src_cnt[s] * (double)__uint_as_float(*D.pmax) * (double)fup;
+  double omax = 0.;
+  for (int d = 0; d < 3; d++)
+    omax = fmax(omax, fabs((double)kp[d]));
+  const double umax = len + omax * 0x1p-23;
+  int em = 61, ex = 61;
+  if (mtot > 0.)
+  {
+    int e;
+    frexp(mtot, &e); // mtot < 2^e
+    em = 61 - e;
+    ex = em;
+    if (umax > 0.)
+    {
+      frexp(mtot * umax, &e);
+      ex = 61 - e;
+    }
+  }
+  kp[9] = __int_as_float(em);
+  kp[10] = __int_as_float(ex);
+  kp[11] = (float)len;
   // first iteration: the sources are every particle (a warm start decides the
   // wrap from every particle before it starts)
-  if (D.iter[s] == 1 && !D.corr[s] && !(D.warm && D.warm[s] == 1))
+  if (D.state[s] == kActive && D.iter[s] == 1 && !D.corr[s] && !(D.warm && D.warm[s] == 1))
     D.wrap[s] = K.periodic && (len > (double)K.half);
 }
 
@@ -637,19 +681,41 @@ __global__ void k_tree_count(DevState D, int total)
   D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
 }
 
-// Item j of the double prefix sums of mass and mass-weighted offset from the
-// root centre (scanned by scan_load straight into D.P).
+// m x (x - o) in fixed point at scale 2^ex, from FP32 error-free
+// transforms: x - o = u + e exactly (Knuth's TwoSum), m u = p + pe exactly
+// (FMA), and m e, whose rounding is 2^-24 of a term 2^-24 below the rest.
+__device__ __forceinline__ unsigned long long fixed_moment(float m, float x, float o, int ex)
+{
+  const float u = __fsub_rn(x, o);
+  const float bv = __fsub_rn(u, x);
+  const float av = __fsub_rn(u, bv);
+  const float e = __fsub_rn(__fsub_rn(x, av), __fadd_rn(o, bv));
+  const float p = __fmul_rn(m, u);
+  const float pe = __fmaf_rn(m, u, -p);
+  const float q = __fmul_rn(m, e);
+  return (unsigned long long)__float2ll_rn(ldexpf(p, ex)) + (unsigned long long)__float2ll_rn(ldexpf(pe, ex)) +
+         (unsigned long long)__float2ll_rn(ldexpf(q, ex));
+}
+
+// Item j of the prefix sums behind the cell multipoles (scanned by scan_load
+// straight into D.P): the source mass and mass x offset from the root cube's
+// origin rounded to float (kp[0..2]), in 64-bit fixed point with the
+// subhalo's scales (k_root).  FP32 and integer arithmetic only (FP64
+// throughput is low on this GPU); the items are exact to the fixed-point grid
+// and the sums exact, so k_tree_emit rounds each centre of mass once.
 struct PrefixLoad
 {
   DevState D;
-  __device__ __forceinline__ D4 operator()(long long j) const
+  __device__ __forceinline__ I4 operator()(long long j) const
   {
     const int p = (int)D.val[j];
     const int s = D.seg_of[p];
-    const double *r = D.root + 4 * s;
+    const float *kp = D.keyp + 12 * s;
     const float4 x = D.pm[p];
-    const double m = source_mass(D, s, p);
-    return D4{m, m * ((double)x.x - r[0]), m * ((double)x.y - r[1]), m * ((double)x.z - r[2])};
+    const float m = fabsf(source_mass(D, s, p));
+    const int em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
+    return I4{(unsigned long long)__float2ll_rn(ldexpf(m, em)), fixed_moment(m, x.x, kp[0], ex),
+              fixed_moment(m, x.y, kp[1], ex), fixed_moment(m, x.z, kp[2], ex)};
   }
 };
 
@@ -672,10 +738,13 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(source_mass(D, s, p)));
   if (c == 0)
     return;
-  const double *r = D.root + 4 * s;
-  const int kstar = __float_as_int(D.keyp[12 * s + 8]);
+  const float *kp = D.keyp + 12 * s;
+  const int kstar = __float_as_int(kp[8]), em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
+  const float side = kp[11];
+  // 2^(em - ex) as a double (|em - ex| < 1000)
+  const double unit = __hiloint2double((1023 + em - ex) << 20, 0);
   const unsigned long long kj = D.key[j];
-  const D4 before = (j > 0) ? D.P[j - 1] : D4{0., 0., 0., 0.};
+  const I4 before = (j > 0) ? D.P[j - 1] : I4{0, 0, 0, 0};
   // Deepest cell first: a shallower cell ends at or after a deeper one, so
   // each search gallops forward from the previous cell's last item.
   int a = j; // key[a] shares the current prefix with item j
@@ -712,18 +781,28 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
       }
       b = a;
     }
-    const D4 after = D.P[b];
-    const double mass = after.m - before.m;
-    const double inv_m = 1.0 / mass;
-    const float lenf = (float)ldexp(r[3], -min(L, kstar));
+    const I4 after = D.P[b];
+    // cell mass and centre of mass (src/gravity_tree.cpp:50-80) from the
+    // exact sums, each rounded to float once: 1/M from the float reciprocal
+    // and one Newton step (relative error ~2^-46), then o + X/M in double
+    const long long qm = (long long)(after.m - before.m);
+    const float mass = ldexpf(__ll2float_rn(qm), -em);
+    const double M = (double)qm;
+    double inv = (double)__frcp_rn((float)qm);
+    inv = fma(inv, fma(-M, inv, 1.0), inv);
+    inv = qm > 0 ? inv * unit : 0.;
+    const long long qx[3] = {(long long)(after.x - before.x), (long long)(after.y - before.y),
+                             (long long)(after.z - before.z)};
+    float c[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+      c[d] = (float)fma((double)qx[d], inv, (double)kp[d]);
+    const float lenf = ldexpf(side, -min(L, kstar));
     const float len2 = lenf * lenf;
     const float crit = __fdiv_rn(len2, K.theta2);
     const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
-    D.nodes[base + 2 * t] = make_float4((float)(r[0] + (after.x - before.x) * inv_m),
-                                        (float)(r[1] + (after.y - before.y) * inv_m),
-                                        (float)(r[2] + (after.z - before.z) * inv_m),
-                                        __uint_as_float(__float_as_uint(crit) | 0x80000000u));
-    D.nodes[base + 2 * t + 1] = make_float4((float)mass, __int_as_float(skip), 0.f, 0.f);
+    D.nodes[base + 2 * t] = make_float4(c[0], c[1], c[2], __uint_as_float(__float_as_uint(crit) | 0x80000000u));
+    D.nodes[base + 2 * t + 1] = make_float4(mass, __int_as_float(skip), 0.f, 0.f);
   }
 }
 
@@ -1064,6 +1143,9 @@ __global__ void k_plan_refine(DevState D, KParams K)
   D.ngrav[s] = 0;
   for (int t = 0; t < 6; t++)
     D.factor[6 * s + t] = 1.f;
+  // a fresh bounding box for the prefix's own tree (k_bbox, k_root)
+  D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
+  D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
 }
 
 __global__ void k_refine_keys(DevState D, KParams K, int total)

@@ -52,7 +52,7 @@ constexpr size_t kN1 = (size_t)kNoAllocMaxParticles + 1;
 constexpr size_t kS1 = (size_t)kNoAllocMaxSubhaloes + 1;
 constexpr size_t kTable = (size_t)256 * ((kNoAllocMaxParticles + kRadixTile - 1) / kRadixTile);
 constexpr size_t kScanScr = 2 * (kN1 + kTable) / 64 + 4096; // > scan_scratch_elems<int> of any scan here
-constexpr size_t kD4Scr = 2 * kN1 / 256 + 256;              // > scan_scratch_elems<D4>(N)
+constexpr size_t kPScr = 2 * kN1 / 256 + 256;               // > scan_scratch_elems<I4>(N)
 constexpr size_t kScratchBytes =
   al(sizeof(long long) * kS1) +              // offsets
   2 * al(sizeof(float4) * kN1) +             // pm, vu
@@ -72,11 +72,11 @@ constexpr size_t kScratchBytes =
   6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
   al(sizeof(int) * kN1) + al(sizeof(int)) +  // key fallback list and its count
   4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
-  al(sizeof(D4) * kN1) +                     // prefix sums
+  al(sizeof(I4) * kN1) + al(sizeof(unsigned)) + // prefix sums, largest mass
   al(sizeof(float4) * kNoAllocMaxRecords) +  // tree slots
   al(sizeof(int) * kTable) +                 // radix table
   al(sizeof(int) * kScanScr) +               // scan scratch
-  al(sizeof(D4) * kD4Scr) +                  // D4 scan scratch
+  al(sizeof(I4) * kPScr) +                   // prefix-sum scan scratch
   al(sizeof(unsigned long long));            // interaction counter
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -147,7 +147,7 @@ inline unsigned nblocks(long long n, int threads)
 struct StaticMem
 {
   int *scan_scr = nullptr, *table = nullptr;
-  D4 *d4_scr = nullptr;
+  I4 *p_scr = nullptr;
   float4 *slots = nullptr;
 
   void check(cudaError_t e) { ck(e); }
@@ -164,11 +164,11 @@ struct StaticMem
     return table;
   }
   int *radix_scan_scratch(long long n) { return scan_scratch(radix_table_elems(std::max<long long>(n, 1)) + 1); }
-  D4 *d4_scratch(long long n)
+  I4 *prefix_scratch(long long n)
   {
-    if (scan_scratch_elems<D4>(n) > kD4Scr)
+    if (scan_scratch_elems<I4>(n) > kPScr)
       throw Fail{HBTG_ERR_NOMEM};
-    return d4_scr;
+    return p_scr;
   }
   float4 *tree_slots(long long n)
   {
@@ -302,15 +302,16 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.X = c.take<int>(kN1);
   D.flags = c.take<int>(kN1);
   D.F = c.take<int>(kN1);
-  D.P = c.take<D4>(kN1);
+  D.P = c.take<I4>(kN1);
+  D.pmax = c.take<unsigned>(1);
   mem.slots = c.take<float4>(kNoAllocMaxRecords);
   D.nodes = mem.slots;
   mem.table = c.take<int>(kTable);
   mem.scan_scr = c.take<int>(kScanScr);
-  mem.d4_scr = c.take<D4>(kD4Scr);
+  mem.p_scr = c.take<I4>(kPScr);
   D.interactions = c.take<unsigned long long>(1);
   if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr ||
-      (size_t)scan_scratch_elems<D4>(kN1) > kD4Scr)
+      (size_t)scan_scratch_elems<I4>(kN1) > kPScr)
     return HBTG_ERR_NOMEM; // layout does not fit the reserve (cannot happen with the constants above)
   D.ref_pos = b->ref_pos;
   D.ref_vel = b->ref_vel;
@@ -323,6 +324,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   {
     ck(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
     ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+    ck(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
     if (N > 0)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
     k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D, R.K);

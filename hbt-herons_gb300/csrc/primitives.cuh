@@ -17,8 +17,7 @@ namespace hbtg
 
 constexpr int kScanThreads = 256;
 
-// Items per thread of a scan tile: 8 for 4/8-byte types, 4 for D4 (keeps the
-// tile in 32 KB of shared memory).
+// Rows per warp of a scan tile: 8 for 4/8-byte types, 4 for 32-byte I4.
 template <typename T>
 __host__ __device__ constexpr int scan_items()
 {
@@ -30,10 +29,13 @@ __host__ __device__ constexpr int scan_tile()
   return kScanThreads * scan_items<T>();
 }
 
-struct D4
+// Four 64-bit fixed-point sums, modulo 2^64 (exact, so any summation order
+// gives the same result; a difference of two prefixes is exact whenever the
+// true difference fits in 63 bits).
+struct I4
 {
-  double m, x, y, z;
-  __host__ __device__ D4 operator+(const D4 &o) const { return D4{m + o.m, x + o.x, y + o.y, z + o.z}; }
+  unsigned long long m, x, y, z;
+  __host__ __device__ I4 operator+(const I4 &o) const { return I4{m + o.m, x + o.x, y + o.y, z + o.z}; }
 };
 
 template <typename T>
@@ -43,7 +45,7 @@ __device__ __forceinline__ int zero_of<int>() { return 0; }
 template <>
 __device__ __forceinline__ long long zero_of<long long>() { return 0; }
 template <>
-__device__ __forceinline__ D4 zero_of<D4>() { return D4{0., 0., 0., 0.}; }
+__device__ __forceinline__ I4 zero_of<I4>() { return I4{0, 0, 0, 0}; }
 
 template <typename T>
 __device__ __forceinline__ T shfl_up(T v, int d)
@@ -51,9 +53,9 @@ __device__ __forceinline__ T shfl_up(T v, int d)
   return __shfl_up_sync(0xffffffffu, v, d);
 }
 template <>
-__device__ __forceinline__ D4 shfl_up<D4>(D4 v, int d)
+__device__ __forceinline__ I4 shfl_up<I4>(I4 v, int d)
 {
-  return D4{__shfl_up_sync(0xffffffffu, v.m, d), __shfl_up_sync(0xffffffffu, v.x, d),
+  return I4{__shfl_up_sync(0xffffffffu, v.m, d), __shfl_up_sync(0xffffffffu, v.x, d),
             __shfl_up_sync(0xffffffffu, v.y, d), __shfl_up_sync(0xffffffffu, v.z, d)};
 }
 
@@ -63,9 +65,9 @@ __device__ __forceinline__ T shfl_idx(T v, int src)
   return __shfl_sync(0xffffffffu, v, src);
 }
 template <>
-__device__ __forceinline__ D4 shfl_idx<D4>(D4 v, int src)
+__device__ __forceinline__ I4 shfl_idx<I4>(I4 v, int src)
 {
-  return D4{__shfl_sync(0xffffffffu, v.m, src), __shfl_sync(0xffffffffu, v.x, src),
+  return I4{__shfl_sync(0xffffffffu, v.m, src), __shfl_sync(0xffffffffu, v.x, src),
             __shfl_sync(0xffffffffu, v.y, src), __shfl_sync(0xffffffffu, v.z, src)};
 }
 
@@ -143,7 +145,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(Load load, T *out, 
     const T inc = warp_inclusive_scan(x, lane);
     T part = inc;
     if (!Inclusive)
-    { // exclusive = the previous lane's inclusive value (no subtraction: exact for doubles)
+    { // exclusive = the previous lane's inclusive value
       part = shfl_up(inc, 1);
       if (lane == 0)
         part = zero_of<T>();

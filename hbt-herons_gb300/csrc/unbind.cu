@@ -29,14 +29,17 @@ namespace
 {
 __global__ void k_pot_repack(DevState D, const float *__restrict__ pos, const float *__restrict__ mass)
 {
+  unsigned mbits = 0u;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
   {
     D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
+    mbits = max(mbits, __float_as_uint(fabsf(mass[i])));
     D.vu[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     D.ty[i] = 1;
     D.seg_of[i] = 0;
     D.ord[i] = (int)i;
   }
+  note_mass_bound(D, mbits);
 }
 
 // One "subhalo" whose every particle is a source; the walk takes the
@@ -132,9 +135,9 @@ enum Slot
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_D4SCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
+  S_NODES, S_TABLE, S_SCRATCH, S_PSCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
-  S_POTI, S_WCTR,
+  S_POTI, S_WCTR, S_PMAX,
   S_NUM
 };
 
@@ -309,7 +312,10 @@ struct PoolMem
                                          std::max<long long>(radix_table_elems(std::max<long long>(n, 1)) + 1,
                                                              256LL * 4096)));
   }
-  D4 *d4_scratch(long long n) { return H->pool.get<D4>(S_D4SCR, scan_scratch_elems<D4>(std::max<long long>(n, 1))); }
+  I4 *prefix_scratch(long long n)
+  {
+    return H->pool.get<I4>(S_PSCR, scan_scratch_elems<I4>(std::max<long long>(n, 1)));
+  }
   float4 *tree_slots(long long slots)
   {
     if (slots >= (1LL << 31) - 64)
@@ -435,10 +441,12 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.X = P.get<int>(S_X, n1 + 1);
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
   D.F = P.get<int>(S_F, n1 + 1);
-  D.P = P.get<D4>(S_P, n1);
+  D.P = P.get<I4>(S_P, n1);
+  D.pmax = P.get<unsigned>(S_PMAX, 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+  HBTG_CUDA(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
 
   if (N > 0)
   {
@@ -787,11 +795,13 @@ int pot_call(void *arg)
   D.fb_count = P.get<int>(S_FBC, 1);
   D.cnt = P.get<int>(S_CNT, n1 + 1);
   D.X = P.get<int>(S_X, n1 + 1);
-  D.P = P.get<D4>(S_P, n1);
+  D.P = P.get<I4>(S_P, n1);
+  D.pmax = P.get<unsigned>(S_PMAX, 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));
   HBTG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
+  HBTG_CUDA(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
   k_pot_repack<<<blocks_for(c.ns, 256), 256, 0, st>>>(D, c.pos, c.mass);
   k_pot_plan<<<1, 32, 0, st>>>(D, (int)c.nt, 0);
   R.check();
