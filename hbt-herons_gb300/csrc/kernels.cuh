@@ -719,6 +719,31 @@ struct PrefixLoad
   }
 };
 
+// v = hi + lo with hi = v rounded to float and lo the remainder rounded to
+// float (relative precision ~2^-48).
+__device__ __forceinline__ void ll_to_float2(long long v, float &hi, float &lo)
+{
+  hi = __ll2float_rn(v);
+  lo = __ll2float_rn(v - __float2ll_rn(hi));
+}
+
+// o + X/M rounded to float once, in FP32 arithmetic (float-float quotient,
+// then Knuth's TwoSum with the origin); X, M given as float-float pairs and
+// scale = 2^(em - ex).
+__device__ __forceinline__ float centre_coord(float o, float xh, float xl, float mh, float ml, float scale)
+{
+  const float q1 = __fdiv_rn(xh, mh);
+  const float ph = __fmul_rn(q1, mh);
+  const float pl = __fmaf_rn(q1, mh, -ph); // q1 mh = ph + pl exactly
+  const float r = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(xh, ph), pl), xl), __fmul_rn(q1, ml));
+  const float q2 = __fdiv_rn(r, mh);
+  const float a = __fmul_rn(q1, scale), b = __fmul_rn(q2, scale);
+  const float s = __fadd_rn(o, a);
+  const float bv = __fsub_rn(s, o);
+  const float e = __fadd_rn(__fsub_rn(o, __fsub_rn(s, bv)), __fsub_rn(a, bv)); // o + a = s + e exactly
+  return __fadd_rn(s, __fadd_rn(e, b));
+}
+
 // Writes the particle leaf and the cells that start at item j, in preorder.
 // Slot index: cell (j, level lo+t) = j + 2 X[j] + 2t; leaf of item j =
 // j + 2 X[j] + 2 cnt[j].  A cell's subtree ends after its last particle's leaf.
@@ -741,8 +766,7 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   const float *kp = D.keyp + 12 * s;
   const int kstar = __float_as_int(kp[8]), em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
   const float side = kp[11];
-  // 2^(em - ex) as a double (|em - ex| < 1000)
-  const double unit = __hiloint2double((1023 + em - ex) << 20, 0);
+  const float unit = ldexpf(1.f, em - ex);
   const unsigned long long kj = D.key[j];
   const I4 before = (j > 0) ? D.P[j - 1] : I4{0, 0, 0, 0};
   // Deepest cell first: a shallower cell ends at or after a deeper one, so
@@ -783,20 +807,21 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
     }
     const I4 after = D.P[b];
     // cell mass and centre of mass (src/gravity_tree.cpp:50-80) from the
-    // exact sums, each rounded to float once: 1/M from the float reciprocal
-    // and one Newton step (relative error ~2^-46), then o + X/M in double
+    // exact sums, each rounded to float once, in FP32 arithmetic
     const long long qm = (long long)(after.m - before.m);
     const float mass = ldexpf(__ll2float_rn(qm), -em);
-    const double M = (double)qm;
-    double inv = (double)__frcp_rn((float)qm);
-    inv = fma(inv, fma(-M, inv, 1.0), inv);
-    inv = qm > 0 ? inv * unit : 0.;
+    float mh, ml;
+    ll_to_float2(qm, mh, ml);
     const long long qx[3] = {(long long)(after.x - before.x), (long long)(after.y - before.y),
                              (long long)(after.z - before.z)};
     float c[3];
 #pragma unroll
     for (int d = 0; d < 3; d++)
-      c[d] = (float)fma((double)qx[d], inv, (double)kp[d]);
+    {
+      float xh, xl;
+      ll_to_float2(qx[d], xh, xl);
+      c[d] = qm > 0 ? centre_coord(kp[d], xh, xl, mh, ml, unit) : kp[d];
+    }
     const float lenf = ldexpf(side, -min(L, kstar));
     const float len2 = lenf * lenf;
     const float crit = __fdiv_rn(len2, K.theta2);
