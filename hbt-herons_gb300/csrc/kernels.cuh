@@ -681,6 +681,52 @@ __global__ void k_tree_count(DevState D, int total)
   D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
 }
 
+// 64-bit integer <-> float conversions by exponent and mantissa arithmetic
+// (the hardware's 64-bit conversions issue to the FP64 pipe, whose
+// throughput is low on this GPU).
+
+// Nearest integer to f (ties to even), |f| < 2^62.
+__device__ __forceinline__ long long float_to_ll_rn(float f)
+{
+  const unsigned b = __float_as_uint(f);
+  const int e = (int)((b >> 23) & 0xffu) - 127;
+  if (e < 31)
+    return (long long)__float2int_rn(f);
+  const long long v = (long long)((b & 0x7fffffu) | 0x800000u) << (e - 23);
+  return (b >> 31) ? -v : v;
+}
+
+// v = hi + lo: hi is v rounded to float (to nearest even), lo the remainder
+// rounded to float.  |v| < 2^63.
+__device__ __forceinline__ void ll_to_float2(long long v, float &hi, float &lo)
+{
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  float h, l = 0.f;
+  if (a < (1ull << 24))
+    h = __uint2float_rn((unsigned)a);
+  else
+  {
+    const int e = 63 - __clzll((long long)a);
+    const int sh = e - 23;
+    unsigned long long mant = a >> sh;
+    const unsigned long long rem = a & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    long long r = (long long)rem;
+    if (rem > half || (rem == half && (mant & 1ull)))
+    {
+      mant++;
+      r -= (long long)(1ull << sh);
+    }
+    // a mantissa carried to 2^24 steps the exponent field by itself
+    h = __uint_as_float((unsigned)((e + 127) << 23) + (unsigned)(mant - (1ull << 23)));
+    const unsigned long long ar = r < 0 ? 0ull - (unsigned long long)r : (unsigned long long)r; // < 2^39
+    l = __fmaf_rn(__uint2float_rn((unsigned)(ar >> 16)), 65536.f, __uint2float_rn((unsigned)(ar & 0xffffu)));
+    if (r < 0)
+      l = -l;
+  }
+  hi = v < 0 ? -h : h;
+  lo = v < 0 ? -l : l;
+}
+
 // m x (x - o) in fixed point at scale 2^ex, from FP32 error-free
 // transforms: x - o = u + e exactly (Knuth's TwoSum), m u = p + pe exactly
 // (FMA), and m e, whose rounding is 2^-24 of a term 2^-24 below the rest.
@@ -693,8 +739,8 @@ __device__ __forceinline__ unsigned long long fixed_moment(float m, float x, flo
   const float p = __fmul_rn(m, u);
   const float pe = __fmaf_rn(m, u, -p);
   const float q = __fmul_rn(m, e);
-  return (unsigned long long)__float2ll_rn(ldexpf(p, ex)) + (unsigned long long)__float2ll_rn(ldexpf(pe, ex)) +
-         (unsigned long long)__float2ll_rn(ldexpf(q, ex));
+  return (unsigned long long)float_to_ll_rn(ldexpf(p, ex)) + (unsigned long long)float_to_ll_rn(ldexpf(pe, ex)) +
+         (unsigned long long)float_to_ll_rn(ldexpf(q, ex));
 }
 
 // Item j of the prefix sums behind the cell multipoles (scanned by scan_load
@@ -714,18 +760,10 @@ struct PrefixLoad
     const float4 x = D.pm[p];
     const float m = fabsf(source_mass(D, s, p));
     const int em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
-    return I4{(unsigned long long)__float2ll_rn(ldexpf(m, em)), fixed_moment(m, x.x, kp[0], ex),
+    return I4{(unsigned long long)float_to_ll_rn(ldexpf(m, em)), fixed_moment(m, x.x, kp[0], ex),
               fixed_moment(m, x.y, kp[1], ex), fixed_moment(m, x.z, kp[2], ex)};
   }
 };
-
-// v = hi + lo with hi = v rounded to float and lo the remainder rounded to
-// float (relative precision ~2^-48).
-__device__ __forceinline__ void ll_to_float2(long long v, float &hi, float &lo)
-{
-  hi = __ll2float_rn(v);
-  lo = __ll2float_rn(v - __float2ll_rn(hi));
-}
 
 // o + X/M rounded to float once, in FP32 arithmetic (float-float quotient,
 // then Knuth's TwoSum with the origin); X, M given as float-float pairs and
@@ -744,90 +782,117 @@ __device__ __forceinline__ float centre_coord(float o, float xh, float xl, float
   return __fadd_rn(s, __fadd_rn(e, b));
 }
 
-// Writes the particle leaf and the cells that start at item j, in preorder.
-// Slot index: cell (j, level lo+t) = j + 2 X[j] + 2t; leaf of item j =
-// j + 2 X[j] + 2 cnt[j].  A cell's subtree ends after its last particle's leaf.
-__global__ void k_tree_emit(DevState D, KParams K, int total)
+// One cell: item j's cell at level L (slot `slot`), in segment s ending at
+// seg_end.  Its last item b is found by galloping forward from j over the
+// keys; mass and centre of mass come from the prefix sums over [j, b]
+// (src/gravity_tree.cpp:50-80), each rounded to float once, in FP32.
+__device__ __forceinline__ void emit_cell(const DevState &D, const KParams &K, int j, int s, int seg_end, int L,
+                                          int slot)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= total)
-    return;
-  const int s = find_segment<int>(D.src_off, D.S, j);
-  const int seg0 = D.src_off[s], i = j - seg0, m = D.src_cnt[s], seg_end = seg0 + m;
-  int lo, hi;
-  cell_levels(D, j, i, m, lo, hi);
-  const int c = hi >= lo ? hi - lo + 1 : 0;
-  const int base = j + 2 * D.X[j];
-  const int p = (int)D.val[j];
-  const float4 x = D.pm[p];
-  D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(source_mass(D, s, p)));
-  if (c == 0)
-    return;
+  int b;
+  if (L == 0)
+    b = seg_end - 1;
+  else
+  {
+    const int shift = 63 - 3 * L;
+    const unsigned long long pref = D.key[j] >> shift;
+    int a = j, e, step = 1; // key[a] has the prefix
+    for (;;)
+    {
+      const int probe = a + step;
+      if (probe >= seg_end || (D.key[probe] >> shift) != pref)
+      {
+        e = min(probe, seg_end);
+        break;
+      }
+      a = probe;
+      step <<= 1;
+    }
+    while (e - a > 1) // answer in [a, e)
+    {
+      const int mid = (a + e) >> 1;
+      if ((D.key[mid] >> shift) == pref)
+        a = mid;
+      else
+        e = mid;
+    }
+    b = a;
+  }
   const float *kp = D.keyp + 12 * s;
   const int kstar = __float_as_int(kp[8]), em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
-  const float side = kp[11];
-  const float unit = ldexpf(1.f, em - ex);
-  const unsigned long long kj = D.key[j];
   const I4 before = (j > 0) ? D.P[j - 1] : I4{0, 0, 0, 0};
-  // Deepest cell first: a shallower cell ends at or after a deeper one, so
-  // each search gallops forward from the previous cell's last item.
-  int a = j; // key[a] shares the current prefix with item j
-  for (int t = c - 1; t >= 0; t--)
-  {
-    const int L = lo + t;
-    // last item whose first L digits equal those of item j
-    int b;
-    if (L == 0)
-      b = seg_end - 1;
-    else
-    {
-      const int shift = 63 - 3 * L;
-      const unsigned long long pref = kj >> shift;
-      int e, step = 1;
-      for (;;)
-      {
-        const int probe = a + step;
-        if (probe >= seg_end || (D.key[probe] >> shift) != pref)
-        {
-          e = min(probe, seg_end);
-          break;
-        }
-        a = probe;
-        step <<= 1;
-      }
-      while (e - a > 1) // key[a] has the prefix; answer in [a, e)
-      {
-        const int mid = (a + e) >> 1;
-        if ((D.key[mid] >> shift) == pref)
-          a = mid;
-        else
-          e = mid;
-      }
-      b = a;
-    }
-    const I4 after = D.P[b];
-    // cell mass and centre of mass (src/gravity_tree.cpp:50-80) from the
-    // exact sums, each rounded to float once, in FP32 arithmetic
-    const long long qm = (long long)(after.m - before.m);
-    const float mass = ldexpf(__ll2float_rn(qm), -em);
-    float mh, ml;
-    ll_to_float2(qm, mh, ml);
-    const long long qx[3] = {(long long)(after.x - before.x), (long long)(after.y - before.y),
-                             (long long)(after.z - before.z)};
-    float c[3];
+  const I4 after = D.P[b];
+  const long long qm = (long long)(after.m - before.m);
+  float mh, ml;
+  ll_to_float2(qm, mh, ml);
+  const float mass = ldexpf(mh, -em);
+  const float unit = ldexpf(1.f, em - ex);
+  const long long qx[3] = {(long long)(after.x - before.x), (long long)(after.y - before.y),
+                           (long long)(after.z - before.z)};
+  float c[3];
 #pragma unroll
-    for (int d = 0; d < 3; d++)
+  for (int d = 0; d < 3; d++)
+  {
+    float xh, xl;
+    ll_to_float2(qx[d], xh, xl);
+    c[d] = qm > 0 ? centre_coord(kp[d], xh, xl, mh, ml, unit) : kp[d];
+  }
+  const float lenf = ldexpf(kp[11], -min(L, kstar));
+  const float crit = __fdiv_rn(lenf * lenf, K.theta2);
+  const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
+  D.nodes[slot] = make_float4(c[0], c[1], c[2], __uint_as_float(__float_as_uint(crit) | 0x80000000u));
+  D.nodes[slot + 1] = make_float4(mass, __int_as_float(skip), 0.f, 0.f);
+}
+
+// Writes the tree slots in preorder.  Slot index: cell (j, level lo+t) =
+// j + 2 X[j] + 2t; leaf of item j = j + 2 X[j] + 2 cnt[j].  A cell's subtree
+// ends after its last particle's leaf.  Each thread writes its item's leaf;
+// the warp then gathers the cells of its 32 items into one list (a shuffle
+// scan of their counts) and emits them one per lane, so items with many
+// cells do not hold the other lanes.
+__global__ void k_tree_emit(DevState D, KParams K, int total)
+{
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = 0, lo = 0, c = 0, seg_end = 0, base = 0;
+  if (j < total)
+  {
+    s = find_segment<int>(D.src_off, D.S, j);
+    const int seg0 = D.src_off[s], m = D.src_cnt[s];
+    seg_end = seg0 + m;
+    int hi;
+    cell_levels(D, j, j - seg0, m, lo, hi);
+    c = hi >= lo ? hi - lo + 1 : 0;
+    base = j + 2 * D.X[j];
+    const int p = (int)D.val[j];
+    const float4 x = D.pm[p];
+    D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(source_mass(D, s, p)));
+  }
+  int incl = c; // inclusive scan of the cell counts over the warp
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1)
+  {
+    const int o = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d)
+      incl += o;
+  }
+  const int cells = __shfl_sync(0xffffffffu, incl, 31);
+  for (int q0 = 0; q0 < cells; q0 += 32)
+  {
+    const int q = q0 + lane;
+    int owner = 0; // first lane whose inclusive count exceeds q
+#pragma unroll
+    for (int w = 16; w > 0; w >>= 1)
+      if (__shfl_sync(0xffffffffu, incl, owner + w - 1) <= q)
+        owner += w;
+    const int o_incl = __shfl_sync(0xffffffffu, incl, owner), o_c = __shfl_sync(0xffffffffu, c, owner);
+    const int o_s = __shfl_sync(0xffffffffu, s, owner), o_lo = __shfl_sync(0xffffffffu, lo, owner);
+    const int o_end = __shfl_sync(0xffffffffu, seg_end, owner), o_base = __shfl_sync(0xffffffffu, base, owner);
+    if (q < cells)
     {
-      float xh, xl;
-      ll_to_float2(qx[d], xh, xl);
-      c[d] = qm > 0 ? centre_coord(kp[d], xh, xl, mh, ml, unit) : kp[d];
+      const int t = q - (o_incl - o_c);
+      emit_cell(D, K, j - lane + owner, o_s, o_end, o_lo + t, o_base + 2 * t);
     }
-    const float lenf = ldexpf(side, -min(L, kstar));
-    const float len2 = lenf * lenf;
-    const float crit = __fdiv_rn(len2, K.theta2);
-    const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
-    D.nodes[base + 2 * t] = make_float4(c[0], c[1], c[2], __uint_as_float(__float_as_uint(crit) | 0x80000000u));
-    D.nodes[base + 2 * t + 1] = make_float4(mass, __int_as_float(skip), 0.f, 0.f);
   }
 }
 
@@ -1023,7 +1088,7 @@ __global__ void k_energy(DevState D, KParams K, int total)
     const float ovl[3] = {D.old_vel[3 * s], D.old_vel[3 * s + 1], D.old_vel[3 * s + 2]};
     rel_vel(make_float3(op[0], op[1], op[2]), make_float3(ovl[0], ovl[1], ovl[2]), D.ref_pos + 3 * s,
             D.ref_vel + 3 * s, K, dV);
-    const float dK = (float)(0.5 * (double)norm2_rn(dV));
+    const float dK = __fmul_rn(0.5f, norm2_rn(dV)); // halving is exact
     rel_vel(x3, v3, op, ovl, K, ov);
     const float dot = __fadd_rn(__fadd_rn(__fmul_rn(ov[0], dV[0]), __fmul_rn(ov[1], dV[1])), __fmul_rn(ov[2], dV[2]));
     D.Ep[p] = __fadd_rn(D.Ep[p], __fsub_rn(__fadd_rn(dot, dK), D.pot[p]));
