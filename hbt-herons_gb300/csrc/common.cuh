@@ -37,6 +37,43 @@ __device__ __forceinline__ int find_segment(const T *__restrict__ off, int n, T 
   return lo;
 }
 
+// find_segment for a warp whose 32 lanes all call it with non-decreasing
+// indices: a 32-ary search for the first and the last lane's segment (each
+// step probes 32 evenly spaced offsets at once and counts them with a
+// ballot), then each lane searches only between those two segments.
+__device__ __forceinline__ int find_segment_32ary(const int *__restrict__ off, int lo, int hi, int target)
+{
+  const int lane = threadIdx.x & 31;
+  while (hi - lo > 1) // off[lo] <= target; answer in [lo, hi)
+  {
+    const int step = (hi - lo + 31) >> 5;
+    const int pos = lo + (lane + 1) * step;
+    const bool ok = pos < hi && __ldg(off + pos) <= target;
+    const int c = __popc(__ballot_sync(0xffffffffu, ok));
+    const int nlo = lo + c * step;
+    hi = min(hi, nlo + step);
+    lo = nlo;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int find_segment_warp(const int *__restrict__ off, int n, int idx)
+{
+  const int first = __shfl_sync(0xffffffffu, idx, 0), last = __shfl_sync(0xffffffffu, idx, 31);
+  const int s0 = find_segment_32ary(off, 0, n, first);
+  const int s1 = (last == first) ? s0 : find_segment_32ary(off, s0, n, last);
+  int lo = s0, hi = s1 + 1;
+  while (hi - lo > 1)
+  {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= idx)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
 // Reference NEAREST macro (src/config_parser.h:218-219) in float.
 __device__ __forceinline__ float nearest_f(float x, float half, float box)
 {

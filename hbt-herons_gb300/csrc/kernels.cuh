@@ -264,7 +264,8 @@ __global__ void k_bbox(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = j < total;
-  const int s = valid ? find_segment<int>(D.src_off, D.S, j) : -1;
+  const int sw = find_segment_warp(D.src_off, D.S, min(j, total - 1));
+  const int s = valid ? sw : -1;
   unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   if (valid)
   {
@@ -448,9 +449,9 @@ __global__ void k_keys(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j < total)
   {
-    const int s = find_segment<int>(D.src_off, D.S, j);
     const int p = src_particle(D, s, j);
     unsigned long long key;
     need = !descent_key_fast(D.pm[p], D.keyp + 12 * s, key);
@@ -520,9 +521,9 @@ __global__ void k_segkeys(const uint32_t *__restrict__ val, const int *__restric
 __global__ void k_record_key_order(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.src_off, D.S, j);
   if (!D.corr[s] && !D.ngrav[s])
     D.sp[D.off[s] + (j - D.src_off[s])] = (int)D.val[j];
 }
@@ -532,9 +533,9 @@ __global__ void k_record_key_order(DevState D, int total)
 __global__ void k_record_candidates(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.part_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.part_off, D.S, j);
   if (!D.corr[s] && D.ngrav[s])
   {
     const long long g = D.off[s] + (j - D.part_off[s]);
@@ -631,6 +632,7 @@ __global__ void __launch_bounds__(256) k_upscale(DevState D, KParams K)
 __global__ void k_tgt_flags(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.sp_off, D.S, min(j, total - 1));
   if (j > total)
     return;
   if (j == total)
@@ -638,16 +640,15 @@ __global__ void k_tgt_flags(DevState D, int total)
     D.flags[j] = 0;
     return;
   }
-  const int s = find_segment<int>(D.sp_off, D.S, j);
   D.flags[j] = D.bnd[D.sp[D.off[s] + (j - D.sp_off[s])]];
 }
 
 __global__ void k_tgt_scatter(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.sp_off, D.S, min(j, total - 1));
   if (j >= total || !D.flags[j])
     return;
-  const int s = find_segment<int>(D.sp_off, D.S, j);
   D.tgt[D.off[s] + (D.F[j] - D.F[D.sp_off[s]])] = D.sp[D.off[s] + (j - D.sp_off[s])];
 }
 
@@ -667,6 +668,7 @@ __device__ __forceinline__ void cell_levels(const DevState &D, int j, int i, int
 __global__ void k_tree_count(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j > total)
     return;
   if (j == total)
@@ -674,7 +676,6 @@ __global__ void k_tree_count(DevState D, int total)
     D.cnt[j] = 0;
     return;
   }
-  const int s = find_segment<int>(D.src_off, D.S, j);
   const int i = j - D.src_off[s], m = D.src_cnt[s];
   int lo, hi;
   cell_levels(D, j, i, m, lo, hi);
@@ -854,10 +855,10 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
 {
   const int lane = threadIdx.x & 31;
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = 0, lo = 0, c = 0, seg_end = 0, base = 0;
+  int lo = 0, c = 0, seg_end = 0, base = 0;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j < total)
   {
-    s = find_segment<int>(D.src_off, D.S, j);
     const int seg0 = D.src_off[s], m = D.src_cnt[s];
     seg_end = seg0 + m;
     int hi;
@@ -968,7 +969,7 @@ template <bool Count>
 __device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, int c, int lane,
                                            unsigned long long &cnt)
 {
-  const int s = find_segment<int>(D.chunk_off, D.S, c);
+  const int s = find_segment_warp(D.chunk_off, D.S, c); // c is the same on every lane
   const int t = (c - D.chunk_off[s]) * kWarp + lane;
   const bool valid = t < D.tgt_cnt[s];
   const bool corr = D.corr[s] != 0;
@@ -1065,9 +1066,9 @@ __device__ __forceinline__ float norm2_rn(const float *d)
 __global__ void k_energy(DevState D, KParams K, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.part_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.part_off, D.S, j);
   const int k = j - D.part_off[s];
   const int p = D.ord[D.off[s] + k];
   const float4 x = D.pm[p], v = D.vu[p];
@@ -1098,6 +1099,7 @@ __global__ void k_energy(DevState D, KParams K, int total)
 __global__ void k_part_flags(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.part_off, D.S, min(j, total - 1));
   if (j > total)
     return;
   if (j == total)
@@ -1105,7 +1107,6 @@ __global__ void k_part_flags(DevState D, int total)
     D.flags[j] = 0;
     return;
   }
-  const int s = find_segment<int>(D.part_off, D.S, j);
   const int k = j - D.part_off[s];
   D.flags[j] = D.Ep[D.ord[D.off[s] + k]] < 0.f ? 1 : 0;
 }
@@ -1123,10 +1124,11 @@ __global__ void k_part_scatter(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = j < total;
-  int s = -1, tracer = 0;
+  int s = find_segment_warp(D.part_off, D.S, min(j, total - 1)), tracer = 0;
+  if (!valid)
+    s = -1;
   if (valid)
   {
-    s = find_segment<int>(D.part_off, D.S, j);
     const int k = j - D.part_off[s];
     const int rb = D.F[j] - D.F[D.part_off[s]];
     const bool bound = D.flags[j] != 0;
@@ -1145,9 +1147,9 @@ __global__ void k_part_scatter(DevState D, int total)
 __global__ void k_part_copy(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.part_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.part_off, D.S, j);
   const long long g = D.off[s] + (j - D.part_off[s]);
   D.ord[g] = D.ord_tmp[g];
 }
@@ -1254,9 +1256,9 @@ __global__ void k_refine_keys(DevState D, KParams K, int total)
 __global__ void k_refine_write(DevState D, const uint32_t *__restrict__ sorted_val, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.src_off, D.S, j);
   D.ord[D.off[s] + (j - D.src_off[s])] = (int)sorted_val[j];
 }
 
@@ -1265,9 +1267,9 @@ __global__ void k_refine_write(DevState D, const uint32_t *__restrict__ sorted_v
 __global__ void k_energy_keys(DevState D, const int *__restrict__ offs, int total, int mode)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(offs, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(offs, D.S, j);
   const int k = (mode == 0 ? D.nbound[s] : 0) + (j - offs[s]);
   const int p = D.ord[D.off[s] + k];
   D.k32[j] = float_to_ordered(D.Ep[p]);
@@ -1278,9 +1280,9 @@ __global__ void k_energy_write(DevState D, const uint32_t *__restrict__ sorted_v
                                int total, int mode)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(offs, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(offs, D.S, j);
   const int k = (mode == 0 ? D.nbound[s] : 0) + (j - offs[s]);
   D.ord[D.off[s] + k] = (int)sorted_val[j];
 }

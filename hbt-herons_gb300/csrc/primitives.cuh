@@ -238,95 +238,98 @@ __global__ void __launch_bounds__(kRadixThreads) k_radix_hist(const K *__restric
   table[(long long)threadIdx.x * tiles + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// Stable scatter of one tile: the tile's items are first ranked by digit
-// into shared memory (so that each digit's items are contiguous there, in
-// their input order), then written out in that order, so consecutive threads
-// store to consecutive addresses of a digit's output run.
+// Items of a scatter tile: warp w owns the contiguous items [w*256,
+// (w+1)*256), read as 8 rows of 32 consecutive items.
+// Stable scatter of one tile.  Each warp ranks its own items against a
+// private per-digit count (match_any gives the equal-digit peers of a row),
+// the per-digit counts are scanned across warps and digits, the items are
+// placed into shared memory in digit order (input order within a digit) and
+// written out so that consecutive threads store consecutive addresses of a
+// digit's output run.
 template <typename K>
 __global__ void __launch_bounds__(kRadixThreads)
   k_radix_scatter(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
                   uint32_t *__restrict__ vout, long long n, int shift, uint32_t mask, const int *__restrict__ table,
                   int tiles)
 {
+  constexpr int kWarps = kRadixThreads / kWarp;
   __shared__ K s_key[kRadixTile];
   __shared__ uint32_t s_val[kRadixTile];
-  __shared__ int s_off[256];   // this tile's first output slot per digit (scanned table)
-  __shared__ int s_start[256]; // first shared-memory slot per digit
-  __shared__ int s_base[256];  // items of the digit ranked so far
-  __shared__ int s_warp[kRadixThreads / kWarp][256];
+  __shared__ int s_off[256];         // this tile's first output slot per digit (scanned table)
+  __shared__ int s_start[256];       // first shared-memory slot per digit
+  __shared__ int s_wcnt[kWarps][256]; // per warp and digit: count, then the warp's offset within the digit
+  __shared__ int s_wsum[kWarps];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long base = (long long)blockIdx.x * kRadixTile;
-  const int count = (int)min((long long)kRadixTile, n - base);
+  const long long tile0 = (long long)blockIdx.x * kRadixTile;
+  const int count = (int)min((long long)kRadixTile, n - tile0);
   s_off[tid] = table[(long long)tid * tiles + blockIdx.x];
-  s_base[tid] = 0;
-  s_start[tid] = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++)
+    s_wcnt[w][tid] = 0;
   __syncthreads();
-  K key[kRadixItems];
-  uint32_t val[kRadixItems];
-#pragma unroll
-  for (int r = 0; r < kRadixItems; r++)
-  {
-    const int k = r * kRadixThreads + tid;
-    key[r] = k < count ? kin[base + k] : K(0);
-    val[r] = k < count ? vin[base + k] : 0u;
-    if (k < count)
-      atomicAdd(&s_start[(uint32_t)(key[r] >> shift) & mask], 1);
-  }
-  __syncthreads();
-  if (warp == 0)
-  { // exclusive scan of the 256 digit counts, 8 per lane
-    int v[8], sum = 0;
-#pragma unroll
-    for (int q = 0; q < 8; q++)
-    {
-      v[q] = s_start[8 * lane + q];
-      sum += v[q];
-    }
-    int incl = sum;
-    for (int o = 1; o < 32; o <<= 1)
-    {
-      const int y = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o)
-        incl += y;
-    }
-    int run = incl - sum;
-#pragma unroll
-    for (int q = 0; q < 8; q++)
-    {
-      s_start[8 * lane + q] = run;
-      run += v[q];
-    }
-  }
+  // 1. rank within the warp, row by row
   const uint32_t lt_mask = (1u << lane) - 1u;
+  const int wbase = warp * (kWarp * kRadixItems);
+  K key[kRadixItems];
+  uint32_t val[kRadixItems], dr[kRadixItems]; // digit (9 bits, 256 = no item) | rank in the warp << 9
 #pragma unroll
   for (int r = 0; r < kRadixItems; r++)
   {
-#pragma unroll
-    for (int w = 0; w < kRadixThreads / kWarp; w++)
-      s_warp[w][tid] = 0;
-    __syncthreads();
-    const bool valid = r * kRadixThreads + tid < count;
-    const uint32_t d = valid ? ((uint32_t)(key[r] >> shift) & mask) : (256u + lane);
+    const int k = wbase + r * kWarp + lane;
+    const bool valid = k < count;
+    key[r] = valid ? kin[tile0 + k] : K(0);
+    val[r] = valid ? vin[tile0 + k] : 0u;
+    const uint32_t d = valid ? ((uint32_t)(key[r] >> shift) & mask) : 256u;
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    if (valid && lane == __ffs(peers) - 1)
-      s_warp[warp][d] = __popc(peers);
-    __syncthreads();
-    if (valid)
-    {
-      int rank = s_base[d] + __popc(peers & lt_mask);
-      for (int w = 0; w < warp; w++)
-        rank += s_warp[w][d];
-      s_key[s_start[d] + rank] = key[r];
-      s_val[s_start[d] + rank] = val[r];
-    }
-    __syncthreads();
-    int add = 0;
-#pragma unroll
-    for (int w = 0; w < kRadixThreads / kWarp; w++)
-      add += s_warp[w][tid];
-    s_base[tid] += add;
+    const int before = (d < 256u) ? s_wcnt[warp][d] : 0;
+    dr[r] = d | ((uint32_t)(before + __popc(peers & lt_mask)) << 9);
+    __syncwarp();
+    if (d < 256u && lane == __ffs(peers) - 1)
+      s_wcnt[warp][d] = before + __popc(peers);
+    __syncwarp();
   }
   __syncthreads();
+  // 2. per digit (thread tid = digit): warp offsets within the digit, then
+  // the digit's start in the tile (exclusive scan over digits)
+  int run = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++)
+  {
+    const int c = s_wcnt[w][tid];
+    s_wcnt[w][tid] = run;
+    run += c;
+  }
+  int incl = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o)
+      incl += y;
+  }
+  if (lane == 31)
+    s_wsum[warp] = incl;
+  __syncthreads();
+  int woff = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; w++)
+    woff += (w < warp) ? s_wsum[w] : 0;
+  s_start[tid] = woff + incl - run;
+  __syncthreads();
+  // 3. place into shared memory in digit order
+#pragma unroll
+  for (int r = 0; r < kRadixItems; r++)
+  {
+    const uint32_t d = dr[r] & 511u;
+    if (d < 256u)
+    {
+      const int pos = s_start[d] + s_wcnt[warp][d] + (int)(dr[r] >> 9);
+      s_key[pos] = key[r];
+      s_val[pos] = val[r];
+    }
+  }
+  __syncthreads();
+  // 4. write out
   for (int k = tid; k < count; k += kRadixThreads)
   {
     const K kk = s_key[k];

@@ -473,9 +473,9 @@ __global__ void k_first_tgt_flags(DevState D, WarmBufs W, int total)
 __global__ void k_first_tgt_scatter(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
   if (j >= total || !D.flags[j])
     return;
-  const int s = find_segment<int>(D.src_off, D.S, j);
   D.tgt[D.off[s] + (D.F[j] - D.F[D.src_off[s]])] = (int)D.val[j];
 }
 
@@ -484,6 +484,7 @@ __global__ void k_first_tgt_scatter(DevState D, int total)
 __global__ void k_readmit_energy(DevState D, KParams K, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.part_off, D.S, min(j, total - 1));
   if (j > total)
     return;
   if (j == total)
@@ -491,7 +492,6 @@ __global__ void k_readmit_energy(DevState D, KParams K, int total)
     D.flags[j] = 0;
     return;
   }
-  const int s = find_segment<int>(D.part_off, D.S, j);
   const int p = D.tgt[D.off[s] + (j - D.part_off[s])];
   const float4 x = D.pm[p], v = D.vu[p];
   float dv[3];
@@ -508,9 +508,9 @@ __global__ void k_readmit_energy(DevState D, KParams K, int total)
 __global__ void k_readmit_scatter(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.tail_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.tail_off, D.S, j);
   const int q = j - D.tail_off[s];
   const int nb = D.nbound[s];
   const int base = D.part_off[s];
@@ -524,9 +524,9 @@ __global__ void k_readmit_scatter(DevState D, int total)
 __global__ void k_readmit_copy(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.tail_off, D.S, min(j, total - 1));
   if (j >= total)
     return;
-  const int s = find_segment<int>(D.tail_off, D.S, j);
   const long long g = D.off[s] + D.nbound[s] + (j - D.tail_off[s]);
   D.ord[g] = D.ord_tmp[g];
 }
@@ -536,6 +536,7 @@ __global__ void k_readmit_copy(DevState D, int total)
 __global__ void k_first_flags(DevState D, int total)
 {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp(D.tail_off, D.S, min(j, total - 1));
   if (j > total)
     return;
   if (j == total)
@@ -543,7 +544,6 @@ __global__ void k_first_flags(DevState D, int total)
     D.flags[j] = 0;
     return;
   }
-  const int s = find_segment<int>(D.tail_off, D.S, j);
   const int p = D.ord[D.off[s] + D.nbound[s] + (j - D.tail_off[s])];
   const bool kept = D.Ep[p] < 0.f;
   D.flags[j] = kept ? 1 : 0;
