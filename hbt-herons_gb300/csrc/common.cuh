@@ -41,7 +41,8 @@ __device__ __forceinline__ int find_segment(const T *__restrict__ off, int n, T 
 // indices: a 32-ary search for the first and the last lane's segment (each
 // step probes 32 evenly spaced offsets at once and counts them with a
 // ballot), then each lane searches only between those two segments.
-__device__ __forceinline__ int find_segment_32ary(const int *__restrict__ off, int lo, int hi, int target)
+template <typename T>
+__device__ __forceinline__ int find_segment_32ary(const T *__restrict__ off, int lo, int hi, T target)
 {
   const int lane = threadIdx.x & 31;
   while (hi - lo > 1) // off[lo] <= target; answer in [lo, hi)
@@ -57,9 +58,10 @@ __device__ __forceinline__ int find_segment_32ary(const int *__restrict__ off, i
   return lo;
 }
 
-__device__ __forceinline__ int find_segment_warp(const int *__restrict__ off, int n, int idx)
+template <typename T>
+__device__ __forceinline__ int find_segment_warp(const T *__restrict__ off, int n, T idx)
 {
-  const int first = __shfl_sync(0xffffffffu, idx, 0), last = __shfl_sync(0xffffffffu, idx, 31);
+  const T first = __shfl_sync(0xffffffffu, idx, 0), last = __shfl_sync(0xffffffffu, idx, 31);
   const int s0 = find_segment_32ary(off, 0, n, first);
   const int s1 = (last == first) ? s0 : find_segment_32ary(off, s0, n, last);
   int lo = s0, hi = s1 + 1;

@@ -128,7 +128,7 @@ struct IterationDriver
   {
     const unsigned sb = grid_for(S + 1, 256);
     mem.check(cudaMemsetAsync(D.fb_count, 0, sizeof(int), st));
-    k_bbox<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
+    k_bbox<<<grid_for(src_total, 256 * kBboxRows), 256, 0, st>>>(D, src_total);
     k_root<<<sb, 256, 0, st>>>(D, K);
     k_keys<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
     k_keys_fallback<<<sm_count * 4, 256, 0, st>>>(D);

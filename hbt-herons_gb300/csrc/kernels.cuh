@@ -148,18 +148,20 @@ __device__ __forceinline__ void note_mass_bound(const DevState &D, unsigned mbit
 __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, const float *__restrict__ vel,
                          const float *__restrict__ mass, const float *__restrict__ u, const uint8_t *__restrict__ type)
 {
+  // one particle per thread (the grid covers N); the whole warp looks up the subhaloes
   unsigned mbits = 0u;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = find_segment_warp<long long>(D.off, D.S, min(i, D.N - 1));
+  if (i < D.N)
   {
     D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
-    mbits = max(mbits, __float_as_uint(fabsf(mass[i])));
+    mbits = __float_as_uint(fabsf(mass[i]));
     D.vu[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], (K.thermal && u) ? u[i] : 0.f);
     int t = K.dm_only ? 1 : (type ? (int)type[i] : 1);
     t = t < 0 ? 0 : (t > 5 ? 5 : t);
     const bool tr = K.dm_only || ((1 << t) & K.tracer_mask);
     const bool ns = !K.dm_only && ((1 << t) & K.nosub_mask);
     D.ty[i] = (uint8_t)(t | (tr ? 8 : 0) | (ns ? 16 : 0));
-    const int s = find_segment<long long>(D.off, D.S, i);
     D.seg_of[i] = s;
     D.ord[i] = (int)i;
     D.bnd[i] = 1;
@@ -260,35 +262,99 @@ __device__ __forceinline__ int src_particle(const DevState &D, int s, int j)
   return D.ord[D.off[s] + k];
 }
 
-__global__ void k_bbox(DevState D, int total)
+// Per-subhalo bounding boxes of the sources (ordered-float min/max atomics).
+// A block covers kBboxRows x 256 consecutive items; when they all belong to
+// one subhalo (the common case for large subhaloes, whose atomics would
+// otherwise all meet on the same six words) the block reduces them first and
+// issues one set of atomics, else each warp reduces each row per subhalo.
+constexpr int kBboxRows = 4;
+
+__global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
 {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = j < total;
-  const int sw = find_segment_warp(D.src_off, D.S, min(j, total - 1));
-  const int s = valid ? sw : -1;
+  __shared__ unsigned s_red[8][6];
+  const long long tile0 = (long long)blockIdx.x * (256 * kBboxRows);
+  const int jl = (int)min((long long)total - 1, tile0 + 256 * kBboxRows - 1);
+  const int s_first = find_segment_warp(D.src_off, D.S, (int)tile0); // the same on every lane
+  const int s_last = find_segment_warp(D.src_off, D.S, jl);
   unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
-  if (valid)
+  if (s_first == s_last)
   {
-    const float4 x = D.pm[src_particle(D, s, j)];
-    lo[0] = hi[0] = float_to_ordered(x.x);
-    lo[1] = hi[1] = float_to_ordered(x.y);
-    lo[2] = hi[2] = float_to_ordered(x.z);
-  }
-  const unsigned peers = __match_any_sync(0xffffffffu, s);
-  const int leader = __ffs(peers) - 1;
 #pragma unroll
-  for (int d = 0; d < 3; d++)
-  {
-    lo[d] = __reduce_min_sync(peers, lo[d]);
-    hi[d] = __reduce_max_sync(peers, hi[d]);
-  }
-  if (valid && (int)(threadIdx.x & 31) == leader)
+    for (int r = 0; r < kBboxRows; r++)
+    {
+      const long long j = tile0 + r * 256 + threadIdx.x;
+      if (j < total)
+      {
+        const float4 x = D.pm[src_particle(D, s_first, (int)j)];
+        const unsigned v[3] = {float_to_ordered(x.x), float_to_ordered(x.y), float_to_ordered(x.z)};
+#pragma unroll
+        for (int d = 0; d < 3; d++)
+        {
+          lo[d] = min(lo[d], v[d]);
+          hi[d] = max(hi[d], v[d]);
+        }
+      }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d < 3; d++)
     {
-      atomicMin(&D.bb_lo[3 * s + d], lo[d]);
-      atomicMax(&D.bb_hi[3 * s + d], hi[d]);
+      lo[d] = __reduce_min_sync(0xffffffffu, lo[d]);
+      hi[d] = __reduce_max_sync(0xffffffffu, hi[d]);
     }
+    if (lane == 0)
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+      {
+        s_red[warp][d] = lo[d];
+        s_red[warp][3 + d] = hi[d];
+      }
+    __syncthreads();
+    if (threadIdx.x < 6)
+    {
+      const int q = threadIdx.x;
+      unsigned v = s_red[0][q];
+      for (int w = 1; w < 8; w++)
+        v = q < 3 ? min(v, s_red[w][q]) : max(v, s_red[w][q]);
+      if (q < 3)
+        atomicMin(&D.bb_lo[3 * s_first + q], v);
+      else
+        atomicMax(&D.bb_hi[3 * s_first + q - 3], v);
+    }
+    return;
+  }
+#pragma unroll 1
+  for (int r = 0; r < kBboxRows; r++)
+  {
+    const long long jj = tile0 + r * 256 + threadIdx.x;
+    const bool valid = jj < total;
+    const int j = (int)jj;
+    const int sw = find_segment_warp(D.src_off, D.S, min(j, total - 1));
+    const int s = valid ? sw : -1;
+    unsigned l[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, h[3] = {0u, 0u, 0u};
+    if (valid)
+    {
+      const float4 x = D.pm[src_particle(D, s, j)];
+      l[0] = h[0] = float_to_ordered(x.x);
+      l[1] = h[1] = float_to_ordered(x.y);
+      l[2] = h[2] = float_to_ordered(x.z);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, s);
+    const int leader = __ffs(peers) - 1;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      l[d] = __reduce_min_sync(peers, l[d]);
+      h[d] = __reduce_max_sync(peers, h[d]);
+    }
+    if (valid && (int)(threadIdx.x & 31) == leader)
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+      {
+        atomicMin(&D.bb_lo[3 * s + d], l[d]);
+        atomicMax(&D.bb_hi[3 * s + d], h[d]);
+      }
+  }
 }
 
 // Root cube (src/oct_tree.tpp:44-65): centre of the box, side = largest extent.
@@ -376,14 +442,14 @@ __global__ void k_root(DevState D, KParams K)
 // (src/oct_tree.tpp:70-92).  The 3-bit child indices of that descent, root
 // first, form the key, so sorting by key orders particles as the reference
 // walk visits them.
-__device__ __forceinline__ unsigned long long descent_key(float4 x, const double *root)
+__device__ __forceinline__ unsigned long long descent_key(float4 x, const double *root, int levels = 21)
 {
   double c0 = root[0], c1 = root[1], c2 = root[2];
   double half = 0.5 * root[3];
   const double x0 = x.x, x1 = x.y, x2 = x.z;
   unsigned long long key = 0;
 #pragma unroll 1
-  for (int l = 0; l < 21; l++)
+  for (int l = 0; l < levels; l++)
   {
     half *= 0.5;
     unsigned dgt = 0;
@@ -412,8 +478,8 @@ __device__ __forceinline__ unsigned long long spread3(unsigned long long v)
 // containing x: index = ceil(t) - 1 with t = (x - origin) * 2^21 / side.  The
 // float estimate of t is within 0.75 slab widths of the exact value, so the
 // first `exact_levels` digits are exact unless t lies within one slab of a
-// boundary at those levels (or is not finite); then the reference's double
-// descent is used.  Digits below the exact levels only order particles inside
+// boundary at those levels (or is not finite); then k_keys_fallback decides
+// them exactly in double.  Digits below the exact levels only order particles inside
 // cells smaller than the tree resolution, where the reference itself breaks
 // ties at random (src/oct_tree.tpp:108-120).
 // Returns false when the float estimate cannot guarantee the exact digits.
@@ -424,7 +490,8 @@ __device__ __forceinline__ bool descent_key_fast(float4 x, const float *kp, unsi
   if (inv == 0.f) // zero-size cube: every digit is 0, as in the reference
     return true;
   const int lv = __float_as_int(kp[7]);
-  const float unit = __int_as_float((127 + 21 - lv) << 23); // 2^(21 - lv)
+  const float unit = __int_as_float((127 + 21 - lv) << 23);     // 2^(21 - lv)
+  const float inv_unit = __int_as_float((127 - 21 + lv) << 23); // 2^(lv - 21): t / unit exactly
   const float xs[3] = {x.x, x.y, x.z};
 #pragma unroll
   for (int d = 0; d < 3; d++)
@@ -432,13 +499,13 @@ __device__ __forceinline__ bool descent_key_fast(float4 x, const float *kp, unsi
     const float t = __fmul_rn(__fsub_rn(__fsub_rn(xs[d], kp[d]), kp[3 + d]), inv);
     if (!(t > -1e30f && t < 1e30f))
       return false;
-    const float q = t / unit;
+    const float q = __fmul_rn(t, inv_unit);
     const float rem = (q - floorf(q)) * unit; // distance above the last exact-level boundary
     if (rem < 1.5f || unit - rem < 1.5f)
       return false;
     float c = floorf(t);
     c = c < 0.f ? 0.f : (c > 2097151.f ? 2097151.f : c);
-    key |= spread3((unsigned long long)c) << d;
+    key |= spread3((unsigned long long)__float2uint_rz(c)) << d; // 32-bit conversion (c < 2^21)
   }
   return true;
 }
@@ -471,6 +538,14 @@ __global__ void k_keys(DevState D, int total)
   }
 }
 
+// Items the fast descent could not decide.  Per axis the exact-level slab
+// index (slabs of width w = side 2^-lv, cells left-open, right-closed) lies
+// within one of the float estimate's, so two exact comparisons in double
+// settle it: x > o + m w with o the root cube's origin, the same dyadic
+// boundaries that the reference's descent (src/oct_tree.tpp:70-92) computes
+// without rounding.  The digits below the exact levels follow the float
+// estimate, kept inside the decided cell.  A non-finite estimate takes the
+// reference's descent level by level.
 __global__ void k_keys_fallback(DevState D)
 {
   const int n = *D.fb_count;
@@ -478,7 +553,45 @@ __global__ void k_keys_fallback(DevState D)
   {
     const int j = D.fb_list[i];
     const int p = (int)D.val[j];
-    D.key[j] = descent_key(D.pm[p], D.root + 4 * D.seg_of[p]);
+    const int s = D.seg_of[p];
+    const float *kp = D.keyp + 12 * s;
+    const double *r = D.root + 4 * s;
+    const int lv = __float_as_int(kp[7]);
+    const int low = 21 - lv;
+    const float4 x = D.pm[p];
+    const float xs[3] = {x.x, x.y, x.z};
+    const double w = r[3] * __hiloint2double((1023 - lv) << 20, 0); // side 2^-lv, exact
+    const float inv_unit = __int_as_float((127 - low) << 23);       // 2^-low
+    const unsigned top = (1u << lv) - 1u;
+    unsigned long long key = 0;
+    bool finite = true;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      const float t = __fmul_rn(__fsub_rn(__fsub_rn(xs[d], kp[d]), kp[3 + d]), kp[6]);
+      if (!(t > -1e30f && t < 1e30f))
+      {
+        finite = false;
+        break;
+      }
+      const float tl = floorf(__fmul_rn(t, inv_unit));
+      const int m0 = (int)fminf(fmaxf(tl, -1.f), (float)top + 1.f);
+      const double dx = (double)xs[d] - (r[d] - 0.5 * r[3]); // x - o
+      int k = m0 - 1; // sign of dx - m w from one fused rounding: exact
+      if (fma(-(double)m0, w, dx) > 0.)
+        k = (fma(-(double)(m0 + 1), w, dx) > 0.) ? m0 + 1 : m0;
+      k = k < 0 ? 0 : (k > (int)top ? (int)top : k);
+      // digits below the exact levels: the float slab index, clamped into slab k
+      float c = floorf(t);
+      c = c < 0.f ? 0.f : (c > 2097151.f ? 2097151.f : c);
+      unsigned c21 = __float2uint_rz(c);
+      const unsigned lo21 = (unsigned)k << low, hi21 = lo21 | ((1u << low) - 1u);
+      c21 = c21 < lo21 ? lo21 : (c21 > hi21 ? hi21 : c21);
+      key |= spread3((unsigned long long)c21) << d;
+    }
+    if (!finite)
+      key = descent_key(x, r);
+    D.key[j] = key;
   }
 }
 

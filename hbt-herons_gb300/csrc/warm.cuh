@@ -175,7 +175,8 @@ __global__ void __launch_bounds__(256) k_feat_hist(DevState D, KParams K, WarmBu
     if (!(x.w > 0.f) || !(mmax > 0.f))
       continue;
     const int b = radial_bin(radius_about(x, D.ref_pos + 3 * s, K), __uint_as_float(W.rmax[s]));
-    const unsigned long long q = (unsigned long long)__float2ull_rn(__fmul_rn(__fdiv_rn(x.w, mmax), kQScale));
+    // <= 2^30, so a 32-bit conversion (64-bit ones issue to the FP64 pipe)
+    const unsigned long long q = (unsigned long long)__float2uint_rn(__fmul_rn(__fdiv_rn(x.w, mmax), kQScale));
     if (one >= 0)
       atomicAdd(&sh[b], q);
     else
