@@ -102,11 +102,20 @@ __global__ void k_feat_reset(DevState D, WarmBufs W)
   }
 }
 
-// Largest radius about the input frame, bounding box, largest mass.
-__global__ void k_feat_extent(DevState D, KParams K, WarmBufs W)
+// Largest radius about the input frame, bounding box, largest mass.  The
+// block reduces first: to one set of atomics when all its particles belong
+// to one subhalo (large subhaloes would otherwise send every warp's atomics
+// to the same words), else per warp and subhalo; the largest mass always
+// once per block.
+__global__ void __launch_bounds__(256) k_feat_extent(DevState D, KParams K, WarmBufs W)
 {
+  __shared__ unsigned s_red[8][8];
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < D.N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const long long b0 = (long long)blockIdx.x * blockDim.x;
+  const long long b1 = min(D.N, b0 + (long long)blockDim.x) - 1;
+  const bool uniform = b0 < D.N && D.seg_of[b0] == D.seg_of[b1];
   const int s = valid ? D.seg_of[i] : -1;
   unsigned r = 0u, m = 0u, lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   if (valid)
@@ -118,10 +127,8 @@ __global__ void k_feat_extent(DevState D, KParams K, WarmBufs W)
     lo[1] = hi[1] = float_to_ordered(x.y);
     lo[2] = hi[2] = float_to_ordered(x.z);
   }
+  const unsigned peers = uniform ? 0xffffffffu : __match_any_sync(0xffffffffu, s);
   const unsigned mm = __reduce_max_sync(0xffffffffu, m);
-  if ((threadIdx.x & 31) == 0 && mm)
-    atomicMax(W.mmax, mm);
-  const unsigned peers = __match_any_sync(0xffffffffu, s);
   r = __reduce_max_sync(peers, r);
 #pragma unroll
   for (int d = 0; d < 3; d++)
@@ -129,7 +136,41 @@ __global__ void k_feat_extent(DevState D, KParams K, WarmBufs W)
     lo[d] = __reduce_min_sync(peers, lo[d]);
     hi[d] = __reduce_max_sync(peers, hi[d]);
   }
-  if (valid && (int)(threadIdx.x & 31) == __ffs(peers) - 1)
+  if (lane == 0)
+  {
+    s_red[warp][0] = mm;
+    s_red[warp][1] = r;
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      s_red[warp][2 + d] = lo[d];
+      s_red[warp][5 + d] = hi[d];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 8)
+  { // q = 0: largest mass; q = 1..7: the uniform subhalo's radius and box
+    const int q = threadIdx.x;
+    if (q == 0 || uniform)
+    {
+      unsigned v = s_red[0][q];
+      for (int w = 1; w < 8; w++)
+        v = (q >= 2 && q < 5) ? min(v, s_red[w][q]) : max(v, s_red[w][q]);
+      const int su = uniform ? D.seg_of[b0] : 0;
+      if (q == 0)
+      {
+        if (v)
+          atomicMax(W.mmax, v);
+      }
+      else if (q == 1)
+        atomicMax(&W.rmax[su], v);
+      else if (q < 5)
+        atomicMin(&W.bb[6 * su + (q - 2)], v);
+      else
+        atomicMax(&W.bb[6 * su + 3 + (q - 5)], v);
+    }
+  }
+  if (!uniform && valid && lane == __ffs(peers) - 1)
   {
     atomicMax(&W.rmax[s], r);
 #pragma unroll
@@ -201,34 +242,38 @@ __global__ void __launch_bounds__(256) k_feat_profile(DevState D, KParams K, War
   if (s >= D.S)
     return;
   float *tab = W.tab + (long long)kTab * s;
-  const double unit = (double)__uint_as_float(*W.mmax) / (double)kQScale;
+  // FP32 throughout (FP64 throughput is low on this GPU; the features feed a
+  // BF16 network); the 64-bit bin masses are converted by bit arithmetic
+  const float unit = __fmul_rn(__uint_as_float(*W.mmax), 1.f / kQScale); // exact: kQScale is 2^30
   const float rmax = __uint_as_float(W.rmax[s]);
-  const double m0 = (double)W.hist[(long long)kBins * s + 2 * lane] * unit;
-  const double m1 = (double)W.hist[(long long)kBins * s + 2 * lane + 1] * unit;
-  auto edge = [&](int k) { return (double)rmax * exp2((k - kBins) * 0.25); };
-  const double w0 = m0 / (edge(2 * lane) * 1.0905077326652577), w1 = m1 / (edge(2 * lane + 1) * 1.0905077326652577);
+  float m0, m1, lo_unused;
+  ll_to_float2((long long)W.hist[(long long)kBins * s + 2 * lane], m0, lo_unused);
+  ll_to_float2((long long)W.hist[(long long)kBins * s + 2 * lane + 1], m1, lo_unused);
+  m0 *= unit;
+  m1 *= unit;
+  const float e0 = rmax * exp2f((2 * lane - kBins) * 0.25f), e1 = rmax * exp2f((2 * lane + 1 - kBins) * 0.25f);
+  const float w0 = m0 / (e0 * 1.0905077326652577f), w1 = m1 / (e1 * 1.0905077326652577f);
   // inclusive scans of the pair sums
-  double cm = m0 + m1, cw = w0 + w1;
+  float cm = m0 + m1, cw = w0 + w1;
   for (int o = 1; o < 32; o <<= 1)
   {
-    const double a = __shfl_up_sync(0xffffffffu, cm, o), b = __shfl_up_sync(0xffffffffu, cw, o);
+    const float a = __shfl_up_sync(0xffffffffu, cm, o), b = __shfl_up_sync(0xffffffffu, cw, o);
     if (lane >= o)
     {
       cm += a;
       cw += b;
     }
   }
-  const double M = __shfl_sync(0xffffffffu, cm, 31), Wt = __shfl_sync(0xffffffffu, cw, 31);
-  const double C0 = cm - m0 - m1, C1 = C0 + m0;       // M(<e_2l), M(<e_2l+1)
-  const double O0 = Wt - (cw - w0 - w1), O1 = O0 - w0; // outer sums from bins 2l and 2l+1
-  const double g = (double)K.G_over_a;
-  const double rr = (double)rmax;
-  if (rr > 0.)
+  const float M = __shfl_sync(0xffffffffu, cm, 31), Wt = __shfl_sync(0xffffffffu, cw, 31);
+  const float C0 = cm - m0 - m1, C1 = C0 + m0;       // M(<e_2l), M(<e_2l+1)
+  const float O0 = Wt - (cw - w0 - w1), O1 = O0 - w0; // outer sums from bins 2l and 2l+1
+  const float g = K.G_over_a;
+  if (rmax > 0.f)
   {
-    tab[4 + 2 * lane] = (float)(-g * (C0 / edge(2 * lane) + O0));
-    tab[4 + 2 * lane + 1] = (float)(-g * (C1 / edge(2 * lane + 1) + O1));
+    tab[4 + 2 * lane] = -g * (C0 / e0 + O0);
+    tab[4 + 2 * lane + 1] = -g * (C1 / e1 + O1);
     if (lane == 31)
-      tab[4 + kBins] = (float)(-g * M / rr);
+      tab[4 + kBins] = -g * M / rmax;
   }
   else
   {
@@ -237,27 +282,27 @@ __global__ void __launch_bounds__(256) k_feat_profile(DevState D, KParams K, War
       tab[4 + kBins] = 0.f;
   }
   // half-mass radius: the bin where the cumulative mass crosses M/2, log-interpolated
-  const double half = 0.5 * M;
-  double rh = -1.;
-  if (M > 0.)
+  const float half = 0.5f * M;
+  float rh = -1.f;
+  if (M > 0.f)
   {
-    if (C0 < half && half <= C1 && m0 > 0.)
-      rh = edge(2 * lane) * exp2(0.25 * (half - C0) / m0);
-    else if (C1 < half && half <= C1 + m1 && m1 > 0.)
-      rh = edge(2 * lane + 1) * exp2(0.25 * (half - C1) / m1);
+    if (C0 < half && half <= C1 && m0 > 0.f)
+      rh = e0 * exp2f(0.25f * (half - C0) / m0);
+    else if (C1 < half && half <= C1 + m1 && m1 > 0.f)
+      rh = e1 * exp2f(0.25f * (half - C1) / m1);
   }
-  const unsigned has = __ballot_sync(0xffffffffu, rh > 0.);
+  const unsigned has = __ballot_sync(0xffffffffu, rh > 0.f);
   if (has)
     rh = __shfl_sync(0xffffffffu, rh, __ffs(has) - 1);
   if (lane == 0)
   {
     tab[0] = rmax;
-    if (!(rh > 0.))
-      rh = rr;
-    const double vc2 = (rh > 0.) ? g * half / rh : 0.;
-    tab[1] = rh > 0. ? (float)(1. / rh) : 0.f;
-    tab[2] = vc2 > 0. ? (float)(1. / vc2) : 0.f;
-    tab[3] = vc2 > 0. ? (float)(1. / sqrt(vc2)) : 0.f;
+    if (!(rh > 0.f))
+      rh = rmax;
+    const float vc2 = (rh > 0.f) ? g * half / rh : 0.f;
+    tab[1] = rh > 0.f ? 1.f / rh : 0.f;
+    tab[2] = vc2 > 0.f ? 1.f / vc2 : 0.f;
+    tab[3] = vc2 > 0.f ? rsqrtf(vc2) : 0.f;
   }
 }
 
