@@ -67,6 +67,36 @@ struct IterationDriver
     return h;
   }
 
+  struct Count3Load
+  {
+    const int *a, *b, *c;
+    __device__ I3 operator()(long long i) const { return I3{a[i], b[i], c[i]}; }
+  };
+  struct Count3Store
+  {
+    int *a, *b, *c;
+    __device__ void operator()(long long i, const I3 &v) const
+    {
+      a[i] = v.a;
+      b[i] = v.b;
+      c[i] = v.c;
+    }
+  };
+
+  // Exclusive scans of three count arrays (n counts plus a trailing zero
+  // each) in one pass, with one host read of the three totals.
+  void scan_counts3(const int *c0, int *o0, const int *c1, int *o1, const int *c2, int *o2, long long n, int tot[3])
+  {
+    // an int scratch for 8 (n + 1) items covers scan_scratch_elems<I3>(n + 1) I3s
+    I3 *scr = reinterpret_cast<I3 *>(mem.scan_scratch(8 * (n + 1)));
+    scan_load_store<I3, false>(Count3Load{c0, c1, c2}, Count3Store{o0, o1, o2}, n + 1, scr, st, &launches);
+    check();
+    mem.check(cudaMemcpyAsync(&tot[0], o0 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    mem.check(cudaMemcpyAsync(&tot[1], o1 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    mem.check(cudaMemcpyAsync(&tot[2], o2 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    mem.check(cudaStreamSynchronize(st));
+  }
+
   // Exclusive scan of n counts plus a trailing zero; returns the total.
   int scan_counts(const int *cnt, int *offs, long long n)
   {
@@ -198,9 +228,9 @@ struct IterationDriver
       k_plan<<<sb, 256, 0, st>>>(D, K);
       launches++;
       check();
-      const int src_total = scan_counts(D.src_cnt, D.src_off, S);
-      const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
-      const int part_total = scan_counts(D.part_cnt, D.part_off, S);
+      int tot[3];
+      scan_counts3(D.src_cnt, D.src_off, D.chunk_cnt, D.chunk_off, D.part_cnt, D.part_off, S, tot);
+      const int src_total = tot[0], chunk_total = tot[1], part_total = tot[2];
       mem.mark(0);
       if (part_total == 0 && src_total == 0)
         break;

@@ -1658,7 +1658,10 @@ __global__ void k_epi_order(DevState D, OutPtrs O)
 __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
 {
   const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kItemsPerThread;
-  double acc[6] = {0., 0., 0., 0., 0., 0.};
+  // AverageKinematics sums (src/subhalo_unbind.cpp:200-249) in compensated
+  // FP32 per thread (the per-particle terms the reference forms in double
+  // carry one FP32 rounding each here), totals in double
+  KahanF acc[6];
   int tn[6] = {0, 0, 0, 0, 0, 0};
   double tm[6] = {0., 0., 0., 0., 0., 0.};
   int ft = 0x7fffffff;
@@ -1685,10 +1688,12 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
       if (j >= D.fin_off[s + 1])
       {
         for (int q = 0; q < 6; q++)
-          if (acc[q] != 0.)
-            atomicAdd(&D.com[7 * s + q], acc[q]);
-        for (int q = 0; q < 6; q++)
-          acc[q] = 0.;
+        {
+          const double v = acc[q].value();
+          if (v != 0.)
+            atomicAdd(&D.com[7 * s + q], v);
+          acc[q] = KahanF();
+        }
         flush_types(s);
         s = find_segment<int>(D.fin_off, D.S, j); // skips any run of empty segments
       }
@@ -1700,29 +1705,32 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
       if (O.energy)
         O.energy[off + k] = e;
       const float m = x.w;
-      acc[0] += (double)__fmul_rn(e, m);
+      acc[0].add(__fmul_rn(e, m));
       if (K.thermal)
-        acc[0] -= (double)__fmul_rn(v.w, m);
+        acc[0].add(-__fmul_rn(v.w, m));
       const float *rp = D.ref_pos + 3 * s, *rv = D.ref_vel + 3 * s;
       const float xs[3] = {x.x, x.y, x.z}, vs[3] = {v.x, v.y, v.z};
-      double dx[3], dv[3];
+      float dx[3], dv[3];
       float pe = K.thermal ? __fsub_rn(e, v.w) : e;
+#pragma unroll
       for (int d = 0; d < 3; d++)
       {
-        dx[d] = (double)__fsub_rn(xs[d], rp[d]);
+        dx[d] = __fsub_rn(xs[d], rp[d]);
         if (K.periodic)
-          dx[d] = nearest_d(dx[d], K.half, K.box);
-        dx[d] *= (double)K.a;
-        dv[d] = (double)__fsub_rn(vs[d], rv[d]) + (double)K.hz * dx[d];
-        acc[1] += dv[d] * dv[d] * m;
-        pe = (float)((double)pe - 0.5 * dv[d] * dv[d]);
+          dx[d] = nearest_f(dx[d], K.half, K.box);
+        dx[d] = __fmul_rn(dx[d], K.a);
+        dv[d] = __fmaf_rn(K.hz, dx[d], __fsub_rn(vs[d], rv[d]));
+        const float dv2 = __fmul_rn(dv[d], dv[d]);
+        acc[1].add(__fmul_rn(dv2, m));
+        if (O.potential)
+          pe = __fsub_rn(pe, __fmul_rn(0.5f, dv2));
       }
       if (O.potential)
         O.potential[off + k] = pe;
-      acc[2] += (dx[1] * dv[2] - dx[2] * dv[1]) * m;
-      acc[3] += (dx[2] * dv[0] - dx[0] * dv[2]) * m;
-      acc[4] += (dx[0] * dv[1] - dx[1] * dv[0]) * m;
-      acc[5] += m;
+      acc[2].add(__fmul_rn(__fmaf_rn(dx[1], dv[2], -__fmul_rn(dx[2], dv[1])), m));
+      acc[3].add(__fmul_rn(__fmaf_rn(dx[2], dv[0], -__fmul_rn(dx[0], dv[2])), m));
+      acc[4].add(__fmul_rn(__fmaf_rn(dx[0], dv[1], -__fmul_rn(dx[1], dv[0])), m));
+      acc[5].add(m);
       const uint8_t t = D.ty[p];
 #pragma unroll
       for (int q = 0; q < 6; q++)
@@ -1736,7 +1744,8 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
     }
     flush_types(s);
   }
-  double acc7[7] = {acc[0], acc[1], acc[2], acc[3], acc[4], acc[5], 0.};
+  double acc7[7] = {acc[0].value(), acc[1].value(), acc[2].value(), acc[3].value(), acc[4].value(),
+                    acc[5].value(), 0.};
   segmented_flush<7>(acc7, s, D.com);
 }
 

@@ -17,7 +17,8 @@ namespace hbtg
 
 constexpr int kScanThreads = 256;
 
-// Rows per warp of a scan tile: 8 for 4/8-byte types, 4 for 32-byte I4.
+// Rows per warp of a scan tile: 8 for 4/8-byte types, 4 for the 12-byte I3
+// and 32-byte I4.
 template <typename T>
 __host__ __device__ constexpr int scan_items()
 {
@@ -38,6 +39,13 @@ struct I4
   __host__ __device__ I4 operator+(const I4 &o) const { return I4{m + o.m, x + o.x, y + o.y, z + o.z}; }
 };
 
+// Three counts scanned together (one pass, one host read of the totals).
+struct I3
+{
+  int a, b, c;
+  __host__ __device__ I3 operator+(const I3 &o) const { return I3{a + o.a, b + o.b, c + o.c}; }
+};
+
 template <typename T>
 __device__ __forceinline__ T zero_of();
 template <>
@@ -46,11 +54,19 @@ template <>
 __device__ __forceinline__ long long zero_of<long long>() { return 0; }
 template <>
 __device__ __forceinline__ I4 zero_of<I4>() { return I4{0, 0, 0, 0}; }
+template <>
+__device__ __forceinline__ I3 zero_of<I3>() { return I3{0, 0, 0}; }
 
 template <typename T>
 __device__ __forceinline__ T shfl_up(T v, int d)
 {
   return __shfl_up_sync(0xffffffffu, v, d);
+}
+template <>
+__device__ __forceinline__ I3 shfl_up<I3>(I3 v, int d)
+{
+  return I3{__shfl_up_sync(0xffffffffu, v.a, d), __shfl_up_sync(0xffffffffu, v.b, d),
+            __shfl_up_sync(0xffffffffu, v.c, d)};
 }
 template <>
 __device__ __forceinline__ I4 shfl_up<I4>(I4 v, int d)
@@ -63,6 +79,12 @@ template <typename T>
 __device__ __forceinline__ T shfl_idx(T v, int src)
 {
   return __shfl_sync(0xffffffffu, v, src);
+}
+template <>
+__device__ __forceinline__ I3 shfl_idx<I3>(I3 v, int src)
+{
+  return I3{__shfl_sync(0xffffffffu, v.a, src), __shfl_sync(0xffffffffu, v.b, src),
+            __shfl_sync(0xffffffffu, v.c, src)};
 }
 template <>
 __device__ __forceinline__ I4 shfl_idx<I4>(I4 v, int src)
@@ -84,12 +106,18 @@ __device__ __forceinline__ T warp_inclusive_scan(T v, int lane)
   return v;
 }
 
-// Scan input read straight from an array.
+// Scan input read straight from an array, output written to one.
 template <typename T>
 struct ArrayLoad
 {
   const T *in;
   __device__ __forceinline__ T operator()(long long i) const { return in[i]; }
+};
+template <typename T>
+struct ArrayStore
+{
+  T *out;
+  __device__ __forceinline__ void operator()(long long i, const T &v) const { out[i] = v; }
 };
 
 // Reduce-then-scan.  A tile is 8 warps x 32 lanes x scan_items<T>() rows;
@@ -127,8 +155,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Load load, T *__re
   }
 }
 
-template <typename T, bool Inclusive, typename Load>
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(Load load, T *out, const T *__restrict__ tile_off,
+template <typename T, bool Inclusive, typename Load, typename Store>
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(Load load, Store store, const T *__restrict__ tile_off,
                                                              long long n)
 {
   constexpr int kTile = scan_tile<T>(), kRows = scan_items<T>();
@@ -164,7 +192,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(Load load, T *out, 
   {
     const long long i = wbase + k * kWarp + lane;
     if (i < n)
-      out[i] = off + v[k];
+      store(i, off + v[k]);
   }
 }
 
@@ -182,10 +210,10 @@ inline size_t scan_scratch_elems(long long n)
   return tot + 2;
 }
 
-// Device-wide scan of the n items load(0..n-1) into out.  `scratch` must hold
-// scan_scratch_elems(n) items of T.
-template <typename T, bool Inclusive, typename Load>
-void scan_load(Load load, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
+// Device-wide scan of the n items load(0..n-1), result i passed to store(i, .).
+// `scratch` must hold scan_scratch_elems(n) items of T.
+template <typename T, bool Inclusive, typename Load, typename Store>
+void scan_load_store(Load load, Store store, long long n, T *scratch, cudaStream_t st, int64_t *launches)
 {
   constexpr int kTile = scan_tile<T>();
   if (n <= 0)
@@ -193,15 +221,23 @@ void scan_load(Load load, T *out, long long n, T *scratch, cudaStream_t st, int6
   const long long tiles = (n + kTile - 1) / kTile;
   if (tiles == 1)
   {
-    k_scan_apply<T, Inclusive, Load><<<1, kScanThreads, 0, st>>>(load, out, nullptr, n);
+    k_scan_apply<T, Inclusive, Load, Store><<<1, kScanThreads, 0, st>>>(load, store, nullptr, n);
     (*launches)++;
     return;
   }
   T *sums = scratch, *sums_scanned = scratch + tiles;
   k_scan_reduce<T, Load><<<(unsigned)tiles, kScanThreads, 0, st>>>(load, sums, n);
-  scan_load<T, false>(ArrayLoad<T>{sums}, sums_scanned, tiles, scratch + 2 * tiles, st, launches);
-  k_scan_apply<T, Inclusive, Load><<<(unsigned)tiles, kScanThreads, 0, st>>>(load, out, sums_scanned, n);
+  scan_load_store<T, false>(ArrayLoad<T>{sums}, ArrayStore<T>{sums_scanned}, tiles, scratch + 2 * tiles, st,
+                            launches);
+  k_scan_apply<T, Inclusive, Load, Store><<<(unsigned)tiles, kScanThreads, 0, st>>>(load, store, sums_scanned, n);
   *launches += 2;
+}
+
+// Device-wide scan of the n items load(0..n-1) into out.
+template <typename T, bool Inclusive, typename Load>
+void scan_load(Load load, T *out, long long n, T *scratch, cudaStream_t st, int64_t *launches)
+{
+  scan_load_store<T, Inclusive>(load, ArrayStore<T>{out}, n, scratch, st, launches);
 }
 
 // Device-wide scan of n items (in may equal out).
