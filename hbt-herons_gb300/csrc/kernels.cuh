@@ -4,8 +4,12 @@
 // subhaloes that are still iterating advance together: each lock-step
 // iteration runs the same kernel sequence over the "active" segments, packed
 // by device-side exclusive scans of per-subhalo counts (src_off, chunk_off,
-// part_off, ...).  A packed item j is mapped back to its subhalo by a binary
-// search over the packed offsets.
+// part_off, ...).  A packed item j is mapped back to its subhalo by a search
+// over the packed offsets (warp-cooperative in the per-item kernels:
+// find_segment_warp).  FP64 throughput is low on this GPU (about 1/64 of
+// FP32, and 64-bit integer/float conversions issue to the same pipe), so the
+// per-item kernels use FP32 and integer arithmetic, with error-free
+// transforms or fixed point where the reference accumulates in double.
 //
 // Reference correspondence (HBT-HERONS):
 //   k_bbox/k_root   bounding cube of the tree        src/oct_tree.tpp:27-47
