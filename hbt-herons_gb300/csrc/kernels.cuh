@@ -93,6 +93,7 @@ struct DevState
   int *ngrav;              // tree sources of a subsampled iteration (0 = not subsampled)
   float *factor;           // [6S] mass upscale factor per type of the current iteration
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
+  unsigned *bb_m;          // [S] float bits of the largest |source mass| (k_bbox, reset with the boxes)
   double *root;            // [4S] centre xyz, side length
   float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
   int *fb_list, *fb_count; // packed items whose key needs the exact double descent
@@ -104,7 +105,6 @@ struct DevState
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
   int *cnt, *X, *flags, *F;
   I4 *P;          // fixed-point prefix sums of source mass and mass x offset (k_tree_emit)
-  unsigned *pmax; // [1] float bits of the largest |particle mass| of the call
   float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
   int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
@@ -140,26 +140,15 @@ __device__ __forceinline__ float source_mass(const DevState &D, int s, int p)
 // ---------------------------------------------------------------------------
 // Set-up
 // ---------------------------------------------------------------------------
-// Largest |mass| of the call (D.pmax, zeroed before the repack): bounds the
-// fixed-point prefix sums of the tree build.  Every thread of the block calls it.
-__device__ __forceinline__ void note_mass_bound(const DevState &D, unsigned mbits)
-{
-  mbits = __reduce_max_sync(0xffffffffu, mbits);
-  if ((threadIdx.x & 31) == 0 && mbits)
-    atomicMax(D.pmax, mbits);
-}
-
 __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, const float *__restrict__ vel,
                          const float *__restrict__ mass, const float *__restrict__ u, const uint8_t *__restrict__ type)
 {
   // one particle per thread (the grid covers N); the whole warp looks up the subhaloes
-  unsigned mbits = 0u;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int s = find_segment_warp<long long>(D.off, D.S, min(i, D.N - 1));
   if (i < D.N)
   {
     D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
-    mbits = __float_as_uint(fabsf(mass[i]));
     D.vu[i] = make_float4(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2], (K.thermal && u) ? u[i] : 0.f);
     int t = K.dm_only ? 1 : (type ? (int)type[i] : 1);
     t = t < 0 ? 0 : (t > 5 ? 5 : t);
@@ -170,7 +159,6 @@ __global__ void k_repack(DevState D, KParams K, const float *__restrict__ pos, c
     D.ord[i] = (int)i;
     D.bnd[i] = 1;
   }
-  note_mass_bound(D, mbits);
 }
 
 __global__ void k_init_subs(DevState D, KParams K)
@@ -254,6 +242,7 @@ __global__ void k_plan(DevState D, KParams K)
     D.sp_cnt[s] = D.sp_len[s];
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
+  D.bb_m[s] = 0u;
   D.tracers[s] = 0;
 }
 
@@ -275,12 +264,12 @@ constexpr int kBboxRows = 4;
 
 __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
 {
-  __shared__ unsigned s_red[8][6];
+  __shared__ unsigned s_red[8][7];
   const long long tile0 = (long long)blockIdx.x * (256 * kBboxRows);
   const int jl = (int)min((long long)total - 1, tile0 + 256 * kBboxRows - 1);
   const int s_first = find_segment_warp(D.src_off, D.S, (int)tile0); // the same on every lane
   const int s_last = find_segment_warp(D.src_off, D.S, jl);
-  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u}, mm = 0u;
   if (s_first == s_last)
   {
 #pragma unroll
@@ -289,7 +278,9 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       const long long j = tile0 + r * 256 + threadIdx.x;
       if (j < total)
       {
-        const float4 x = D.pm[src_particle(D, s_first, (int)j)];
+        const int p = src_particle(D, s_first, (int)j);
+        const float4 x = D.pm[p];
+        mm = max(mm, __float_as_uint(fabsf(source_mass(D, s_first, p))));
         const unsigned v[3] = {float_to_ordered(x.x), float_to_ordered(x.y), float_to_ordered(x.z)};
 #pragma unroll
         for (int d = 0; d < 3; d++)
@@ -306,15 +297,19 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       lo[d] = __reduce_min_sync(0xffffffffu, lo[d]);
       hi[d] = __reduce_max_sync(0xffffffffu, hi[d]);
     }
+    mm = __reduce_max_sync(0xffffffffu, mm);
     if (lane == 0)
+    {
 #pragma unroll
       for (int d = 0; d < 3; d++)
       {
         s_red[warp][d] = lo[d];
         s_red[warp][3 + d] = hi[d];
       }
+      s_red[warp][6] = mm;
+    }
     __syncthreads();
-    if (threadIdx.x < 6)
+    if (threadIdx.x < 7)
     {
       const int q = threadIdx.x;
       unsigned v = s_red[0][q];
@@ -322,8 +317,10 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
         v = q < 3 ? min(v, s_red[w][q]) : max(v, s_red[w][q]);
       if (q < 3)
         atomicMin(&D.bb_lo[3 * s_first + q], v);
-      else
+      else if (q < 6)
         atomicMax(&D.bb_hi[3 * s_first + q - 3], v);
+      else if (v)
+        atomicMax(&D.bb_m[s_first], v);
     }
     return;
   }
@@ -335,10 +332,12 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
     const int j = (int)jj;
     const int sw = find_segment_warp(D.src_off, D.S, min(j, total - 1));
     const int s = valid ? sw : -1;
-    unsigned l[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, h[3] = {0u, 0u, 0u};
+    unsigned l[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, h[3] = {0u, 0u, 0u}, m = 0u;
     if (valid)
     {
-      const float4 x = D.pm[src_particle(D, s, j)];
+      const int p = src_particle(D, s, j);
+      const float4 x = D.pm[p];
+      m = __float_as_uint(fabsf(source_mass(D, s, p)));
       l[0] = h[0] = float_to_ordered(x.x);
       l[1] = h[1] = float_to_ordered(x.y);
       l[2] = h[2] = float_to_ordered(x.z);
@@ -351,13 +350,18 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       l[d] = __reduce_min_sync(peers, l[d]);
       h[d] = __reduce_max_sync(peers, h[d]);
     }
+    m = __reduce_max_sync(peers, m);
     if (valid && (int)(threadIdx.x & 31) == leader)
+    {
 #pragma unroll
       for (int d = 0; d < 3; d++)
       {
         atomicMin(&D.bb_lo[3 * s + d], l[d]);
         atomicMax(&D.bb_hi[3 * s + d], h[d]);
       }
+      if (m)
+        atomicMax(&D.bb_m[s], m);
+    }
   }
 }
 
@@ -408,13 +412,10 @@ __global__ void k_root(DevState D, KParams K)
   kp[8] = __int_as_float(kstar);
   // fixed-point scales of the prefix sums (PrefixLoad): 2^em per mass unit and
   // 2^ex per mass x length unit.  The subhalo's source mass is below count x
-  // largest mass x largest upscale factor, and offsets from the float origin
+  // its largest source mass (k_bbox), and offsets from the float origin
   // kp[0..2] are below side + |origin| 2^-23, so every partial sum of the
   // subhalo stays below 2^61.
-  float fup = 1.f;
-  for (int t = 0; t < 6; t++)
-    fup = fmaxf(fup, D.factor[6 * s + t]);
-  const double mtot = (double)D.src_cnt[s] * (double)__uint_as_float(*D.pmax) * (double)fup;
+  const double mtot = (double)D.src_cnt[s] * (double)__uint_as_float(D.bb_m[s]);
   double omax = 0.;
   for (int d = 0; d < 3; d++)
     omax = fmax(omax, fabs((double)kp[d]));
@@ -1355,6 +1356,7 @@ __global__ void k_plan_refine(DevState D, KParams K)
   // a fresh bounding box for the prefix's own tree (k_bbox, k_root)
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
+  D.bb_m[s] = 0u;
 }
 
 __global__ void k_refine_keys(DevState D, KParams K, int total)

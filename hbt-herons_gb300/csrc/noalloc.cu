@@ -62,7 +62,7 @@ constexpr size_t kScratchBytes =
   26 * al(sizeof(int) * kS1) +               // per-subhalo ints
   al(sizeof(float) * 6 * kS1) +              // mass upscale factors
   al(sizeof(float) * 8 * kS1) +              // old frame, mbound
-  al(sizeof(unsigned) * 6 * kS1) +           // bounding boxes
+  al(sizeof(unsigned) * 7 * kS1) +           // bounding boxes, largest source masses
   al(sizeof(double) * 4 * kS1) +             // root cubes
   al(sizeof(float) * 12 * kS1) +             // fast key-descent constants
   al(sizeof(double) * 7 * kS1) +             // frame sums
@@ -72,7 +72,7 @@ constexpr size_t kScratchBytes =
   6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
   al(sizeof(int) * kN1) + al(sizeof(int)) +  // key fallback list and its count
   4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
-  al(sizeof(I4) * kN1) + al(sizeof(unsigned)) + // prefix sums, largest mass
+  al(sizeof(I4) * kN1) +                     // prefix sums
   al(sizeof(float4) * kNoAllocMaxRecords) +  // tree slots
   al(sizeof(int) * kTable) +                 // radix table
   al(sizeof(int) * kScanScr) +               // scan scratch
@@ -279,9 +279,10 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.old_pos = subf;
   D.old_vel = subf + 3 * kS1;
   D.mbound = subf + 6 * kS1;
-  unsigned *bb = c.take<unsigned>(6 * kS1);
+  unsigned *bb = c.take<unsigned>(7 * kS1);
   D.bb_lo = bb;
   D.bb_hi = bb ? bb + 3 * kS1 : nullptr;
+  D.bb_m = bb ? bb + 6 * kS1 : nullptr;
   D.factor = c.take<float>(6 * kS1);
   D.root = c.take<double>(4 * kS1);
   D.keyp = c.take<float>(12 * kS1);
@@ -303,7 +304,6 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.flags = c.take<int>(kN1);
   D.F = c.take<int>(kN1);
   D.P = c.take<I4>(kN1);
-  D.pmax = c.take<unsigned>(1);
   mem.slots = c.take<float4>(kNoAllocMaxRecords);
   D.nodes = mem.slots;
   mem.table = c.take<int>(kTable);
@@ -324,7 +324,6 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   {
     ck(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
     ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
-    ck(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
     if (N > 0)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
     k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D, R.K);

@@ -29,17 +29,14 @@ namespace
 {
 __global__ void k_pot_repack(DevState D, const float *__restrict__ pos, const float *__restrict__ mass)
 {
-  unsigned mbits = 0u;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < D.N; i += (long long)gridDim.x * blockDim.x)
   {
     D.pm[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], mass[i]);
-    mbits = max(mbits, __float_as_uint(fabsf(mass[i])));
     D.vu[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     D.ty[i] = 1;
     D.seg_of[i] = 0;
     D.ord[i] = (int)i;
   }
-  note_mass_bound(D, mbits);
 }
 
 // One "subhalo" whose every particle is a source; the walk takes the
@@ -68,6 +65,7 @@ __global__ void k_pot_plan(DevState D, int n_tgt, int phase)
       D.bb_lo[d] = 0xffffffffu;
       D.bb_hi[d] = 0u;
     }
+    D.bb_m[0] = 0u;
     for (int t = 0; t < 6; t++)
       D.factor[t] = 1.f;
   }
@@ -137,7 +135,7 @@ enum Slot
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
   S_NODES, S_TABLE, S_SCRATCH, S_PSCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
-  S_POTI, S_WCTR, S_PMAX,
+  S_POTI, S_WCTR,
   S_NUM
 };
 
@@ -419,9 +417,10 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.mb_pos = b->mostbound_pos;
   D.mb_vel = b->mostbound_vel;
   D.mb_id = reinterpret_cast<long long *>(b->most_bound_id);
-  unsigned *bb = P.get<unsigned>(S_BB, (size_t)S * 6);
+  unsigned *bb = P.get<unsigned>(S_BB, (size_t)S * 7);
   D.bb_lo = bb;
   D.bb_hi = bb + 3 * (size_t)S;
+  D.bb_m = bb + 6 * (size_t)S;
   D.root = P.get<double>(S_ROOT, (size_t)S * 4);
   D.keyp = P.get<float>(S_KEYP, (size_t)S * 12);
   D.com = P.get<double>(S_COM, (size_t)S * 7);
@@ -442,11 +441,9 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
   D.F = P.get<int>(S_F, n1 + 1);
   D.P = P.get<I4>(S_P, n1);
-  D.pmax = P.get<unsigned>(S_PMAX, 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
-  HBTG_CUDA(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
 
   if (N > 0)
   {
@@ -778,9 +775,10 @@ int pot_call(void *arg)
   D.self_cnt = nexti();
   int *bad = nexti();
   D.factor = P.get<float>(S_FACTOR, 6);
-  unsigned *bb = P.get<unsigned>(S_BB, 6);
+  unsigned *bb = P.get<unsigned>(S_BB, 7);
   D.bb_lo = bb;
   D.bb_hi = bb + 3;
+  D.bb_m = bb + 6;
   D.root = P.get<double>(S_ROOT, 4);
   D.keyp = P.get<float>(S_KEYP, 12);
   D.key = P.get<unsigned long long>(S_KEY, n1);
@@ -796,12 +794,10 @@ int pot_call(void *arg)
   D.cnt = P.get<int>(S_CNT, n1 + 1);
   D.X = P.get<int>(S_X, n1 + 1);
   D.P = P.get<I4>(S_P, n1);
-  D.pmax = P.get<unsigned>(S_PMAX, 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));
   HBTG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
-  HBTG_CUDA(cudaMemsetAsync(D.pmax, 0, sizeof(unsigned), st));
   k_pot_repack<<<blocks_for(c.ns, 256), 256, 0, st>>>(D, c.pos, c.mass);
   k_pot_plan<<<1, 32, 0, st>>>(D, (int)c.nt, 0);
   R.check();

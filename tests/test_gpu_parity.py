@@ -70,6 +70,20 @@ def test_gpu_hydro_thermal_vs_oracle(unbinder):
     assert np.all(rel < 1e-4), rel
 
 
+def test_gpu_mass_dynamic_range_vs_oracle(unbinder):
+    """One particle 1e10 times heavier than the rest in the first subhalo: the
+    fixed-point multipole sums of the other subhaloes are scaled by their own
+    largest mass, so their energies keep the precision of an ordinary batch."""
+    inp = synthetic.hydro(seed=5, n_sub=40, nmin=100, nmax=20_000, box=300.0)
+    inp.mass[int(inp.offsets[0])] = 1e10
+    prm = abi.parity_params(thermal=1, box_size=300.0)
+    got = unbinder.unbind(inp, prm)
+    ref = oracle.run_port(inp, prm)
+    check_invariants(inp, got)
+    m = assert_parity(inp, got, ref, prm)
+    assert m["energy_rel_median"] < 1e-5, m
+
+
 def test_gpu_nfw_single_1e5(unbinder):
     inp = synthetic.nfw_single(n=100_000, seed=0)
     prm = abi.parity_params(dm_only=1, box_size=100.0)
