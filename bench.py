@@ -286,7 +286,7 @@ def bench_gpu(args):
         assert rc in (0, 4), rc
 
     e2e_call()  # warm the host path once
-    e2e_times, h2d, d2h = [], 0, 0
+    e2e_times, e2e_device, h2d, d2h = [], [], 0, 0
     for _ in range(args.steps):
         _reset_frames(buf, hin)
         barrier()
@@ -295,6 +295,7 @@ def bench_gpu(args):
         e2e_times.append(time.perf_counter() - t0)
         st = u.stats()
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+        e2e_device.append(st["ms_total"])
     t_e2e = float(np.mean(e2e_times))
     if world > 1:
         t_e2e = _max_over_ranks(t_e2e)
@@ -348,7 +349,9 @@ def bench_gpu(args):
                                                 "ms_propose", "ms_walk", "ms_tree", "ms_part", "ms_frame",
                                                 "ms_plan", "ms_final")},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "call": "hbtg_unbind_batch_learned (host pointers, pinned)"},
+                    "call": "hbtg_unbind_batch_learned (host pointers, pinned)",
+                    "ms_per_call": 1e3 * float(np.mean(e2e_times)),
+                    "ms_device_part": float(np.mean(e2e_device))},
             "gpu_launches": warm["kernel_launches"] // args.steps,
             "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
