@@ -173,8 +173,7 @@ struct IterationDriver
     tree_nodes += internal;
     scan_load<I4, true>(PrefixLoad{D}, D.P, src_total, mem.prefix_scratch(src_total), st, &launches);
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
-    k_record_key_order<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
-    launches += 2;
+    launches++;
     check();
   }
 

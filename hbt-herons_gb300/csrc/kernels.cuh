@@ -635,17 +635,6 @@ __global__ void k_segkeys(const uint32_t *__restrict__ val, const int *__restric
     k32[j] = (uint32_t)seg_of[val[j]];
 }
 
-// After a full tree build: remember each such subhalo's particles in key order.
-__global__ void k_record_key_order(DevState D, int total)
-{
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
-  if (j >= total)
-    return;
-  if (!D.corr[s] && !D.ngrav[s])
-    D.sp[D.off[s] + (j - D.src_off[s])] = (int)D.val[j];
-}
-
 // Subsampled subhaloes: the sources are not every candidate, so their
 // correction targets come from the energy-list order instead (packed by part_off).
 __global__ void k_record_candidates(DevState D, int total)
@@ -986,6 +975,9 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
     const int p = (int)D.val[j];
     const float4 x = D.pm[p];
     D.nodes[base + 2 * c] = make_float4(x.x, x.y, x.z, fabsf(source_mass(D, s, p)));
+    // a full build records the subhalo's particles in key order (correction walks' targets)
+    if (!D.corr[s] && !D.ngrav[s])
+      D.sp[D.off[s] + (j - seg0)] = p;
   }
   int incl = c; // inclusive scan of the cell counts over the warp
 #pragma unroll
@@ -1466,9 +1458,11 @@ __global__ void k_com(DevState D, KParams K, int total)
       acc[q] = KahanF();
     }
   };
+  // the whole warp looks up its threads' first subhaloes (first items ascend with the lane)
+  const int s_first = find_segment_warp(D.fin_off, D.S, (int)min(first, (long long)total - 1));
   if (first < total)
   {
-    s = find_segment<int>(D.fin_off, D.S, (int)first);
+    s = s_first;
     const int last = (int)min((long long)total, first + kItemsPerThread);
     float4 o = D.pm[D.ord[D.off[s]]];
     for (int j = (int)first; j < last; j++)
