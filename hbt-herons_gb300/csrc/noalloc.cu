@@ -13,22 +13,29 @@
 //
 // Limits: at most kNoAllocMaxParticles particles and kNoAllocMaxSubhaloes
 // subhaloes per call, and at most kNoAllocMaxRecords tree records (leaves
-// plus cells) in one iteration; larger calls are rejected with
-// HBTG_ERR_INVALID (sizes) or HBTG_ERR_NOMEM (tree larger than the reserve,
-// found mid-run; the outputs are then not written).
+// plus cells) in one tree; larger calls are rejected with HBTG_ERR_INVALID
+// (sizes, checked before any GPU work) or HBTG_ERR_NOMEM (a tree larger than
+// the reserve, found mid-run).  The iteration runs on copies of the in/out
+// frames (ref_pos, ref_vel, mostbound_pos, mostbound_vel) held in the
+// reserve, and every caller array is written only after the last tree is
+// built, so on HBTG_ERR_NOMEM none of the caller's arrays has changed and the
+// same batch can be retried through an allocating entry point.
 //
 // Sharing: every call on a device uses the same array and leaves its contents
 // behind; each call initialises what it reads before reading it.  Calls whose
 // GPU work overlaps (two host threads, or two streams) race on the array and
 // must be serialised by the caller.
 //
-// Set-up: the first call on each device looks up the array's device address
-// with cudaGetSymbolAddress while that device is current (host code cannot
-// use the array's name as a device pointer).  Make that first call before
-// any stream capture begins.
+// Set-up: every call looks up the array's device address with
+// cudaGetSymbolAddress on the current device (host code cannot use the
+// array's name as a device pointer); the lookup is not cached, so a device
+// reset between calls is harmless.  With lazy module loading (the CUDA
+// default) the array itself is allocated when this file's module is first
+// loaded, which happens in the first call on each device: make one warm-up
+// call outside any region where the device must not allocate, and before any
+// stream capture begins.
 #include <algorithm>
 #include <cstring>
-#include <mutex>
 
 #include "../../include/hbt_unbind_gpu.h"
 #include "common.cuh"
@@ -44,6 +51,7 @@ namespace
 constexpr long long kNoAllocMaxParticles = 1LL << 16; // 65,536
 constexpr int kNoAllocMaxSubhaloes = 8192;
 constexpr long long kNoAllocMaxRecords = 3 * kNoAllocMaxParticles;
+constexpr int kMaxWalkRanges = 256; // walk ranges (one per SM) the counters cover
 
 constexpr size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
@@ -77,32 +85,23 @@ constexpr size_t kScratchBytes =
   al(sizeof(int) * kTable) +                 // radix table
   al(sizeof(int) * kScanScr) +               // scan scratch
   al(sizeof(I4) * kPScr) +                   // prefix-sum scan scratch
-  al(sizeof(unsigned long long));            // interaction counter
+  al(sizeof(unsigned long long)) +           // interaction counter
+  al(sizeof(float) * 12 * kS1) +             // working copies of the in/out frames
+  al(sizeof(unsigned) * kMaxWalkRanges);     // per-SM walk chunk counters
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-unsigned char *g_scratch_addr[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (looked up once).
-int scratch_address(int device, unsigned char **out)
+// Device address of g_noalloc_scratch on the current device.
+int scratch_address(unsigned char **out)
 {
-  if (device < 0 || device >= kMaxDevices)
-    return HBTG_ERR_NO_DEVICE;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[device])
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
   {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-    {
-      cudaGetLastError();
-      return HBTG_ERR_CUDA;
-    }
-    g_scratch_addr[device] = static_cast<unsigned char *>(p);
+    cudaGetLastError();
+    return HBTG_ERR_CUDA;
   }
-  *out = g_scratch_addr[device];
+  *out = static_cast<unsigned char *>(p);
   return HBTG_OK;
 }
 
@@ -241,14 +240,21 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   if (cudaGetDevice(&device) != cudaSuccess)
     return HBTG_ERR_NO_DEVICE;
   unsigned char *base = nullptr;
-  int rc = scratch_address(device, &base);
+  int rc = scratch_address(&base);
   if (rc != HBTG_OK)
     return rc;
+  int sms = 0;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || sms <= 0)
+  {
+    cudaGetLastError();
+    return HBTG_ERR_CUDA;
+  }
 
   StaticMem mem;
   IterationDriver<StaticMem> R(mem, st);
   R.K = noalloc_kparams(p);
   R.S = (int)S;
+  R.sm_count = std::min(sms, kMaxWalkRanges);
   int bits = 0;
   while ((1LL << bits) < S)
     bits++;
@@ -310,19 +316,27 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   mem.scan_scr = c.take<int>(kScanScr);
   mem.p_scr = c.take<I4>(kPScr);
   D.interactions = c.take<unsigned long long>(1);
+  float *frames = c.take<float>(12 * kS1);
+  D.walk_ctr = c.take<unsigned>(kMaxWalkRanges);
   if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr ||
       (size_t)scan_scratch_elems<I4>(kN1) > kPScr)
     return HBTG_ERR_NOMEM; // layout does not fit the reserve (cannot happen with the constants above)
-  D.ref_pos = b->ref_pos;
-  D.ref_vel = b->ref_vel;
-  D.mb_pos = b->mostbound_pos;
-  D.mb_vel = b->mostbound_vel;
+  // the iteration moves the frames: it works on copies in the reserve
+  D.ref_pos = frames;
+  D.ref_vel = frames + 3 * kS1;
+  D.mb_pos = frames + 6 * kS1;
+  D.mb_vel = frames + 9 * kS1;
   D.mb_id = reinterpret_cast<long long *>(b->most_bound_id);
   D.id = reinterpret_cast<const long long *>(b->id);
+  const size_t fbytes = sizeof(float) * 3 * (size_t)S;
 
   try
   {
     ck(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
+    ck(cudaMemcpyAsync(D.ref_pos, b->ref_pos, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(D.ref_vel, b->ref_vel, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(D.mb_pos, b->mostbound_pos, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(D.mb_vel, b->mostbound_vel, fbytes, cudaMemcpyDefault, st));
     ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
     if (N > 0)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
@@ -344,6 +358,10 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
     O.iterations = b->iterations;
     O.status = b->status;
     R.epilogue(O);
+    ck(cudaMemcpyAsync(b->ref_pos, D.ref_pos, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(b->ref_vel, D.ref_vel, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(b->mostbound_pos, D.mb_pos, fbytes, cudaMemcpyDefault, st));
+    ck(cudaMemcpyAsync(b->mostbound_vel, D.mb_vel, fbytes, cudaMemcpyDefault, st));
     ck(cudaStreamSynchronize(st));
   }
   catch (Fail &f)

@@ -135,7 +135,7 @@ enum Slot
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
   S_NODES, S_TABLE, S_SCRATCH, S_PSCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
-  S_POTI, S_WCTR,
+  S_POTI, S_WCTR, S_FRAMEW,
   S_NUM
 };
 
@@ -412,10 +412,19 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.old_pos = subf;
   D.old_vel = subf + 3 * (size_t)S;
   D.mbound = subf + 6 * (size_t)S;
-  D.ref_pos = b->ref_pos;
-  D.ref_vel = b->ref_vel;
-  D.mb_pos = b->mostbound_pos;
-  D.mb_vel = b->mostbound_vel;
+  // The iteration moves the in/out frames: it works on copies and writes the
+  // caller's arrays back after the epilogue, so a call that fails part-way
+  // (HBTG_ERR_NOMEM when the pool cannot grow) leaves them as they were.
+  float *framew = P.get<float>(S_FRAMEW, (size_t)S * 12);
+  const size_t fbytes = sizeof(float) * 3 * (size_t)S;
+  D.ref_pos = framew;
+  D.ref_vel = framew + 3 * (size_t)S;
+  D.mb_pos = framew + 6 * (size_t)S;
+  D.mb_vel = framew + 9 * (size_t)S;
+  HBTG_CUDA(cudaMemcpyAsync(D.ref_pos, b->ref_pos, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(D.ref_vel, b->ref_vel, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(D.mb_pos, b->mostbound_pos, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(D.mb_vel, b->mostbound_vel, fbytes, cudaMemcpyDefault, st));
   D.mb_id = reinterpret_cast<long long *>(b->most_bound_id);
   unsigned *bb = P.get<unsigned>(S_BB, (size_t)S * 7);
   D.bb_lo = bb;
@@ -531,6 +540,10 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   O.iterations = b->iterations;
   O.status = b->status;
   R.epilogue(O);
+  HBTG_CUDA(cudaMemcpyAsync(b->ref_pos, D.ref_pos, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(b->ref_vel, D.ref_vel, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(b->mostbound_pos, D.mb_pos, fbytes, cudaMemcpyDefault, st));
+  HBTG_CUDA(cudaMemcpyAsync(b->mostbound_vel, D.mb_vel, fbytes, cudaMemcpyDefault, st));
   HBTG_CUDA(cudaEventRecord(t1, st));
   HBTG_CUDA(cudaEventSynchronize(t1));
   H->last_S = S;

@@ -208,9 +208,15 @@ void hbtg_default_params(hbtg_params *params);
  * reserve of about 17 MiB inside the library, held on every GPU that loads it
  * until the process exits.  Limits: at most 65,536 particles and 8,192
  * subhaloes per call (else HBTG_ERR_INVALID) and at most 196,608 tree records
- * per iteration (else HBTG_ERR_NOMEM, outputs unwritten).  The first call on a
- * device resolves the reserve's device address; make it before any stream
- * capture.  All calls share the reserve: calls that overlap on the GPU race. */
+ * in one tree (else HBTG_ERR_NOMEM).  On either of these two returns none
+ * of the caller's arrays has been written: the iteration runs on copies of the
+ * in/out frames inside the reserve, so the batch can be retried through an
+ * allocating entry point.  Every call looks up the reserve's device address.
+ * With lazy module loading (the CUDA default) the reserve itself is
+ * allocated when the first call on a device loads the library's module: make
+ * one warm-up call outside any region that must not allocate and before any
+ * stream capture.  All calls share the reserve: calls that overlap on the GPU
+ * race. */
 int hbtg_unbind_batch_noalloc(const hbtg_params *params, hbtg_batch *batch, void *cuda_stream);
 
 /* The tree potential of one particle set: GravityTree_t::Build over the n_src

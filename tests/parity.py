@@ -134,3 +134,214 @@ def check_invariants(inp, out, sorted_energies=True):
             assert np.all(e < 0), ("kept particle with E >= 0", s)
             if sorted_energies:
                 assert np.all(np.diff(e) >= 0), ("bound set not sorted by energy", s)
+
+
+# ---------------------------------------------------------------------------
+# Full-output parity: every field one call returns.
+#
+# Bars for a subhalo whose bound ID set is the reference's ("matched"):
+#   * bound order      position by position the reference's, except where the
+#                      two particles' reference energies tie within
+#                      ENERGY_TIE_REL * |potential| (FP32 walk vs the
+#                      reference's double walk); skipped under
+#                      RefineMostBoundParticle, whose prefix order comes from
+#                      energies that are not returned
+#   * unbound tail     (removal batches, most recent first, each sorted by
+#                      energy; src/subhalo_unbind.cpp:673) the same particles
+#                      at each position, except ties moved within a window of
+#                      TAIL_WINDOW positions; and the source kept by
+#                      TruncateSource (first SourceSubRelaxFactor * Nbound
+#                      particles, src/subhalo_unbind.cpp:843-853) the same set
+#   * energy, potential |got - ref| <= FLOAT_REL * |potential_ref| for all but
+#                      FLOAT_OUTLIER_FRAC of the particles (a borderline
+#                      opening decision moves one particle by the tree's own
+#                      approximation error)
+#   * counts per type  identical; masses (total and per type) FLOAT_REL
+#   * frames, kinematics, core phase space  FLOAT_REL relative to the scale of
+#                      the quantity (positions: the box, with two float ulps of
+#                      the coordinate as a floor)
+#   * tracer index, most-bound ID and position/velocity  identical (the
+#                      most-bound ID up to an energy tie, as above)
+#   * iterations       identical
+# Over the whole batch: membership <= MEMBERSHIP_TOL and the raw total bound
+# mass within MASS_TOL.
+# ---------------------------------------------------------------------------
+FLOAT_REL = 1e-5
+FLOAT_OUTLIER_FRAC = 1e-3
+TAIL_WINDOW = 8
+SOURCE_RELAX = 3.0  # SourceSubRelaxFactor default (src/config_parser.cpp)
+
+
+def _ulp32(x):
+    x = np.abs(np.asarray(x, np.float32))
+    return np.spacing(np.maximum(x, np.float32(1e-30))).astype(np.float64)
+
+
+def _close(got, ref, scale, floor=None):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    tol = FLOAT_REL * np.asarray(scale, np.float64)
+    if floor is not None:
+        tol = np.maximum(tol, floor)
+    return np.abs(got - ref) <= tol
+
+
+def compare_full(inp, got, ref, params, refine=None, box=None):
+    """Compares every output of `got` with `ref` (same inputs).  Returns
+    (metrics, violations): violations is a list of (field, subhalo, detail)."""
+    if refine is None:
+        refine = bool(params.max_sample_size > 0 and params.refine_most_bound)
+    if box is None:
+        box = float(params.box_size)
+    viol = []
+    base = compare(inp, got, ref)
+    ns = inp.n_sub
+    matched = 0
+    tail_moved = 0
+    tail_checked = 0
+    trunc_mism = 0
+    trunc_total = 0
+    n_float = 0
+    n_float_bad = 0
+    iter_diff = 0
+    for s in range(ns):
+        off, end = int(inp.offsets[s]), int(inp.offsets[s + 1])
+        n = end - off
+        nbg, nbr = int(got.nbound[s]), int(ref.nbound[s])
+        ids_g = inp.id[off + got.order[off:end]]
+        ids_r = inp.id[off + ref.order[off:end]]
+        # TruncateSource keeps the first max(Nbound * relax, Nbound <= 1) particles
+        keep = nbr if nbr <= 1 else min(n, int(nbr * SOURCE_RELAX))
+        keep_g = nbg if nbg <= 1 else min(n, int(nbg * SOURCE_RELAX))
+        trunc_mism += len(np.setxor1d(ids_g[:keep_g], ids_r[:keep], assume_unique=True))
+        trunc_total += keep
+        if got.status[s] != ref.status[s]:
+            continue
+        if nbg != nbr or not np.array_equal(np.sort(ids_g[:nbg]), np.sort(ids_r[:nbr])):
+            continue
+        matched += 1
+        nb = nbr
+        if got.iterations[s] != ref.iterations[s]:
+            iter_diff += 1
+            viol.append(("iterations", s, (int(got.iterations[s]), int(ref.iterations[s]))))
+        # scales of this subhalo
+        pot_r = ref.potential[off:off + nb] if (ref.potential is not None) else None
+        e_r = ref.energy[off:off + nb].astype(np.float64) if ref.energy is not None else None
+        escale = np.abs(pot_r).astype(np.float64) if pot_r is not None else (np.abs(e_r) if e_r is not None else None)
+        # bound order (ties allowed)
+        if nb and not refine and e_r is not None:
+            pos_r = {int(i): k for k, i in enumerate(ids_r[:nb])}
+            diff = np.nonzero(ids_g[:nb] != ids_r[:nb])[0]
+            for k in diff:
+                other = pos_r[int(ids_g[k])]
+                if abs(e_r[other] - e_r[k]) > ENERGY_TIE_REL * max(escale[k], escale[other]):
+                    viol.append(("bound_order", s, (int(k), int(ids_g[k]), int(ids_r[k]))))
+                    break
+        # unbound tail: ties moved within a window
+        if got.iterations[s] == ref.iterations[s] and n > nb and got.status[s] in (0, 3):
+            tg, tr = ids_g[nb:], ids_r[nb:]
+            tail_checked += len(tr)
+            where_r = {int(i): k for k, i in enumerate(tr)}
+            moved = np.nonzero(tg != tr)[0]
+            tail_moved += len(moved)
+            for k in moved:
+                if abs(where_r[int(tg[k])] - int(k)) > TAIL_WINDOW:
+                    viol.append(("tail_order", s, (int(k), int(tg[k]), int(tr[k]))))
+                    break
+        if not nb:
+            continue
+        # per-particle floats of the bound set, matched by ID
+        if escale is not None:
+            idx_r = np.argsort(ids_r[:nb])
+            idx_g = np.argsort(ids_g[:nb])
+            sc = np.maximum(escale[idx_r], 1e-30)
+            for field in ("energy", "potential"):
+                a, b = getattr(got, field), getattr(ref, field)
+                if a is None or b is None:
+                    continue
+                va = a[off:off + nb].astype(np.float64)[idx_g]
+                vb = b[off:off + nb].astype(np.float64)[idx_r]
+                bad = np.abs(va - vb) > FLOAT_REL * sc
+                n_float += nb
+                n_float_bad += int(bad.sum())
+        # counts and masses
+        if not np.array_equal(got.nbound_type[s], ref.nbound_type[s]):
+            viol.append(("nbound_type", s, (got.nbound_type[s].tolist(), ref.nbound_type[s].tolist())))
+        if not _close(got.mbound[s], ref.mbound[s], abs(float(ref.mbound[s]))):
+            viol.append(("mbound", s, (float(got.mbound[s]), float(ref.mbound[s]))))
+        mt = float(np.abs(ref.mbound_type[s]).sum())
+        if not np.all(_close(got.mbound_type[s], ref.mbound_type[s], mt)):
+            viol.append(("mbound_type", s, (got.mbound_type[s].tolist(), ref.mbound_type[s].tolist())))
+        # frames: positions against the box (two ulps floor), velocities against |V| + spread
+        if not np.all(_close(got.ref_pos[s], ref.ref_pos[s], 0.0, floor=2 * _ulp32(ref.ref_pos[s]) + FLOAT_REL * 1e-3 * box)):
+            viol.append(("ref_pos", s, (got.ref_pos[s].tolist(), ref.ref_pos[s].tolist())))
+        vscale = np.linalg.norm(ref.ref_vel[s]) + np.sqrt(max(2.0 * abs(float(ref.kinematics[s][1])), 0.0))
+        if not np.all(_close(got.ref_vel[s], ref.ref_vel[s], vscale)):
+            viol.append(("ref_vel", s, (got.ref_vel[s].tolist(), ref.ref_vel[s].tolist())))
+        # kinematics: energies against |<E-K>| + |<K>|, angular momentum against its norm + |r||v| floor
+        kg, kr = got.kinematics[s].astype(np.float64), ref.kinematics[s].astype(np.float64)
+        esc = abs(kr[0]) + abs(kr[1])
+        lsc = np.linalg.norm(kr[2:5]) + np.sqrt(2.0 * abs(kr[1])) * float(ref.core[s][6] if ref.core is not None else 0.0)
+        if not (np.all(_close(kg[:2], kr[:2], esc)) and np.all(_close(kg[2:], kr[2:], lsc))):
+            viol.append(("kinematics", s, (kg.tolist(), kr.tolist())))
+        # most-bound particle: position/velocity are its own input values
+        if ids_g[0] == ids_r[0]:
+            if not (np.array_equal(got.mostbound_pos[s], ref.mostbound_pos[s])
+                    and np.array_equal(got.mostbound_vel[s], ref.mostbound_vel[s])):
+                viol.append(("mostbound_pos_vel", s, None))
+            if got.tracer_index[s] != ref.tracer_index[s] and not refine:
+                viol.append(("tracer_index", s, (int(got.tracer_index[s]), int(ref.tracer_index[s]))))
+            if got.most_bound_id[s] != ref.most_bound_id[s] and not most_bound_is_tie(inp, got, ref, s):
+                viol.append(("most_bound_id", s, (int(got.most_bound_id[s]), int(ref.most_bound_id[s]))))
+        # core phase space: only where both used the same core particles
+        if got.core is not None and ref.core is not None:
+            core_n = max(int(np.float32(nb) * np.float32(params.sub_core_size_factor)), int(params.sub_core_size_min))
+            tr_mask = _tracer_mask(inp, params, off, end)
+            cg = _core_ids(ids_g[:nb], got.order[off:off + nb], tr_mask, core_n)
+            cr = _core_ids(ids_r[:nb], ref.order[off:off + nb], tr_mask, core_n)
+            if np.array_equal(np.sort(cg), np.sort(cr)):
+                c_g, c_r = got.core[s].astype(np.float64), ref.core[s].astype(np.float64)
+                okp = _close(c_g[:3], c_r[:3], 0.0, floor=2 * _ulp32(c_r[:3]) + FLOAT_REL * 1e-3 * box)
+                vsc = np.linalg.norm(c_r[3:6]) + c_r[7]
+                okv = _close(c_g[3:6], c_r[3:6], vsc)
+                oks = _close(c_g[6:8], c_r[6:8], np.abs(c_r[6:8]), floor=2 * _ulp32(c_r[6:8]))
+                if not (np.all(okp) and np.all(okv) and np.all(oks)):
+                    viol.append(("core", s, (c_g.tolist(), c_r.tolist())))
+    if n_float and n_float_bad > FLOAT_OUTLIER_FRAC * n_float:
+        viol.append(("energy/potential", -1, (n_float_bad, n_float)))
+    # the truncated source differs only through membership flips (bounded above)
+    # and tail ties moved across its end (bounded by the window check)
+    if trunc_mism > 10 * MEMBERSHIP_TOL * max(trunc_total, 1):
+        viol.append(("truncated_source", -1, (trunc_mism, trunc_total)))
+    m = dict(base)
+    m.update(matched=matched, n_sub=ns, tail_moved=tail_moved, tail_checked=tail_checked,
+             trunc_mismatch=trunc_mism / max(trunc_total, 1), float_outliers=n_float_bad / max(n_float, 1),
+             iter_diff=iter_diff)
+    return m, viol
+
+
+def _tracer_mask(inp, params, off, end):
+    if params.dm_only or inp.type is None:
+        return np.ones(end - off, bool)
+    t = inp.type[off:end].astype(np.int64)
+    return ((int(params.tracer_type_mask) >> t) & 1).astype(bool)
+
+
+def _core_ids(ids_bound, order_bound, tracer_mask, core_n):
+    """IDs of the particles GetCorePhaseSpaceProperties uses (first core_n
+    tracers in bound order, then non-tracers; src/subhalo_merge.cpp:120-150)."""
+    tr = tracer_mask[order_bound]
+    first = ids_bound[tr][:core_n]
+    if len(first) < core_n:
+        first = np.concatenate([first, ids_bound[~tr][:core_n - len(first)]])
+    return first
+
+
+def assert_full_parity(inp, got, ref, params, membership_tol=MEMBERSHIP_TOL, mass_tol=MASS_TOL, **kw):
+    """assert_parity plus every other output field (compare_full) and the raw
+    total bound mass."""
+    m0 = assert_parity(inp, got, ref, params, membership_tol=membership_tol, mass_tol=mass_tol)
+    m, viol = compare_full(inp, got, ref, params, **kw)
+    assert m0["mass_rel"] <= mass_tol, ("raw total bound mass", m0)
+    assert not viol, (viol[:10], len(viol), m)
+    return m
