@@ -357,6 +357,7 @@ def bench_gpu(args):
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "FP32 FMA throughput measured in-process (hbtg_measure_fp32_peak)",
                          "flops_per_launch": flops_per_launch, "ms_per_launch": walk_ms_per_launch,
+                         "blocks_per_sm": warm["last"].get("walk_blocks_per_sm"),
                          "walk_share_of_step": warm["ms_walk"] / max(warm["ms"], 1e-9)},
             "cpu_baseline": cpu,
             "clocks": warm["clocks"],

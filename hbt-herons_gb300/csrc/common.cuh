@@ -88,11 +88,11 @@ __device__ __forceinline__ double nearest_d(double x, double half, double box)
 
 // The octree is an array of 16-byte slots in depth-first preorder.
 //   leaf (a particle): one slot  (x, y, z, m),             m >= 0 (sign bit clear)
-//   cell:              two slots (x, y, z, -crit) (m, skip_bits, 0, 0)
+//   cell:              two slots (x, y, z, -crit) (m, skip_bits, len, 0)
 // The sign bit of w marks a cell; crit = len^2 / theta^2 (open when r^2 < crit);
 // skip (an int stored in the float's bits) is the first slot after the
-// subtree.  A cell's first child starts two slots after it.  The walk reads
-// the second slot of a cell only when it accepts the cell.
+// subtree; len is the cell's side length.  A cell's first child starts two
+// slots after it, and its children are the sibling subtrees up to its skip.
 __device__ __forceinline__ bool slot_is_cell(float w) { return (__float_as_uint(w) & 0x80000000u) != 0; }
 
 // Per-subhalo status while iterating.

@@ -12,7 +12,8 @@
 //   int *scan_scratch(long long n)               scratch for scan<int>(n)
 //   int *radix_table(long long n)                table for radix_sort_pairs(n)
 //   int *radix_scan_scratch(long long n)
-//   I4 *prefix_scratch(long long n)              scratch for scan<I4>(n)
+//   int *cell_list(long long cells)              per-level cell lists of one tree (may throw)
+//   int *level_counts()                          2 kLevels ints
 //   float4 *tree_slots(long long slots)          tree storage (may throw when too large)
 //   void mark(int phase)                         phase boundary for timing (may be a no-op)
 #pragma once
@@ -24,6 +25,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
+#include "walk.cuh"
 
 namespace hbtg
 {
@@ -44,6 +46,7 @@ struct IterationDriver
   int S = 0;
   int seg_bits = 0;
   int sm_count = 152;
+  int walk_blocks_per_sm = 1; // resident k_walk blocks per SM (occupancy)
   int64_t launches = 0;
   int64_t walk_launches = 0;
   int64_t tree_nodes = 0;
@@ -51,9 +54,13 @@ struct IterationDriver
 
   IterationDriver(Mem &m, cudaStream_t s) : mem(m), st(s)
   {
-    // the walk uses no shared memory: give the whole on-chip array to L1
-    cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-    cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+    // the walk keeps its stacks and interaction lists in shared memory
+    cudaFuncSetAttribute(k_walk<false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_walk<true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_walk<false>, 32 * kWalkWarps, 0) == cudaSuccess &&
+        nb > 0)
+      walk_blocks_per_sm = nb;
     cudaGetLastError();
   }
 
@@ -158,6 +165,8 @@ struct IterationDriver
   {
     const unsigned sb = grid_for(S + 1, 256);
     mem.check(cudaMemsetAsync(D.fb_count, 0, sizeof(int), st));
+    D.lvl = mem.level_counts();
+    mem.check(cudaMemsetAsync(D.lvl, 0, sizeof(int) * 2 * kLevels, st));
     k_bbox<<<grid_for(src_total, 256 * kBboxRows), 256, 0, st>>>(D, src_total);
     k_root<<<sb, 256, 0, st>>>(D, K);
     k_keys<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
@@ -169,11 +178,21 @@ struct IterationDriver
     launches++;
     check();
     const int internal = scan_counts(D.cnt, D.X, src_total);
-    D.nodes = mem.tree_slots((long long)src_total + 2LL * internal);
+    // one padding slot after the last: the walk reads a node's second slot unconditionally
+    D.nodes = mem.tree_slots((long long)src_total + 2LL * internal + 1);
+    D.cell_list = mem.cell_list(internal);
     tree_nodes += internal;
-    scan_load<I4, true>(PrefixLoad{D}, D.P, src_total, mem.prefix_scratch(src_total), st, &launches);
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
     launches++;
+    // cell multipoles bottom-up, one launch per level (deepest first)
+    const unsigned mg = std::max(1u, std::min(grid_for(internal, 256), (unsigned)sm_count * 8u));
+    for (int L = kLevels - 1; L >= 0; L--)
+    {
+      if (L > 21)
+        continue; // keys have 21 digits: no cell below level 21
+      k_tree_moments<<<mg, 256, 0, st>>>(D, L);
+      launches++;
+    }
     check();
   }
 
@@ -196,16 +215,16 @@ struct IterationDriver
   {
     if (chunk_total <= 0)
       return;
-    unsigned grid = grid_for(chunk_total, 8);
+    unsigned grid = grid_for(chunk_total, kWalkWarps);
     if (D.walk_ctr)
-    { // one resident wave (8 blocks of 8 warps per SM) over per-SM chunk ranges
+    { // one resident wave over per-SM chunk ranges
       mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)sm_count, st));
-      grid = std::min<unsigned>(grid, (unsigned)sm_count * 8u);
+      grid = std::min<unsigned>(grid, (unsigned)sm_count * (unsigned)walk_blocks_per_sm);
     }
     if (K.count_interactions)
-      k_walk<true><<<grid, 256, 0, st>>>(D, K, chunk_total, sm_count);
+      k_walk<true><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, sm_count);
     else
-      k_walk<false><<<grid, 256, 0, st>>>(D, K, chunk_total, sm_count);
+      k_walk<false><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, sm_count);
     launches++;
     walk_launches++;
     check();

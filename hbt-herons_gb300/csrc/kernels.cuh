@@ -93,7 +93,6 @@ struct DevState
   int *ngrav;              // tree sources of a subsampled iteration (0 = not subsampled)
   float *factor;           // [6S] mass upscale factor per type of the current iteration
   unsigned *bb_lo, *bb_hi; // ordered-float bounding boxes [3S]
-  unsigned *bb_m;          // [S] float bits of the largest |source mass| (k_bbox, reset with the boxes)
   double *root;            // [4S] centre xyz, side length
   float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
   int *fb_list, *fb_count; // packed items whose key needs the exact double descent
@@ -104,7 +103,8 @@ struct DevState
   unsigned long long *key, *key_alt;
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
   int *cnt, *X, *flags, *F;
-  I4 *P;          // fixed-point prefix sums of source mass and mass x offset (k_tree_emit)
+  int *cell_list; // tree cells (first slot) grouped by level (k_tree_emit), for the multipole pass
+  int *lvl;       // [2 kLevels]: cells per level (k_tree_count), fill cursors (k_tree_emit)
   float4 *nodes; // tree slots (see slot_is_cell)
   unsigned long long *interactions;
   int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
@@ -118,6 +118,9 @@ struct DevState
   int *ntest = nullptr;      // particles the first test evaluates
   float *ref0 = nullptr;     // [6S] input frame, restored for a cold restart
 };
+
+// Tree levels: keys hold 21 digits, so cells sit at levels 0..21.
+constexpr int kLevels = 32;
 
 __device__ __forceinline__ int lcp_levels(unsigned long long a, unsigned long long b)
 {
@@ -242,7 +245,6 @@ __global__ void k_plan(DevState D, KParams K)
     D.sp_cnt[s] = D.sp_len[s];
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
-  D.bb_m[s] = 0u;
   D.tracers[s] = 0;
 }
 
@@ -264,12 +266,12 @@ constexpr int kBboxRows = 4;
 
 __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
 {
-  __shared__ unsigned s_red[8][7];
+  __shared__ unsigned s_red[8][6];
   const long long tile0 = (long long)blockIdx.x * (256 * kBboxRows);
   const int jl = (int)min((long long)total - 1, tile0 + 256 * kBboxRows - 1);
   const int s_first = find_segment_warp(D.src_off, D.S, (int)tile0); // the same on every lane
   const int s_last = find_segment_warp(D.src_off, D.S, jl);
-  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u}, mm = 0u;
+  unsigned lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   if (s_first == s_last)
   {
 #pragma unroll
@@ -280,7 +282,6 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       {
         const int p = src_particle(D, s_first, (int)j);
         const float4 x = D.pm[p];
-        mm = max(mm, __float_as_uint(fabsf(source_mass(D, s_first, p))));
         const unsigned v[3] = {float_to_ordered(x.x), float_to_ordered(x.y), float_to_ordered(x.z)};
 #pragma unroll
         for (int d = 0; d < 3; d++)
@@ -297,7 +298,6 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       lo[d] = __reduce_min_sync(0xffffffffu, lo[d]);
       hi[d] = __reduce_max_sync(0xffffffffu, hi[d]);
     }
-    mm = __reduce_max_sync(0xffffffffu, mm);
     if (lane == 0)
     {
 #pragma unroll
@@ -306,10 +306,9 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
         s_red[warp][d] = lo[d];
         s_red[warp][3 + d] = hi[d];
       }
-      s_red[warp][6] = mm;
     }
     __syncthreads();
-    if (threadIdx.x < 7)
+    if (threadIdx.x < 6)
     {
       const int q = threadIdx.x;
       unsigned v = s_red[0][q];
@@ -317,10 +316,8 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
         v = q < 3 ? min(v, s_red[w][q]) : max(v, s_red[w][q]);
       if (q < 3)
         atomicMin(&D.bb_lo[3 * s_first + q], v);
-      else if (q < 6)
+      else
         atomicMax(&D.bb_hi[3 * s_first + q - 3], v);
-      else if (v)
-        atomicMax(&D.bb_m[s_first], v);
     }
     return;
   }
@@ -332,12 +329,11 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
     const int j = (int)jj;
     const int sw = find_segment_warp(D.src_off, D.S, min(j, total - 1));
     const int s = valid ? sw : -1;
-    unsigned l[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, h[3] = {0u, 0u, 0u}, m = 0u;
+    unsigned l[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, h[3] = {0u, 0u, 0u};
     if (valid)
     {
       const int p = src_particle(D, s, j);
       const float4 x = D.pm[p];
-      m = __float_as_uint(fabsf(source_mass(D, s, p)));
       l[0] = h[0] = float_to_ordered(x.x);
       l[1] = h[1] = float_to_ordered(x.y);
       l[2] = h[2] = float_to_ordered(x.z);
@@ -350,7 +346,6 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
       l[d] = __reduce_min_sync(peers, l[d]);
       h[d] = __reduce_max_sync(peers, h[d]);
     }
-    m = __reduce_max_sync(peers, m);
     if (valid && (int)(threadIdx.x & 31) == leader)
     {
 #pragma unroll
@@ -359,8 +354,6 @@ __global__ void __launch_bounds__(256) k_bbox(DevState D, int total)
         atomicMin(&D.bb_lo[3 * s + d], l[d]);
         atomicMax(&D.bb_hi[3 * s + d], h[d]);
       }
-      if (m)
-        atomicMax(&D.bb_m[s], m);
     }
   }
 }
@@ -410,31 +403,6 @@ __global__ void k_root(DevState D, KParams K)
   for (double l = len; l >= (double)K.res && kstar < 1000; l *= 0.5)
     kstar++;
   kp[8] = __int_as_float(kstar);
-  // fixed-point scales of the prefix sums (PrefixLoad): 2^em per mass unit and
-  // 2^ex per mass x length unit.  The subhalo's source mass is below count x
-  // its largest source mass (k_bbox), and offsets from the float origin
-  // kp[0..2] are below side + |origin| 2^-23, so every partial sum of the
-  // subhalo stays below 2^61.
-  const double mtot = (double)D.src_cnt[s] * (double)__uint_as_float(D.bb_m[s]);
-  double omax = 0.;
-  for (int d = 0; d < 3; d++)
-    omax = fmax(omax, fabs((double)kp[d]));
-  const double umax = len + omax * 0x1p-23;
-  int em = 61, ex = 61;
-  if (mtot > 0.)
-  {
-    int e;
-    frexp(mtot, &e); // mtot < 2^e
-    em = 61 - e;
-    ex = em;
-    if (umax > 0.)
-    {
-      frexp(mtot * umax, &e);
-      ex = 61 - e;
-    }
-  }
-  kp[9] = __int_as_float(em);
-  kp[10] = __int_as_float(ex);
   kp[11] = (float)len;
   // first iteration: the sources are every particle (a warm start decides the
   // wrap from every particle before it starts)
@@ -772,37 +740,35 @@ __device__ __forceinline__ void cell_levels(const DevState &D, int j, int i, int
     hi = lcp_levels(k, D.key[j + 1]);
 }
 
+// Also counts the cells of each level (block histogram, then one atomic per
+// level and block) for the per-level lists of k_tree_emit.
 __global__ void k_tree_count(DevState D, int total)
 {
+  __shared__ int hist[kLevels];
+  if (threadIdx.x < kLevels)
+    hist[threadIdx.x] = 0;
+  __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
-  if (j > total)
-    return;
   if (j == total)
-  {
     D.cnt[j] = 0;
-    return;
+  else if (j < total)
+  {
+    const int i = j - D.src_off[s], m = D.src_cnt[s];
+    int lo, hi;
+    cell_levels(D, j, i, m, lo, hi);
+    D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
+    for (int L = lo; L <= hi; L++)
+      atomicAdd(&hist[L], 1);
   }
-  const int i = j - D.src_off[s], m = D.src_cnt[s];
-  int lo, hi;
-  cell_levels(D, j, i, m, lo, hi);
-  D.cnt[j] = hi >= lo ? hi - lo + 1 : 0;
+  __syncthreads();
+  if (threadIdx.x < kLevels && hist[threadIdx.x])
+    atomicAdd(&D.lvl[threadIdx.x], hist[threadIdx.x]);
 }
 
 // 64-bit integer <-> float conversions by exponent and mantissa arithmetic
 // (the hardware's 64-bit conversions issue to the FP64 pipe, whose
 // throughput is low on this GPU).
-
-// Nearest integer to f (ties to even), |f| < 2^62.
-__device__ __forceinline__ long long float_to_ll_rn(float f)
-{
-  const unsigned b = __float_as_uint(f);
-  const int e = (int)((b >> 23) & 0xffu) - 127;
-  if (e < 31)
-    return (long long)__float2int_rn(f);
-  const long long v = (long long)((b & 0x7fffffu) | 0x800000u) << (e - 23);
-  return (b >> 31) ? -v : v;
-}
 
 // v = hi + lo: hi is v rounded to float (to nearest even), lo the remainder
 // rounded to float.  |v| < 2^63.
@@ -835,65 +801,13 @@ __device__ __forceinline__ void ll_to_float2(long long v, float &hi, float &lo)
   lo = v < 0 ? -l : l;
 }
 
-// m x (x - o) in fixed point at scale 2^ex, from FP32 error-free
-// transforms: x - o = u + e exactly (Knuth's TwoSum), m u = p + pe exactly
-// (FMA), and m e, whose rounding is 2^-24 of a term 2^-24 below the rest.
-__device__ __forceinline__ unsigned long long fixed_moment(float m, float x, float o, int ex)
-{
-  const float u = __fsub_rn(x, o);
-  const float bv = __fsub_rn(u, x);
-  const float av = __fsub_rn(u, bv);
-  const float e = __fsub_rn(__fsub_rn(x, av), __fadd_rn(o, bv));
-  const float p = __fmul_rn(m, u);
-  const float pe = __fmaf_rn(m, u, -p);
-  const float q = __fmul_rn(m, e);
-  return (unsigned long long)float_to_ll_rn(ldexpf(p, ex)) + (unsigned long long)float_to_ll_rn(ldexpf(pe, ex)) +
-         (unsigned long long)float_to_ll_rn(ldexpf(q, ex));
-}
-
-// Item j of the prefix sums behind the cell multipoles (scanned by scan_load
-// straight into D.P): the source mass and mass x offset from the root cube's
-// origin rounded to float (kp[0..2]), in 64-bit fixed point with the
-// subhalo's scales (k_root).  FP32 and integer arithmetic only (FP64
-// throughput is low on this GPU); the items are exact to the fixed-point grid
-// and the sums exact, so k_tree_emit rounds each centre of mass once.
-struct PrefixLoad
-{
-  DevState D;
-  __device__ __forceinline__ I4 operator()(long long j) const
-  {
-    const int p = (int)D.val[j];
-    const int s = D.seg_of[p];
-    const float *kp = D.keyp + 12 * s;
-    const float4 x = D.pm[p];
-    const float m = fabsf(source_mass(D, s, p));
-    const int em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
-    return I4{(unsigned long long)float_to_ll_rn(ldexpf(m, em)), fixed_moment(m, x.x, kp[0], ex),
-              fixed_moment(m, x.y, kp[1], ex), fixed_moment(m, x.z, kp[2], ex)};
-  }
-};
-
-// o + X/M rounded to float once, in FP32 arithmetic (float-float quotient,
-// then Knuth's TwoSum with the origin); X, M given as float-float pairs and
-// scale = 2^(em - ex).
-__device__ __forceinline__ float centre_coord(float o, float xh, float xl, float mh, float ml, float scale)
-{
-  const float q1 = __fdiv_rn(xh, mh);
-  const float ph = __fmul_rn(q1, mh);
-  const float pl = __fmaf_rn(q1, mh, -ph); // q1 mh = ph + pl exactly
-  const float r = __fsub_rn(__fadd_rn(__fsub_rn(__fsub_rn(xh, ph), pl), xl), __fmul_rn(q1, ml));
-  const float q2 = __fdiv_rn(r, mh);
-  const float a = __fmul_rn(q1, scale), b = __fmul_rn(q2, scale);
-  const float s = __fadd_rn(o, a);
-  const float bv = __fsub_rn(s, o);
-  const float e = __fadd_rn(__fsub_rn(o, __fsub_rn(s, bv)), __fsub_rn(a, bv)); // o + a = s + e exactly
-  return __fadd_rn(s, __fadd_rn(e, b));
-}
-
 // One cell: item j's cell at level L (slot `slot`), in segment s ending at
 // seg_end.  Its last item b is found by galloping forward from j over the
-// keys; mass and centre of mass come from the prefix sums over [j, b]
-// (src/gravity_tree.cpp:50-80), each rounded to float once, in FP32.
+// keys; that gives the slot after its subtree (its skip).  The cell's side
+// length follows src/gravity_tree.cpp:38-42 (halved per level until below
+// TreeNodeResolution) and its opening threshold is len^2 / theta^2, both in
+// float as the reference stores them; mass and centre of mass are filled in
+// by k_tree_moments.  Slots: (centre, -threshold), (mass, skip, side, 0).
 __device__ __forceinline__ void emit_cell(const DevState &D, const KParams &K, int j, int s, int seg_end, int L,
                                           int slot)
 {
@@ -927,29 +841,12 @@ __device__ __forceinline__ void emit_cell(const DevState &D, const KParams &K, i
     b = a;
   }
   const float *kp = D.keyp + 12 * s;
-  const int kstar = __float_as_int(kp[8]), em = __float_as_int(kp[9]), ex = __float_as_int(kp[10]);
-  const I4 before = (j > 0) ? D.P[j - 1] : I4{0, 0, 0, 0};
-  const I4 after = D.P[b];
-  const long long qm = (long long)(after.m - before.m);
-  float mh, ml;
-  ll_to_float2(qm, mh, ml);
-  const float mass = ldexpf(mh, -em);
-  const float unit = ldexpf(1.f, em - ex);
-  const long long qx[3] = {(long long)(after.x - before.x), (long long)(after.y - before.y),
-                           (long long)(after.z - before.z)};
-  float c[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++)
-  {
-    float xh, xl;
-    ll_to_float2(qx[d], xh, xl);
-    c[d] = qm > 0 ? centre_coord(kp[d], xh, xl, mh, ml, unit) : kp[d];
-  }
+  const int kstar = __float_as_int(kp[8]);
   const float lenf = ldexpf(kp[11], -min(L, kstar));
-  const float crit = __fdiv_rn(lenf * lenf, K.theta2);
+  const float crit = __fdiv_rn(__fmul_rn(lenf, lenf), K.theta2);
   const int skip = b + 2 * D.X[b] + 2 * D.cnt[b] + 1;
-  D.nodes[slot] = make_float4(c[0], c[1], c[2], __uint_as_float(__float_as_uint(crit) | 0x80000000u));
-  D.nodes[slot + 1] = make_float4(mass, __int_as_float(skip), 0.f, 0.f);
+  D.nodes[slot] = make_float4(0.f, 0.f, 0.f, __uint_as_float(__float_as_uint(crit) | 0x80000000u));
+  D.nodes[slot + 1] = make_float4(0.f, __int_as_float(skip), lenf, 0.f);
 }
 
 // Writes the tree slots in preorder.  Slot index: cell (j, level lo+t) =
@@ -960,7 +857,23 @@ __device__ __forceinline__ void emit_cell(const DevState &D, const KParams &K, i
 // cells do not hold the other lanes.
 __global__ void k_tree_emit(DevState D, KParams K, int total)
 {
+  __shared__ int lvl_off[kLevels]; // first list position of each level's cells
   const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32)
+  {
+    const int c = lane < kLevels ? D.lvl[lane] : 0;
+    int incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+      const int o = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d)
+        incl += o;
+    }
+    if (lane < kLevels)
+      lvl_off[lane] = incl - c;
+  }
+  __syncthreads();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   int lo = 0, c = 0, seg_end = 0, base = 0;
   const int s = find_segment_warp(D.src_off, D.S, min(j, total - 1));
@@ -999,20 +912,90 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
     const int o_incl = __shfl_sync(0xffffffffu, incl, owner), o_c = __shfl_sync(0xffffffffu, c, owner);
     const int o_s = __shfl_sync(0xffffffffu, s, owner), o_lo = __shfl_sync(0xffffffffu, lo, owner);
     const int o_end = __shfl_sync(0xffffffffu, seg_end, owner), o_base = __shfl_sync(0xffffffffu, base, owner);
+    const int t = q - (o_incl - o_c);
+    const int L = q < cells ? o_lo + t : -1;
     if (q < cells)
+      emit_cell(D, K, j - lane + owner, o_s, o_end, L, o_base + 2 * t);
+    // append the cell to its level's list (one atomic per level and warp)
+    const unsigned peers = __match_any_sync(0xffffffffu, L);
+    const int leader = __ffs(peers) - 1;
+    int at = 0;
+    if (L >= 0 && lane == leader)
+      at = atomicAdd(&D.lvl[kLevels + L], __popc(peers));
+    at = __shfl_sync(0xffffffffu, at, leader);
+    if (L >= 0)
+      D.cell_list[lvl_off[L] + at + __popc(peers & ((1u << lane) - 1u))] = o_base + 2 * t;
+  }
+}
+
+// Mass and centre of mass of the cells of level L, from their children
+// (GravityTree_t::UpdateInternalNodes / ProcessNode / FillNodeCenter,
+// src/gravity_tree.cpp:18-80): children in octant order (their slot order),
+// each child's float mass and float position (a leaf) or float centre (a
+// cell) accumulated in double, then stored as float -- the reference's own
+// rounding, so a cell's centre carries its children's roundings as in the
+// reference.  Levels are processed deepest first, one launch per level.
+__global__ void k_tree_moments(DevState D, int L)
+{
+  int off = 0;
+  for (int l = 0; l < L; l++)
+    off += D.lvl[l];
+  const int n = D.lvl[L];
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+  {
+    const int slot = D.cell_list[off + c];
+    const int end = __float_as_int(D.nodes[slot + 1].y);
+    double M = 0., X = 0., Y = 0., Z = 0.;
+    float fx = 0.f, fy = 0.f, fz = 0.f; // first child's position (a massless cell)
+    int ch = slot + 2;
+    while (ch < end)
     {
-      const int t = q - (o_incl - o_c);
-      emit_cell(D, K, j - lane + owner, o_s, o_end, o_lo + t, o_base + 2 * t);
+      const float4 a = D.nodes[ch];
+      float m;
+      int nx;
+      if (slot_is_cell(a.w))
+      {
+        const float2 b = *reinterpret_cast<const float2 *>(&D.nodes[ch + 1]);
+        m = b.x;
+        nx = __float_as_int(b.y);
+      }
+      else
+      {
+        m = a.w;
+        nx = ch + 1;
+      }
+      if (ch == slot + 2)
+      {
+        fx = a.x;
+        fy = a.y;
+        fz = a.z;
+      }
+      const double md = (double)m;
+      M = __dadd_rn(M, md);
+      X = __fma_rn((double)a.x, md, X); // the product is exact in double
+      Y = __fma_rn((double)a.y, md, Y);
+      Z = __fma_rn((double)a.z, md, Z);
+      ch = max(nx, ch + 1); // strictly increasing
     }
+    float *cs = reinterpret_cast<float *>(&D.nodes[slot]);
+    if (M > 0.)
+    {
+      cs[0] = __double2float_rn(__ddiv_rn(X, M));
+      cs[1] = __double2float_rn(__ddiv_rn(Y, M));
+      cs[2] = __double2float_rn(__ddiv_rn(Z, M));
+    }
+    else
+    {
+      cs[0] = fx;
+      cs[1] = fy;
+      cs[2] = fz;
+    }
+    reinterpret_cast<float *>(&D.nodes[slot + 1])[0] = __double2float_rn(M);
   }
 }
 
 // ---------------------------------------------------------------------------
-// Tree walk: one warp evaluates 32 neighbouring targets (key order) of one
-// subhalo; each lane walks the slots for its own target exactly as the
-// reference's stackless walk (open: next slot; accept: interact, jump to the
-// skip slot), so its interaction list is the reference's.  FP32 with
-// Kahan-compensated accumulation.
+// Softened potential kernel of the tree walk (walk.cuh)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ float spline_w(float u)
 {
@@ -1020,136 +1003,6 @@ __device__ __forceinline__ float spline_w(float u)
   return (u < 0.5f) ? -2.8f + u * u * (5.333333333333f + u * u * (6.4f * u - 9.6f))
                     : -3.2f + 0.066666666667f / u +
                         u * u * (10.666666666667f + u * (-16.0f + u * (9.6f - 2.133333333333f * u)));
-}
-
-template <bool Wrap>
-__device__ __forceinline__ void walk_lane(const float4 *__restrict__ T, int root, float4 x, bool valid,
-                                          float self_mass, const KParams &K, float &out, unsigned long long &cnt)
-{
-  float sum = valid ? self_mass / K.soft : 0.f, comp = 0.f;
-  const int end = valid ? __float_as_int(__ldg(&T[root + 1]).y) : root;
-  const float h2 = K.h * K.h;
-  int idx = root;
-  while (idx < end)
-  {
-    const float4 a = __ldg(&T[idx]);
-    float dx = a.x - x.x, dy = a.y - x.y, dz = a.z - x.z;
-    if (Wrap)
-    {
-      dx = nearest_f(dx, K.half, K.box);
-      dy = nearest_f(dy, K.half, K.box);
-      dz = nearest_f(dz, K.half, K.box);
-    }
-    const float r2 = dx * dx + dy * dy + dz * dz;
-    float m;
-    int next;
-    if (slot_is_cell(a.w))
-    {
-      if (r2 < -a.w) // open: the first child follows the cell's two slots
-      {
-        idx += 2;
-        continue;
-      }
-      const float2 b = __ldg(reinterpret_cast<const float2 *>(&T[idx + 1]));
-      m = b.x;
-      next = __float_as_int(b.y);
-    }
-    else
-    {
-      m = a.w;
-      next = idx + 1;
-    }
-    float term;
-    if (r2 >= h2)
-      term = -m * rsqrtf(r2);
-    else
-      term = m * K.h_inv * spline_w(sqrtf(r2) * K.h_inv);
-    const float y = term - comp;
-    const float t = sum + y;
-    comp = (t - sum) - y;
-    sum = t;
-    cnt++;
-    idx = max(next, idx + 1); // strictly increasing
-  }
-  out = sum - comp;
-}
-
-// One 32-target chunk of the walk (a warp).
-template <bool Count>
-__device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, int c, int lane,
-                                           unsigned long long &cnt)
-{
-  const int s = find_segment_warp(D.chunk_off, D.S, c); // c is the same on every lane
-  const int t = (c - D.chunk_off[s]) * kWarp + lane;
-  const bool valid = t < D.tgt_cnt[s];
-  const bool corr = D.corr[s] != 0;
-  const int ngrav = D.ngrav[s];
-  int p = 0;
-  if (valid) // correction: key-ordered bound set; subsampled: every candidate; else the sources
-    p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
-  const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-  // self term: only targets that are tree sources (with their upscaled mass)
-  const int nself = (corr && D.self_cnt) ? D.self_cnt[s] : 0;
-  const float self =
-    !valid ? 0.f : (corr ? (t < nself ? x.w : 0.f) : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w));
-  const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
-  float phi = 0.f;
-  if (D.src_cnt[s] == 0) // no sources this iteration: zero potential
-    ;
-  else if (D.wrap[s])
-    walk_lane<true>(D.nodes, root, x, valid, self, K, phi, cnt);
-  else
-    walk_lane<false>(D.nodes, root, x, valid, self, K, phi, cnt);
-  if (valid)
-    D.pot[p] = phi * K.G_over_a;
-}
-
-// With walk counters, the chunks (key order) are split into `nranges`
-// contiguous ranges, one per SM: the warps resident on an SM take the chunks
-// of their own range in order, so they walk neighbouring targets and share
-// the tree slots in L1; a warp whose range is used up moves on to the next
-// ranges (each tried once).  Without counters, a grid-stride loop.
-template <bool Count>
-__global__ void __launch_bounds__(256) k_walk(DevState D, KParams K, int total_chunks, int nranges)
-{
-  const int lane = threadIdx.x & 31;
-  unsigned long long cnt = 0;
-  if (D.walk_ctr)
-  {
-    unsigned smid;
-    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    const int per = (total_chunks + nranges - 1) / nranges;
-    int r = (int)(smid % (unsigned)nranges);
-    for (int tries = 0; tries < nranges;)
-    {
-      int got = 0;
-      if (lane == 0)
-        got = (int)atomicAdd(&D.walk_ctr[r], 1u);
-      got = __shfl_sync(0xffffffffu, got, 0);
-      const long long c = (long long)r * per + got;
-      if (got >= per || c >= total_chunks)
-      {
-        r = (r + 1 == nranges) ? 0 : r + 1;
-        tries++;
-        continue;
-      }
-      walk_chunk<Count>(D, K, (int)c, lane, cnt);
-    }
-  }
-  else
-  {
-    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int c = warp_global; c < total_chunks; c += nwarps)
-      walk_chunk<Count>(D, K, c, lane, cnt);
-  }
-  if (Count)
-  {
-    for (int o = 16; o > 0; o >>= 1)
-      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if (lane == 0)
-      atomicAdd(D.interactions, cnt);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1348,7 +1201,6 @@ __global__ void k_plan_refine(DevState D, KParams K)
   // a fresh bounding box for the prefix's own tree (k_bbox, k_root)
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
-  D.bb_m[s] = 0u;
 }
 
 __global__ void k_refine_keys(DevState D, KParams K, int total)

@@ -60,7 +60,7 @@ constexpr size_t kN1 = (size_t)kNoAllocMaxParticles + 1;
 constexpr size_t kS1 = (size_t)kNoAllocMaxSubhaloes + 1;
 constexpr size_t kTable = (size_t)256 * ((kNoAllocMaxParticles + kRadixTile - 1) / kRadixTile);
 constexpr size_t kScanScr = 2 * (kN1 + kTable) / 64 + 4096; // > scan_scratch_elems<int> of any scan here
-constexpr size_t kPScr = 2 * kN1 / 256 + 256;               // > scan_scratch_elems<I4>(N)
+constexpr size_t kCells = (size_t)kNoAllocMaxRecords / 2 + 1; // cells of a tree within the record limit
 constexpr size_t kScratchBytes =
   al(sizeof(long long) * kS1) +              // offsets
   2 * al(sizeof(float4) * kN1) +             // pm, vu
@@ -80,11 +80,11 @@ constexpr size_t kScratchBytes =
   6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
   al(sizeof(int) * kN1) + al(sizeof(int)) +  // key fallback list and its count
   4 * al(sizeof(int) * kN1) +                // cnt, X, flags, F
-  al(sizeof(I4) * kN1) +                     // prefix sums
   al(sizeof(float4) * kNoAllocMaxRecords) +  // tree slots
   al(sizeof(int) * kTable) +                 // radix table
   al(sizeof(int) * kScanScr) +               // scan scratch
-  al(sizeof(I4) * kPScr) +                   // prefix-sum scan scratch
+  al(sizeof(int) * kCells) +                 // per-level cell lists
+  al(sizeof(int) * 2 * kLevels) +            // cells per level, list cursors
   al(sizeof(unsigned long long)) +           // interaction counter
   al(sizeof(float) * 12 * kS1) +             // working copies of the in/out frames
   al(sizeof(unsigned) * kMaxWalkRanges);     // per-SM walk chunk counters
@@ -146,7 +146,7 @@ inline unsigned nblocks(long long n, int threads)
 struct StaticMem
 {
   int *scan_scr = nullptr, *table = nullptr;
-  I4 *p_scr = nullptr;
+  int *cells = nullptr, *lvl = nullptr;
   float4 *slots = nullptr;
 
   void check(cudaError_t e) { ck(e); }
@@ -163,12 +163,13 @@ struct StaticMem
     return table;
   }
   int *radix_scan_scratch(long long n) { return scan_scratch(radix_table_elems(std::max<long long>(n, 1)) + 1); }
-  I4 *prefix_scratch(long long n)
+  int *cell_list(long long n)
   {
-    if (scan_scratch_elems<I4>(n) > kPScr)
+    if (n > (long long)kCells)
       throw Fail{HBTG_ERR_NOMEM};
-    return p_scr;
+    return cells;
   }
+  int *level_counts() { return lvl; }
   float4 *tree_slots(long long n)
   {
     if (n > kNoAllocMaxRecords)
@@ -288,7 +289,6 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   unsigned *bb = c.take<unsigned>(7 * kS1);
   D.bb_lo = bb;
   D.bb_hi = bb ? bb + 3 * kS1 : nullptr;
-  D.bb_m = bb ? bb + 6 * kS1 : nullptr;
   D.factor = c.take<float>(6 * kS1);
   D.root = c.take<double>(4 * kS1);
   D.keyp = c.take<float>(12 * kS1);
@@ -309,17 +309,16 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.X = c.take<int>(kN1);
   D.flags = c.take<int>(kN1);
   D.F = c.take<int>(kN1);
-  D.P = c.take<I4>(kN1);
   mem.slots = c.take<float4>(kNoAllocMaxRecords);
   D.nodes = mem.slots;
   mem.table = c.take<int>(kTable);
   mem.scan_scr = c.take<int>(kScanScr);
-  mem.p_scr = c.take<I4>(kPScr);
+  mem.cells = c.take<int>(kCells);
+  mem.lvl = c.take<int>(2 * kLevels);
   D.interactions = c.take<unsigned long long>(1);
   float *frames = c.take<float>(12 * kS1);
   D.walk_ctr = c.take<unsigned>(kMaxWalkRanges);
-  if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr ||
-      (size_t)scan_scratch_elems<I4>(kN1) > kPScr)
+  if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr)
     return HBTG_ERR_NOMEM; // layout does not fit the reserve (cannot happen with the constants above)
   // the iteration moves the frames: it works on copies in the reserve
   D.ref_pos = frames;

@@ -65,7 +65,6 @@ __global__ void k_pot_plan(DevState D, int n_tgt, int phase)
       D.bb_lo[d] = 0xffffffffu;
       D.bb_hi[d] = 0u;
     }
-    D.bb_m[0] = 0u;
     for (int t = 0; t < 6; t++)
       D.factor[t] = 1.f;
   }
@@ -132,8 +131,8 @@ enum Slot
   S_ORDER, S_NB, S_MB, S_NBT, S_MBT, S_TI, S_KIN, S_CORE, S_EN, S_POT, S_ITER, S_STAT,
   S_PM, S_VU, S_TY, S_SEG, S_ORD, S_ORDT, S_EP, S_PHI,
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
-  S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F, S_P,
-  S_NODES, S_TABLE, S_SCRATCH, S_PSCR, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
+  S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F,
+  S_NODES, S_TABLE, S_SCRATCH, S_CELLS, S_LVL, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
   S_POTI, S_WCTR, S_FRAMEW,
   S_NUM
@@ -310,10 +309,8 @@ struct PoolMem
                                          std::max<long long>(radix_table_elems(std::max<long long>(n, 1)) + 1,
                                                              256LL * 4096)));
   }
-  I4 *prefix_scratch(long long n)
-  {
-    return H->pool.get<I4>(S_PSCR, scan_scratch_elems<I4>(std::max<long long>(n, 1)));
-  }
+  int *cell_list(long long cells) { return H->pool.get<int>(S_CELLS, (size_t)std::max<long long>(cells, 1)); }
+  int *level_counts() { return H->pool.get<int>(S_LVL, 2 * kLevels); }
   float4 *tree_slots(long long slots)
   {
     if (slots >= (1LL << 31) - 64)
@@ -429,7 +426,6 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   unsigned *bb = P.get<unsigned>(S_BB, (size_t)S * 7);
   D.bb_lo = bb;
   D.bb_hi = bb + 3 * (size_t)S;
-  D.bb_m = bb + 6 * (size_t)S;
   D.root = P.get<double>(S_ROOT, (size_t)S * 4);
   D.keyp = P.get<float>(S_KEYP, (size_t)S * 12);
   D.com = P.get<double>(S_COM, (size_t)S * 7);
@@ -449,7 +445,6 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.X = P.get<int>(S_X, n1 + 1);
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
   D.F = P.get<int>(S_F, n1 + 1);
-  D.P = P.get<I4>(S_P, n1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
@@ -575,6 +570,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   H->stats.ms_total = ms;
   H->stats.kernel_launches = R.launches;
   H->stats.walk_launches = R.walk_launches;
+  H->stats.walk_blocks_per_sm = R.walk_blocks_per_sm;
   H->stats.global_iterations = R.global_iter;
   H->stats.tree_nodes = R.tree_nodes;
   if (H->count_interactions)
@@ -791,7 +787,6 @@ int pot_call(void *arg)
   unsigned *bb = P.get<unsigned>(S_BB, 7);
   D.bb_lo = bb;
   D.bb_hi = bb + 3;
-  D.bb_m = bb + 6;
   D.root = P.get<double>(S_ROOT, 4);
   D.keyp = P.get<float>(S_KEYP, 12);
   D.key = P.get<unsigned long long>(S_KEY, n1);
@@ -806,7 +801,6 @@ int pot_call(void *arg)
   D.fb_count = P.get<int>(S_FBC, 1);
   D.cnt = P.get<int>(S_CNT, n1 + 1);
   D.X = P.get<int>(S_X, n1 + 1);
-  D.P = P.get<I4>(S_P, n1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
   D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
   D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));

@@ -1,0 +1,485 @@
+// walk.cuh - the tree walk (GravityTree_t::EvaluatePotential,
+// src/gravity_tree.cpp:82-166) for 32 targets at a time.
+//
+// One warp takes 32 neighbouring targets (key order) of one subhalo.  Each
+// target's interaction list is exactly the reference's: the cells its own
+// opening test accepts and the leaves it reaches.  The warp finds the union
+// of those lists in one traversal and evaluates it in a second phase:
+//
+//   traversal   A stack in shared memory holds ranges of sibling subtrees
+//               (first slot, end slot, the targets still walking them).  Each
+//               step pops up to 32 ranges, one per lane; a lane reads its
+//               range's first node and classifies it against the bounding
+//               box of the targets: every target accepts it, every target
+//               opens it, or (near the opening distance) each target decides
+//               with its own test.  The node becomes an entry of the
+//               interaction list with the mask of the targets that accept it;
+//               the rest of the range and, if some targets open the node, its
+//               children (with the mask of those targets) go back on the stack.
+//   evaluation  Entries go to one of two lists: "far" entries, which every
+//               target sees beyond the softening length (box distance), and
+//               "near" ones.  Whenever a list fills, every lane reads each
+//               entry (a shared-memory broadcast) and adds the term of the
+//               entries its mask bit selects: -m / r for the far list with no
+//               branch, the cubic-spline softened kernel where r < h for the
+//               near list.  Lists are padded to a multiple of eight with
+//               massless entries; blocks of eight terms are summed in FP32
+//               and Kahan-added to the potential.
+//
+// Opening test.  The reference opens a cell when len^2 > r^2 theta^2, with
+// len^2 in float and r^2 in double from the float coordinates
+// (src/gravity_tree.cpp:137-145).  Here r^2 is FP32; outside a band of 1e-6
+// relative around the stored threshold len^2 / theta^2 (far wider than the
+// FP32 error of r^2 and of the threshold) the FP32 comparison decides as the
+// reference does, and inside the band the reference's double arithmetic
+// decides.  The bounding-box classifications use the same band, and the box
+// distances are computed with the same monotonic FP32 operations as each
+// target's own r^2, so "every target accepts" and "every target opens" never
+// disagree with a target's own test.
+//
+// Bounds.  Stack pushes happen only in steps that start with at most
+// kWalkStack - 64 ranges (a step pops k <= 32 ranges and pushes at most 2k);
+// above that the warp drains the stack one range at a time, each target
+// walking that range on its own with the reference's stackless walk (no
+// pushes).  A list holding more than its capacity - 40 entries after a step
+// (at most 32 added per step) is evaluated, so with its padding (at most 7)
+// it never exceeds its capacity.  Every loop advances a slot index strictly.
+// A node's second slot is read for leaves too: the tree array carries one
+// padding slot after its last slot.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace hbtg
+{
+namespace
+{
+
+constexpr int kWalkWarps = 4;   // warps per block
+constexpr int kWalkFar = 160;   // far-list entries per warp
+constexpr int kWalkNear = 64;   // near-list entries per warp
+constexpr int kWalkStack = 256; // traversal ranges per warp
+constexpr int kFlushMargin = 40; // a list is evaluated once it holds more than capacity - this
+constexpr float kBandLo = 1.f - 1e-6f, kBandHi = 1.f + 1e-6f;
+
+struct WalkShared
+{
+  float4 far[kWalkWarps][kWalkFar];     // x, y, z, m
+  unsigned fmsk[kWalkWarps][kWalkFar];  // targets (lanes) that interact with the entry
+  float4 near[kWalkWarps][kWalkNear];
+  unsigned nmsk[kWalkWarps][kWalkNear];
+  int ia[kWalkWarps][kWalkStack];       // range: first slot
+  int ie[kWalkWarps][kWalkStack];       //        end slot
+  unsigned im[kWalkWarps][kWalkStack];  //        targets still walking it
+};
+
+// a - b, with the periodic wrap of NEAREST (src/config_parser.h:218-219)
+// formed without rounding the large intermediate a - b +- box: for a wrapped
+// difference, a - box (or b - box) is exact (that operand is above half the
+// box) and the result rounds once.
+template <bool Wrap>
+__device__ __forceinline__ float sep(float a, float b, const KParams &K)
+{
+  const float d = __fsub_rn(a, b);
+  if (!Wrap)
+    return d;
+  return d > K.half ? __fsub_rn(__fsub_rn(a, K.box), b) : (d < -K.half ? __fsub_rn(a, __fsub_rn(b, K.box)) : d);
+}
+
+__device__ __forceinline__ float dist2(float dx, float dy, float dz)
+{
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// The reference's opening decision in its own arithmetic: float len^2
+// against r^2 theta^2 in double, r^2 from the float coordinates.
+template <bool Wrap>
+__device__ __noinline__ bool opens_exact(float cx, float cy, float cz, float lenf, float tx, float ty, float tz,
+                                         const KParams &K)
+{
+  double d[3] = {(double)cx - (double)tx, (double)cy - (double)ty, (double)cz - (double)tz}; // exact
+  if (K.periodic)
+    for (int q = 0; q < 3; q++)
+      d[q] = nearest_d(d[q], (double)K.half, (double)K.box);
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(d[0], d[0]), __dmul_rn(d[1], d[1])), __dmul_rn(d[2], d[2]));
+  return (double)__fmul_rn(lenf, lenf) > __dmul_rn(r2, (double)K.theta2);
+}
+
+// One target's test of a cell (centre c, threshold crit = len^2/theta^2).
+template <bool Wrap>
+__device__ __forceinline__ bool target_opens(float cx, float cy, float cz, float crit, float lenf, float tx, float ty,
+                                             float tz, const KParams &K)
+{
+  const float r2 = dist2(sep<Wrap>(cx, tx, K), sep<Wrap>(cy, ty, K), sep<Wrap>(cz, tz, K));
+  if (r2 < __fmul_rn(crit, kBandLo))
+    return true;
+  if (r2 > __fmul_rn(crit, kBandHi))
+    return false;
+  return opens_exact<Wrap>(cx, cy, cz, lenf, tx, ty, tz, K);
+}
+
+// The potential term of one entry for one target at squared distance r2.
+__device__ __forceinline__ float softened_term(float m, float r2, const KParams &K, float h2)
+{
+  return r2 >= h2 ? -m * rsqrtf(r2) : m * K.h_inv * spline_w(sqrtf(r2) * K.h_inv);
+}
+
+__device__ __forceinline__ void kahan_add(float &sum, float &comp, float v)
+{
+  const float y = v - comp;
+  const float t = sum + y;
+  comp = (t - sum) - y;
+  sum = t;
+}
+
+// Pads a list to a multiple of eight with massless entries far from every
+// target (finite terms, so the evaluation loops need no guard); returns the
+// padded length.  The caller leaves room for seven more entries.
+__device__ __forceinline__ int pad8(float4 *ent, unsigned *msk, int n, int lane)
+{
+  const int padded = (n + 7) & ~7;
+  if (n + lane < padded)
+  {
+    ent[n + lane] = make_float4(3e18f, 3e18f, 3e18f, 0.f);
+    msk[n + lane] = 0u;
+  }
+  __syncwarp();
+  return padded;
+}
+
+// Far list: every target is at least one softening length from every entry.
+template <bool Wrap>
+__device__ __forceinline__ void eval_far(const float4 *ent, const unsigned *msk, int n, unsigned lanebit, float tx,
+                                         float ty, float tz, const KParams &K, float &sum, float &comp)
+{
+  for (int i = 0; i < n; i += 8)
+  {
+    float p0 = 0.f, p1 = 0.f;
+#pragma unroll
+    for (int u = 0; u < 8; u++)
+    {
+      const float4 e = ent[i + u];
+      const float m = (msk[i + u] & lanebit) ? e.w : 0.f;
+      const float r2 = dist2(sep<Wrap>(e.x, tx, K), sep<Wrap>(e.y, ty, K), sep<Wrap>(e.z, tz, K));
+      if (u & 1)
+        p1 = __fmaf_rn(-m, rsqrtf(r2), p1);
+      else
+        p0 = __fmaf_rn(-m, rsqrtf(r2), p0);
+    }
+    kahan_add(sum, comp, p0 + p1);
+  }
+}
+
+// Near list: the softened kernel where r < h (src/gravity_tree.cpp:150-162).
+template <bool Wrap>
+__device__ __forceinline__ void eval_near(const float4 *ent, const unsigned *msk, int n, unsigned lanebit, float tx,
+                                          float ty, float tz, const KParams &K, float h2, float &sum, float &comp)
+{
+  for (int i = 0; i < n; i += 8)
+  {
+    float part = 0.f;
+#pragma unroll 2
+    for (int u = 0; u < 8; u++)
+    {
+      const float4 e = ent[i + u];
+      const float m = (msk[i + u] & lanebit) ? e.w : 0.f;
+      const float r2 = dist2(sep<Wrap>(e.x, tx, K), sep<Wrap>(e.y, ty, K), sep<Wrap>(e.z, tz, K));
+      part += softened_term(m, r2, K, h2);
+    }
+    kahan_add(sum, comp, part);
+  }
+}
+
+// The reference's stackless walk of one range [a, e) of sibling subtrees for
+// one target (open: next slot; accept: interact and skip the subtree).
+template <bool Wrap>
+__device__ __forceinline__ void walk_range(const float4 *__restrict__ T, int a, int e, float tx, float ty, float tz,
+                                           const KParams &K, float h2, float &sum, float &comp,
+                                           unsigned long long &cnt)
+{
+  int idx = a;
+  while (idx < e)
+  {
+    const float4 n = __ldg(&T[idx]);
+    float m;
+    int next;
+    if (slot_is_cell(n.w))
+    {
+      const float4 b = __ldg(&T[idx + 1]);
+      const float crit = __uint_as_float(__float_as_uint(n.w) & 0x7fffffffu);
+      if (target_opens<Wrap>(n.x, n.y, n.z, crit, b.z, tx, ty, tz, K))
+      {
+        idx += 2;
+        continue;
+      }
+      m = b.x;
+      next = __float_as_int(b.y);
+    }
+    else
+    {
+      m = n.w;
+      next = idx + 1;
+    }
+    const float r2 = dist2(sep<Wrap>(n.x, tx, K), sep<Wrap>(n.y, ty, K), sep<Wrap>(n.z, tz, K));
+    kahan_add(sum, comp, softened_term(m, r2, K, h2));
+    cnt++;
+    idx = max(next, idx + 1);
+  }
+}
+
+// Potentials of the (up to) 32 targets of chunk c.
+template <bool Wrap, bool Count>
+__device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, int s, int root, int lane, bool valid,
+                                           int p, float4 x, float self, WalkShared &sh, int w,
+                                           unsigned long long &cnt)
+{
+  const float4 *__restrict__ T = D.nodes;
+  float4 *far = sh.far[w], *nea = sh.near[w];
+  unsigned *fmsk = sh.fmsk[w], *nmsk = sh.nmsk[w];
+  int *ia = sh.ia[w], *ie = sh.ie[w];
+  unsigned *im = sh.im[w];
+  const unsigned full = 0xffffffffu, lanebit = 1u << lane, below = lanebit - 1u;
+  const float h2 = K.h * K.h;
+  const unsigned vmask = __ballot_sync(full, valid);
+  // bounding box of the targets
+  float lo[3] = {valid ? x.x : INFINITY, valid ? x.y : INFINITY, valid ? x.z : INFINITY};
+  float hi[3] = {valid ? x.x : -INFINITY, valid ? x.y : -INFINITY, valid ? x.z : -INFINITY};
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+    {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(full, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(full, hi[d], o));
+    }
+  float sum = valid ? self / K.soft : 0.f, comp = 0.f;
+  const int root_end = __float_as_int(__ldg(&T[root + 1]).y);
+  if (lane == 0)
+  {
+    ia[0] = root;
+    ie[0] = root_end;
+    im[0] = vmask;
+  }
+  int sp = 1, nf = 0, nn = 0;
+  __syncwarp();
+  while (sp > 0)
+  {
+    if (sp > kWalkStack - 64)
+    { // drain: each target walks the top range on its own
+      sp--;
+      const int a = ia[sp], e = ie[sp];
+      const unsigned m = im[sp];
+      __syncwarp();
+      if (m & lanebit)
+        walk_range<Wrap>(T, a, e, x.x, x.y, x.z, K, h2, sum, comp, cnt);
+      continue;
+    }
+    const int k = min(sp, 32);
+    const int base = sp - k;
+    const bool act = lane < k;
+    int a = 0, e = 0;
+    unsigned m = 0u;
+    if (act)
+    {
+      a = ia[base + lane];
+      e = ie[base + lane];
+      m = im[base + lane];
+    }
+    sp = base;
+    __syncwarp();
+    float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool cell = false, near = true;
+    int cls = 0; // 0: every target accepts, 1: every target opens, 2: each target decides
+    if (act)
+    {
+      na = __ldg(&T[a]);
+      nb = __ldg(&T[a + 1]); // a cell's mass, skip and side length (the tree has a padding slot)
+      cell = slot_is_cell(na.w);
+      if (Wrap)
+        cls = cell ? 2 : 0;
+      else
+      {
+        const float g[3] = {fmaxf(fmaxf(__fsub_rn(lo[0], na.x), __fsub_rn(na.x, hi[0])), 0.f),
+                            fmaxf(fmaxf(__fsub_rn(lo[1], na.y), __fsub_rn(na.y, hi[1])), 0.f),
+                            fmaxf(fmaxf(__fsub_rn(lo[2], na.z), __fsub_rn(na.z, hi[2])), 0.f)};
+        const float rmin2 = dist2(g[0], g[1], g[2]);
+        near = rmin2 < h2;
+        if (cell)
+        {
+          const float crit = __uint_as_float(__float_as_uint(na.w) & 0x7fffffffu);
+          if (!(rmin2 > __fmul_rn(crit, kBandHi)))
+          {
+            const float G[3] = {fmaxf(fabsf(__fsub_rn(na.x, lo[0])), fabsf(__fsub_rn(na.x, hi[0]))),
+                                fmaxf(fabsf(__fsub_rn(na.y, lo[1])), fabsf(__fsub_rn(na.y, hi[1]))),
+                                fmaxf(fabsf(__fsub_rn(na.z, lo[2])), fabsf(__fsub_rn(na.z, hi[2])))};
+            cls = dist2(G[0], G[1], G[2]) < __fmul_rn(crit, kBandLo) ? 1 : 2;
+          }
+        }
+      }
+    }
+    unsigned A = cls == 0 ? m : 0u, O = cls == 1 ? m : 0u;
+    // the targets decide the nodes near their opening distance, one node at a time
+    unsigned mix = __ballot_sync(full, act && cls == 2);
+    while (mix)
+    {
+      const int j = __ffs(mix) - 1;
+      mix &= mix - 1u;
+      const float cx = __shfl_sync(full, na.x, j), cy = __shfl_sync(full, na.y, j), cz = __shfl_sync(full, na.z, j);
+      const float cw = __shfl_sync(full, na.w, j), cl = __shfl_sync(full, nb.z, j);
+      const unsigned mj = __shfl_sync(full, m, j);
+      bool op = false;
+      if (mj & lanebit)
+        op = target_opens<Wrap>(cx, cy, cz, __uint_as_float(__float_as_uint(cw) & 0x7fffffffu), cl, x.x, x.y, x.z, K);
+      const unsigned oj = __ballot_sync(full, op);
+      if (lane == j)
+      {
+        O = oj;
+        A = mj & ~oj;
+      }
+    }
+    const int next = cell ? __float_as_int(nb.y) : a + 1;
+    const bool has_e = act && A != 0u, has_sib = act && next < e, has_kid = act && O != 0u;
+    const bool to_near = Wrap || near;
+    const unsigned bf = __ballot_sync(full, has_e && !to_near), bn = __ballot_sync(full, has_e && to_near),
+                   bs = __ballot_sync(full, has_sib), bk = __ballot_sync(full, has_kid);
+    if (has_e)
+    {
+      const float4 en = make_float4(na.x, na.y, na.z, cell ? nb.x : na.w);
+      if (to_near)
+      {
+        const int at = nn + __popc(bn & below);
+        nea[at] = en;
+        nmsk[at] = A;
+      }
+      else
+      {
+        const int at = nf + __popc(bf & below);
+        far[at] = en;
+        fmsk[at] = A;
+      }
+      if (Count)
+        cnt += __popc(A);
+    }
+    nf += __popc(bf);
+    nn += __popc(bn);
+    // the rest of each range, then the children of opened cells (popped first: depth first)
+    if (has_sib)
+    {
+      const int at = sp + __popc(bs & below);
+      ia[at] = next;
+      ie[at] = e;
+      im[at] = m;
+    }
+    sp += __popc(bs);
+    if (has_kid)
+    {
+      const int at = sp + __popc(bk & below);
+      ia[at] = a + 2;
+      ie[at] = next;
+      im[at] = O;
+    }
+    sp += __popc(bk);
+    __syncwarp();
+    if (nf > kWalkFar - kFlushMargin)
+    {
+      eval_far<Wrap>(far, fmsk, pad8(far, fmsk, nf, lane), lanebit, x.x, x.y, x.z, K, sum, comp);
+      nf = 0;
+      __syncwarp();
+    }
+    if (nn > kWalkNear - kFlushMargin)
+    {
+      eval_near<Wrap>(nea, nmsk, pad8(nea, nmsk, nn, lane), lanebit, x.x, x.y, x.z, K, h2, sum, comp);
+      nn = 0;
+      __syncwarp();
+    }
+  }
+  eval_far<Wrap>(far, fmsk, pad8(far, fmsk, nf, lane), lanebit, x.x, x.y, x.z, K, sum, comp);
+  eval_near<Wrap>(nea, nmsk, pad8(nea, nmsk, nn, lane), lanebit, x.x, x.y, x.z, K, h2, sum, comp);
+  __syncwarp();
+  if (valid)
+    D.pot[p] = (sum - comp) * K.G_over_a;
+}
+
+// One 32-target chunk: its subhalo, targets and self terms (as the
+// reference: a target that is a tree source starts from +m/soft, cancelling
+// its own leaf, src/gravity_tree.cpp:98-101).
+template <bool Count>
+__device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, int c, int lane, WalkShared &sh,
+                                           int w, unsigned long long &cnt)
+{
+  const int s = find_segment_warp(D.chunk_off, D.S, c); // c is the same on every lane
+  const int t = (c - D.chunk_off[s]) * kWarp + lane;
+  const bool valid = t < D.tgt_cnt[s];
+  const bool corr = D.corr[s] != 0;
+  const int ngrav = D.ngrav[s];
+  int p = 0;
+  if (valid) // correction: key-ordered bound set; subsampled: every candidate; else the sources
+    p = corr ? D.tgt[D.off[s] + t] : (ngrav ? D.ord[D.off[s] + t] : (int)D.val[D.src_off[s] + t]);
+  const float4 x = valid ? D.pm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int nself = (corr && D.self_cnt) ? D.self_cnt[s] : 0;
+  const float self =
+    !valid ? 0.f : (corr ? (t < nself ? x.w : 0.f) : (ngrav ? (t < ngrav ? source_mass(D, s, p) : 0.f) : x.w));
+  if (D.src_cnt[s] == 0)
+  { // no sources this iteration: zero potential
+    if (valid)
+      D.pot[p] = 0.f;
+    return;
+  }
+  const int root = D.src_off[s] + 2 * D.X[D.src_off[s]];
+  if (D.wrap[s])
+    walk_group<true, Count>(D, K, s, root, lane, valid, p, x, self, sh, w, cnt);
+  else
+    walk_group<false, Count>(D, K, s, root, lane, valid, p, x, self, sh, w, cnt);
+}
+
+// With walk counters, the chunks (key order) are split into `nranges`
+// contiguous ranges, one per SM: the warps resident on an SM take the chunks
+// of their own range in order, so they walk neighbouring targets and share
+// the tree slots in L1; a warp whose range is used up moves on to the next
+// ranges (each tried once).  Without counters, a grid-stride loop.
+template <bool Count>
+__global__ void __launch_bounds__(32 * kWalkWarps) k_walk(DevState D, KParams K, int total_chunks, int nranges)
+{
+  __shared__ WalkShared sh;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned long long cnt = 0;
+  if (D.walk_ctr)
+  {
+    unsigned smid;
+    asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
+    const int per = (total_chunks + nranges - 1) / nranges;
+    int r = (int)(smid % (unsigned)nranges);
+    for (int tries = 0; tries < nranges;)
+    {
+      int got = 0;
+      if (lane == 0)
+        got = (int)atomicAdd(&D.walk_ctr[r], 1u);
+      got = __shfl_sync(0xffffffffu, got, 0);
+      const long long c = (long long)r * per + got;
+      if (got >= per || c >= total_chunks)
+      {
+        r = (r + 1 == nranges) ? 0 : r + 1;
+        tries++;
+        continue;
+      }
+      walk_chunk<Count>(D, K, (int)c, lane, sh, w, cnt);
+    }
+  }
+  else
+  {
+    const int warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int c = warp_global; c < total_chunks; c += nwarps)
+      walk_chunk<Count>(D, K, c, lane, sh, w, cnt);
+  }
+  if (Count)
+  {
+    for (int o = 16; o > 0; o >>= 1)
+      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if (lane == 0)
+      atomicAdd(D.interactions, cnt);
+  }
+}
+
+} // namespace
+} // namespace hbtg

@@ -504,7 +504,6 @@ __global__ void k_plan_first(DevState D)
   D.tail_cnt[s] = ne;
   D.bb_lo[3 * s] = D.bb_lo[3 * s + 1] = D.bb_lo[3 * s + 2] = 0xffffffffu;
   D.bb_hi[3 * s] = D.bb_hi[3 * s + 1] = D.bb_hi[3 * s + 2] = 0u;
-  D.bb_m[s] = 0u;
 }
 
 // Targets of the first test in the tree's key order: the sources (packed by

@@ -151,6 +151,7 @@ typedef struct hbtg_stats
   int64_t readmitted;         /* untrusted particles the first test kept */
   int64_t cold_restarts;      /* warm subhaloes restarted cold (their first iteration converges) */
   int64_t readmit_rounds;     /* first tests run (lock-step) */
+  int64_t walk_blocks_per_sm; /* resident tree-walk blocks per SM of the last call's launches */
 } hbtg_stats;
 
 typedef struct hbtg_handle hbtg_handle;

@@ -163,6 +163,13 @@ def check_invariants(inp, out, sorted_energies=True):
 #   * tracer index, most-bound ID and position/velocity  identical (the
 #                      most-bound ID up to an energy tie, as above)
 #   * iterations       identical
+# Particles near a pair closer than TreeNodeResolution are exempt from the
+# energy, potential and order bars (not from membership, mass or IDs): when
+# two particles share a cell smaller than the resolution the reference places
+# one of them in a child drawn with drand48 (src/oct_tree.tpp:108-120), where
+# the GPU keeps their geometric order.  Only targets that open such a cell
+# (within len / theta of it, a few resolution lengths) see a different tree;
+# the exemption covers everything within SUBRES_REACH resolution lengths.
 # Over the whole batch: membership <= MEMBERSHIP_TOL and the raw total bound
 # mass within MASS_TOL.
 # ---------------------------------------------------------------------------
@@ -170,6 +177,7 @@ FLOAT_REL = 1e-5
 FLOAT_OUTLIER_FRAC = 1e-3
 TAIL_WINDOW = 8
 SOURCE_RELAX = 3.0  # SourceSubRelaxFactor default (src/config_parser.cpp)
+SUBRES_REACH = 10.0  # exemption radius around sub-resolution pairs, in resolution lengths
 
 
 def _ulp32(x):
@@ -196,6 +204,8 @@ def compare_full(inp, got, ref, params, refine=None, box=None):
     viol = []
     base = compare(inp, got, ref)
     ns = inp.n_sub
+    res = float(params.tree_node_resolution)
+    near_ids = subresolution_neighbours(inp, res, SUBRES_REACH * res)
     matched = 0
     tail_moved = 0
     tail_checked = 0
@@ -234,6 +244,8 @@ def compare_full(inp, got, ref, params, refine=None, box=None):
             diff = np.nonzero(ids_g[:nb] != ids_r[:nb])[0]
             for k in diff:
                 other = pos_r[int(ids_g[k])]
+                if int(ids_g[k]) in near_ids or int(ids_r[k]) in near_ids:
+                    continue
                 if abs(e_r[other] - e_r[k]) > ENERGY_TIE_REL * max(escale[k], escale[other]):
                     viol.append(("bound_order", s, (int(k), int(ids_g[k]), int(ids_r[k]))))
                     break
@@ -245,6 +257,8 @@ def compare_full(inp, got, ref, params, refine=None, box=None):
             moved = np.nonzero(tg != tr)[0]
             tail_moved += len(moved)
             for k in moved:
+                if int(tg[k]) in near_ids or int(tr[k]) in near_ids:
+                    continue
                 if abs(where_r[int(tg[k])] - int(k)) > TAIL_WINDOW:
                     viol.append(("tail_order", s, (int(k), int(tg[k]), int(tr[k]))))
                     break
@@ -255,14 +269,15 @@ def compare_full(inp, got, ref, params, refine=None, box=None):
             idx_r = np.argsort(ids_r[:nb])
             idx_g = np.argsort(ids_g[:nb])
             sc = np.maximum(escale[idx_r], 1e-30)
+            keep = ~np.isin(np.sort(ids_r[:nb]), np.fromiter(near_ids, np.int64, len(near_ids)))
             for field in ("energy", "potential"):
                 a, b = getattr(got, field), getattr(ref, field)
                 if a is None or b is None:
                     continue
                 va = a[off:off + nb].astype(np.float64)[idx_g]
                 vb = b[off:off + nb].astype(np.float64)[idx_r]
-                bad = np.abs(va - vb) > FLOAT_REL * sc
-                n_float += nb
+                bad = (np.abs(va - vb) > FLOAT_REL * sc) & keep
+                n_float += int(keep.sum())
                 n_float_bad += int(bad.sum())
         # counts and masses
         if not np.array_equal(got.nbound_type[s], ref.nbound_type[s]):
@@ -314,10 +329,33 @@ def compare_full(inp, got, ref, params, refine=None, box=None):
     if trunc_mism > 10 * MEMBERSHIP_TOL * max(trunc_total, 1):
         viol.append(("truncated_source", -1, (trunc_mism, trunc_total)))
     m = dict(base)
-    m.update(matched=matched, n_sub=ns, tail_moved=tail_moved, tail_checked=tail_checked,
+    m.update(matched=matched, n_sub=ns, subres_exempt=len(near_ids), tail_moved=tail_moved, tail_checked=tail_checked,
              trunc_mismatch=trunc_mism / max(trunc_total, 1), float_outliers=n_float_bad / max(n_float, 1),
              iter_diff=iter_diff)
     return m, viol
+
+
+def subresolution_neighbours(inp, res, reach):
+    """IDs of the particles within `reach` of a particle that has another one
+    closer than `res` in its subhalo (positions as stored: the tree's cube
+    is built on them)."""
+    from scipy.spatial import cKDTree
+    out = set()
+    for s in range(inp.n_sub):
+        off, end = int(inp.offsets[s]), int(inp.offsets[s + 1])
+        if end - off < 2:
+            continue
+        x = np.asarray(inp.pos[off:end], np.float64)
+        tree = cKDTree(x)
+        pairs = tree.query_pairs(r=res, output_type="ndarray")
+        if not len(pairs):
+            continue
+        members = np.unique(pairs.ravel())
+        hit = set()
+        for lst in tree.query_ball_point(x[members], r=reach):
+            hit.update(lst)
+        out.update(int(i) for i in inp.id[off + np.fromiter(hit, np.int64, len(hit))])
+    return out
 
 
 def _tracer_mask(inp, params, off, end):

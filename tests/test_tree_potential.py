@@ -88,7 +88,9 @@ def test_periodic_wrap_across_box_faces(unbinder, x):
     pos = np.array([[x0, 10.0, 10.0], [x, 10.0, 10.0]], np.float32)
     mass = np.array([1.0, 1.0], np.float32)
     got = unbinder.tree_potential(prm, pos, mass, [0])[0]
-    dx = float(np.float32(x) - np.float32(x0))
+    # the reference subtracts the float coordinates in double, then wraps
+    # (src/gravity_tree.cpp:122-127)
+    dx = float(np.float32(x)) - float(np.float32(x0))
     half = 50.0
     dx = dx - 100.0 if dx > half else (dx + 100.0 if dx < -half else dx)
     tol = 3 * self_term_ulp(1.0, prm.softening)
