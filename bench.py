@@ -46,6 +46,8 @@ WORKLOADS = {
                "f_unbound~U(0,0.5) heated to 1.5-4 v_esc, 500-unit periodic box",
     "stripped": "learned warm start evaluation: %d held-out tidally stripped NFW subhaloes (N_p~N^-1.9 on "
                 "[20,1e6]) with a previous-output bound set, 500-unit periodic box",
+    "hydro": "hydro mixed species: %.0e particles over subhaloes of N_p~N^-1.9 on [100,2e5] (55%% DM, 35%% gas with "
+             "thermal energy and 0.3 v_circ rotation, 9.9%% Hernquist stars, 0.1%% BH m=50), 500-unit periodic box",
 }
 
 
@@ -53,36 +55,109 @@ def workload(total, seed, kind="batched"):
     from hbtg import abi, synthetic
     if kind == "stripped":
         inp = synthetic.stripped(n_sub=int(total), seed=424242 + seed)  # seeds disjoint from the training traces
+        prm = abi.parity_params(dm_only=1, box_size=500.0)
+    elif kind == "hydro":
+        inp = synthetic.hydro(total=total, seed=seed, nmin=100, nmax=200_000, box=500.0)
+        prm = abi.parity_params(thermal=1, box_size=500.0)
+    elif kind == "batched_n":  # a fixed count of 20,000 subhaloes
+        inp = synthetic.batched(n_sub=20_000, seed=seed)
+        prm = abi.parity_params(dm_only=1, box_size=500.0)
     else:
         inp = synthetic.batched(total=total, seed=seed)
-    prm = abi.parity_params(dm_only=1, box_size=500.0)
+        prm = abi.parity_params(dm_only=1, box_size=500.0)
     return inp, prm
 
 
-def cpu_sample(inp, target_particles):
-    """Systematic sample over the size-sorted subhaloes: keeps the N_p distribution."""
+def cpu_sample(inp, target_particles, seed=0, strict=False):
+    """Particle-weighted stratified sample: the subhaloes are binned by size
+    (decades of N_p); each bin gets a share of `target_particles` equal to its
+    share of the batch's particles and contributes randomly chosen subhaloes
+    until that share is reached (at least one per non-empty bin, so the
+    largest decade is always represented; with `strict`, no bin exceeds 1.5x
+    its share, so bins whose subhaloes are all larger are left out).  Returns
+    (sample, picked indices)."""
     sizes = np.diff(inp.offsets)
-    frac = min(1.0, target_particles / max(1, inp.n_particles))
-    stride = max(1, int(round(1.0 / frac)))
-    order = np.argsort(sizes, kind="stable")
-    pick = np.sort(order[::stride])
-    return inp.subset(pick), stride
+    rng = np.random.default_rng(seed)
+    dec = np.floor(np.log10(np.maximum(sizes, 1))).astype(int)
+    total = max(1, int(sizes.sum()))
+    pick = []
+    for d in np.unique(dec):
+        members = np.nonzero((dec == d) & (sizes > 0))[0]
+        if not len(members):
+            continue
+        share = target_particles * sizes[members].sum() / total
+        got = 0
+        for s in rng.permutation(members):
+            if got >= share and got > 0:
+                break
+            if (got > 0 or strict) and got + sizes[s] > 1.5 * share:
+                continue
+            pick.append(int(s))
+            got += int(sizes[s])
+    pick = np.sort(np.array(pick, np.int64))
+    return inp.subset(pick), pick
 
 
-def run_cpu(inp, prm, threads):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
+
+
+def sample_parity(inp, picked, gpu_out, cpu_out, prm):
+    """GPU outputs of the sampled subhaloes (from the full-batch call) against
+    the CPU leg's outputs on the same subhaloes: membership, raw bound mass,
+    most-bound IDs, status (tests/parity.py)."""
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    from parity import compare, compare_full
+    from hbtg.abi import Outputs
+    sub = inp.subset(picked)
+    rows = np.concatenate([np.arange(inp.offsets[s], inp.offsets[s + 1]) for s in picked])
+    d = {}
+    for k, v in gpu_out.__dict__.items():
+        if v is None:
+            d[k] = None
+        elif k in ("order", "energy", "potential"):
+            d[k] = v[rows]
+        else:
+            d[k] = v[picked]
+    g = Outputs(**d)
+    m = compare(sub, g, cpu_out)
+    mf, viol = compare_full(sub, g, cpu_out, prm)
+    return {"subhaloes": int(sub.n_sub), "particles": int(sub.n_particles), "membership": m["membership"],
+            "mass_rel": m["mass_rel"], "status_diff": len(m["status_diff"]), "mostbound_diff": len(m["mostbound_diff"]),
+            "energy_rel_median": m["energy_rel_median"], "full_output_violations": len(viol),
+            "violations_by_field": sorted({v[0] for v in viol}), "matched_subhaloes": mf["matched"]}
+
+
+def run_cpu(inp, prm, threads, inner_parallel=False):
     from hbtg import oracle
     ref = None
     try:
-        lib = oracle.reference_lib("dmo")
+        lib = oracle.reference_lib("dmo" if prm.dm_only else "hydro")
         if lib is not None:
             ref = "reference"
     except Exception:
         ref = None
     t0 = time.perf_counter()
     if ref == "reference":
-        out = oracle.run_reference(inp, prm, nthreads=threads)
+        out = oracle.run_reference(inp, prm, nthreads=threads, inner_parallel=inner_parallel)
     else:
-        out = oracle.run_port(inp, prm, nthreads=threads)
+        out = oracle.run_port(inp, prm, nthreads=threads, inner_parallel=inner_parallel)
     dt = time.perf_counter() - t0
     return out, dt, ref or "port"
 
@@ -97,7 +172,8 @@ class Clocks:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(HERE, "gpurun_out", "clocks_bench.csv")
+        import tempfile
+        self.path = os.path.join(tempfile.gettempdir(), "hbtg_bench_clocks_%d.csv" % os.getpid())
 
     def __enter__(self):
         try:
@@ -152,7 +228,7 @@ def bench_reference(args):
         return 0
     inp, prm = workload(args.total, args.seed, args.workload)
     threads = os.cpu_count() or 1
-    sample, stride = cpu_sample(inp, args.ref_sample)
+    sample, picked = cpu_sample(inp, args.ref_sample, seed=args.seed)
     for _ in range(args.warmup):
         run_cpu(sample, prm, threads)
     times, bounds, kind = [], [], "port"
@@ -167,13 +243,21 @@ def bench_reference(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic",
         "config": {"workload": WORKLOADS[args.workload] % args.total,
                    "particles": inp.n_particles, "subhaloes": inp.n_sub},
-        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": "every %d-th subhalo of the size-sorted batch: %d subhaloes, %d particles" %
-                                   (stride, sample.n_sub, sample.n_particles)},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": kind, "cpu_model": cpu_model(),
+                         "sample": _sample_text(inp, sample, picked)},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
     return 0
+
+
+def _sample_text(inp, sample, picked):
+    sizes = np.diff(inp.offsets)
+    return ("particle-weighted stratified sample (size decades, shares as in the batch): %d of %d subhaloes, "
+            "%d of %d particles, mean N_p %.0f (batch %.0f), largest %d (batch %d); the reference's schedule "
+            "(OpenMP dynamic over subhaloes)" %
+            (sample.n_sub, inp.n_sub, sample.n_particles, inp.n_particles, sample.n_particles / max(1, sample.n_sub),
+             inp.n_particles / max(1, inp.n_sub), int(sizes[picked].max()) if len(picked) else 0, int(sizes.max())))
 
 
 def bench_gpu(args):
@@ -286,7 +370,7 @@ def bench_gpu(args):
         assert rc in (0, 4), rc
 
     e2e_call()  # warm the host path once
-    e2e_times, e2e_device, h2d, d2h = [], [], 0, 0
+    e2e_times, e2e_device, e2e_h2d, e2e_d2h, h2d, d2h = [], [], [], [], 0, 0
     for _ in range(args.steps):
         _reset_frames(buf, hin)
         barrier()
@@ -296,10 +380,45 @@ def bench_gpu(args):
         st = u.stats()
         h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
         e2e_device.append(st["ms_total"])
+        e2e_h2d.append(st["ms_h2d"])
+        e2e_d2h.append(st["ms_d2h"])
     t_e2e = float(np.mean(e2e_times))
     if world > 1:
         t_e2e = _max_over_ranks(t_e2e)
     e2e_value = (warm["bound_all"] / args.steps) / t_e2e
+    h2d_ms = float(np.mean([x for x in e2e_h2d])) if e2e_h2d else None
+    d2h_ms = float(np.mean([x for x in e2e_d2h])) if e2e_d2h else None
+
+    # the literal configuration of the workload's description: 20,000 subhaloes
+    # (about 7e6 particles), both arms, device-resident inputs
+    literal = None
+    if args.workload == "batched" and not args.skip_literal and rank == 0:
+        lit_inp, _ = workload(0, args.seed + 7, "batched_n")
+        lit_db = DeviceBatch(lit_inp, device="cuda:%d" % local)
+        lit = {}
+        for arm in ("plain", "learned"):
+            def lit_step(arm=arm):
+                lit_db.reset_inout()
+                if arm == "plain":
+                    u.unbind_device(prm, lit_db.c, stream.cuda_stream)
+                else:
+                    u.unbind_learned_device(prm, lit_db, stream.cuda_stream, use_prior=False)
+            for _ in range(max(3, args.warmup)):
+                lit_step()
+            bound = 0
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                lit_step()
+                bound += u.stats()["total_bound"]
+            e1.record(stream)
+            torch.cuda.synchronize()
+            lit[arm] = bound / (e0.elapsed_time(e1) * 1e-3)
+        literal = {"n_sub": int(lit_inp.n_sub), "particles": int(lit_inp.n_particles), "learned": lit["learned"],
+                   "plain": lit["plain"], "learned_vs_plain": lit["learned"] / lit["plain"]}
+        del lit_db
 
     # roofline of the dominant kernel (the tree walk) in the learned arm
     peak = measure_fp32_peak(local)
@@ -309,14 +428,23 @@ def bench_gpu(args):
     achieved = flops_per_launch / (walk_ms_per_launch * 1e-3) / 1e12
     traffic = _walk_traffic(cw)
 
-    cpu = None
+    cpu = parity = None
     if rank == 0 and not args.skip_cpu:
-        sample, stride = cpu_sample(inp, args.cpu_sample)
+        sample, picked = cpu_sample(inp, args.cpu_sample, seed=args.seed)
         threads = os.cpu_count() or 1
         out, dt, kind = run_cpu(sample, prm, threads)
+        # one thread on about 1e5 particles (the same stratification; decades
+        # whose subhaloes exceed their share are left out)
+        small, _ = cpu_sample(inp, 100_000, seed=args.seed + 1, strict=True)
+        out1, dt1, _ = run_cpu(small, prm, 1)
         cpu = {"value": float(out.nbound.sum() / dt), "unit": UNIT, "cores": threads, "kind": kind,
-               "sample": "every %d-th subhalo of the size-sorted batch: %d subhaloes, %d particles, %.1f s" %
-                         (stride, sample.n_sub, sample.n_particles, dt)}
+               "cpu_model": cpu_model(), "sample": _sample_text(inp, sample, picked) + ", %.1f s" % dt,
+               "one_thread": {"value": float(out1.nbound.sum() / dt1), "particles": int(small.n_particles),
+                              "subhaloes": int(small.n_sub), "largest": int(np.diff(small.offsets).max()),
+                              "seconds": dt1}}
+        if plain_out is not None:
+            parity = sample_parity(inp, picked, plain_out, out, prm)
+            parity["against"] = "plain GPU path vs CPU %s on the sampled subhaloes" % kind
 
     if rank == 0:
         last = warm["last"]
@@ -351,7 +479,7 @@ def bench_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "call": "hbtg_unbind_batch_learned (host pointers, pinned)",
                     "ms_per_call": 1e3 * float(np.mean(e2e_times)),
-                    "ms_device_part": float(np.mean(e2e_device))},
+                    "ms_device_part": float(np.mean(e2e_device)), "ms_uploads": h2d_ms, "ms_downloads": d2h_ms},
             "gpu_launches": warm["kernel_launches"] // args.steps,
             "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
@@ -360,6 +488,8 @@ def bench_gpu(args):
                          "blocks_per_sm": warm["last"].get("walk_blocks_per_sm"),
                          "walk_share_of_step": warm["ms_walk"] / max(warm["ms"], 1e-9)},
             "cpu_baseline": cpu,
+            "parity": parity,
+            "literal_20000": literal,
             "clocks": warm["clocks"],
             "clocks_plain": plain and plain["clocks"],
         }
@@ -447,9 +577,10 @@ def main():
     ap.add_argument("--cpu-sample", type=float, default=1e6, help="particles in the CPU baseline sample")
     ap.add_argument("--ref-sample", type=float, default=4e5, help="particles per reference-arm step")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-literal", action="store_true", help="skip the literal 20,000-subhalo timing")
     args = ap.parse_args()
     if args.total is None:
-        args.total = 20000 if args.workload == "stripped" else 5e7
+        args.total = {"stripped": 20000, "hydro": 4e6}.get(args.workload, 5e7)
     args.total = int(args.total)
     args.cpu_sample = int(args.cpu_sample)
     args.ref_sample = int(args.ref_sample)

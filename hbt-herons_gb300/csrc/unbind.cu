@@ -191,6 +191,9 @@ struct hbtg_handle
   int device = 0;
   int sm_count = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;              // uploads that only the epilogue needs (host-pointer calls)
+  cudaEvent_t copy_events[5] = {};          // host-pointer calls: copy phases and the side upload
+  cudaEvent_t epilogue_wait = nullptr;      // set for one call: the epilogue waits for this event
   Pool pool;
   hbtg_stats stats{};
   bool count_interactions = false;
@@ -534,6 +537,8 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   O.potential = b->potential;
   O.iterations = b->iterations;
   O.status = b->status;
+  if (H->epilogue_wait)
+    HBTG_CUDA(cudaStreamWaitEvent(st, H->epilogue_wait, 0));
   R.epilogue(O);
   HBTG_CUDA(cudaMemcpyAsync(b->ref_pos, D.ref_pos, fbytes, cudaMemcpyDefault, st));
   HBTG_CUDA(cudaMemcpyAsync(b->ref_vel, D.ref_vel, fbytes, cudaMemcpyDefault, st));
@@ -670,11 +675,15 @@ int host_call(void *arg)
   Pool &P = H->pool;
   int64_t h2d = 0, d2h = 0;
   hbtg_batch d = *b;
+  cudaEvent_t *ev = H->copy_events;
+  HBTG_CUDA(cudaEventRecord(ev[0], st));
+  // the particle IDs are read only by the epilogue: their upload overlaps the iteration
+  d.id = upload(P, S_ID, b->id, N, H->side, h2d);
+  HBTG_CUDA(cudaEventRecord(ev[4], H->side));
   d.pos = upload(P, S_POS, b->pos, 3 * N, st, h2d);
   d.vel = upload(P, S_VEL, b->vel, 3 * N, st, h2d);
   d.mass = upload(P, S_MASS, b->mass, N, st, h2d);
   d.u = (c.p->thermal && b->u) ? upload(P, S_U, b->u, N, st, h2d) : nullptr;
-  d.id = upload(P, S_ID, b->id, N, st, h2d);
   d.type = (c.p->dm_only || !b->type) ? nullptr : upload(P, S_TYPE, b->type, N, st, h2d);
   d.ref_pos = upload(P, S_REFP, b->ref_pos, 3 * S, st, h2d);
   d.ref_vel = upload(P, S_REFV, b->ref_vel, 3 * S, st, h2d);
@@ -704,9 +713,16 @@ int host_call(void *arg)
         wa.e_prev = upload(P, S_PEN, c.prior->energy_prev, N, st, h2d);
     }
   }
+  HBTG_CUDA(cudaEventRecord(ev[1], st));
+  H->epilogue_wait = ev[4];
   rc = run_device(H, c.p, &d, st, c.learned ? &wa : nullptr);
+  H->epilogue_wait = nullptr;
   if (rc != HBTG_OK && rc != HBTG_ERR_MAX_ITER)
+  {
+    cudaStreamSynchronize(H->side);
     return rc;
+  }
+  HBTG_CUDA(cudaEventRecord(ev[2], st));
   download(b->order, d.order, N, st, d2h);
   download(b->nbound, d.nbound, S, st, d2h);
   download(b->mbound, d.mbound, S, st, d2h);
@@ -724,9 +740,15 @@ int host_call(void *arg)
   download(b->mostbound_pos, d.mostbound_pos, 3 * S, st, d2h);
   download(b->mostbound_vel, d.mostbound_vel, 3 * S, st, d2h);
   download(b->most_bound_id, d.most_bound_id, S, st, d2h);
+  HBTG_CUDA(cudaEventRecord(ev[3], st));
   HBTG_CUDA(cudaStreamSynchronize(st));
   H->stats.h2d_bytes = h2d;
   H->stats.d2h_bytes = d2h;
+  float t_up = 0.f, t_down = 0.f;
+  HBTG_CUDA(cudaEventElapsedTime(&t_up, ev[0], ev[1]));
+  HBTG_CUDA(cudaEventElapsedTime(&t_down, ev[2], ev[3]));
+  H->stats.ms_h2d = t_up;
+  H->stats.ms_d2h = t_down;
   return rc;
 }
 
@@ -926,6 +948,17 @@ int hbtg_create(hbtg_handle **handle, int device)
       delete h;
       return HBTG_ERR_CUDA;
     }
+  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+  {
+    delete h;
+    return HBTG_ERR_CUDA;
+  }
+  for (auto &e : h->copy_events)
+    if (cudaEventCreate(&e) != cudaSuccess)
+    {
+      delete h;
+      return HBTG_ERR_CUDA;
+    }
   *handle = h;
   return HBTG_OK;
 }
@@ -940,6 +973,11 @@ int hbtg_destroy(hbtg_handle *h)
     cudaEventDestroy(e);
   for (auto &e : h->phase_events)
     cudaEventDestroy(e);
+  for (auto &e : h->copy_events)
+    if (e)
+      cudaEventDestroy(e);
+  if (h->side)
+    cudaStreamDestroy(h->side);
   if (h->stream)
     cudaStreamDestroy(h->stream);
   delete h;

@@ -125,7 +125,7 @@ class CStats(C.Structure):
         ("kernel_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
         ("ms_propose", C.c_double), ("warm_subhaloes", C.c_int64), ("excluded", C.c_int64),
         ("readmitted", C.c_int64), ("cold_restarts", C.c_int64), ("readmit_rounds", C.c_int64),
-        ("walk_blocks_per_sm", C.c_int64),
+        ("walk_blocks_per_sm", C.c_int64), ("ms_h2d", C.c_double), ("ms_d2h", C.c_double),
     ]
 
     def as_dict(self):

@@ -152,6 +152,8 @@ typedef struct hbtg_stats
   int64_t cold_restarts;      /* warm subhaloes restarted cold (their first iteration converges) */
   int64_t readmit_rounds;     /* first tests run (lock-step) */
   int64_t walk_blocks_per_sm; /* resident tree-walk blocks per SM of the last call's launches */
+  double ms_h2d;              /* host-pointer calls: uploads on the call's stream before the first kernel */
+  double ms_d2h;              /* host-pointer calls: downloads after the last kernel */
 } hbtg_stats;
 
 typedef struct hbtg_handle hbtg_handle;
