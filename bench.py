@@ -141,7 +141,10 @@ def sample_parity(inp, picked, gpu_out, cpu_out, prm):
     return {"subhaloes": int(sub.n_sub), "particles": int(sub.n_particles), "membership": m["membership"],
             "mass_rel": m["mass_rel"], "status_diff": len(m["status_diff"]), "mostbound_diff": len(m["mostbound_diff"]),
             "energy_rel_median": m["energy_rel_median"], "full_output_violations": len(viol),
-            "violations_by_field": sorted({v[0] for v in viol}), "matched_subhaloes": mf["matched"]}
+            "violations_by_field": sorted({v[0] for v in viol}), "matched_subhaloes": mf["matched"],
+            "float_outlier_fraction": mf["float_outliers"], "tail_moved": mf["tail_moved"],
+            "tail_checked": mf["tail_checked"], "subresolution_exempt": mf["subres_exempt"],
+            "violations": [[v[0], int(v[1]), str(v[2])[:160]] for v in viol[:6]]}
 
 
 def run_cpu(inp, prm, threads, inner_parallel=False):

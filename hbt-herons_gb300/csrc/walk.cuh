@@ -21,10 +21,12 @@
 //               "near" ones.  Whenever a list fills, every lane reads each
 //               entry (a shared-memory broadcast) and adds the term of the
 //               entries its mask bit selects: -m / r for the far list with no
-//               branch, the cubic-spline softened kernel where r < h for the
-//               near list.  Lists are padded to a multiple of eight with
-//               massless entries; blocks of eight terms are summed in FP32
-//               and Kahan-added to the potential.
+//               branch, two entries at a time in packed FP32x2 arithmetic
+//               (each half an IEEE FP32 operation, so the same values as
+//               scalar code), and the cubic-spline softened kernel where
+//               r < h for the near list.  Lists are padded to a multiple of
+//               eight with massless entries; blocks of eight terms are summed
+//               in FP32 and Kahan-added to the potential.
 //
 // Opening test.  The reference opens a cell when len^2 > r^2 theta^2, with
 // len^2 in float and r^2 in double from the float coordinates
@@ -64,8 +66,11 @@ constexpr float kBandLo = 1.f - 1e-6f, kBandHi = 1.f + 1e-6f;
 
 struct WalkShared
 {
-  float4 far[kWalkWarps][kWalkFar];     // x, y, z, m
-  unsigned fmsk[kWalkWarps][kWalkFar];  // targets (lanes) that interact with the entry
+  // far list, two entries per pair (packed FP32x2 evaluation): fa = (x0, x1,
+  // y0, y1), fb = (z0, z1, m0, m1), fm = the two entries' target masks
+  float4 fa[kWalkWarps][kWalkFar / 2];
+  float4 fb[kWalkWarps][kWalkFar / 2];
+  uint2 fm[kWalkWarps][kWalkFar / 2];
   float4 near[kWalkWarps][kWalkNear];
   unsigned nmsk[kWalkWarps][kWalkNear];
   int ia[kWalkWarps][kWalkStack];       // range: first slot
@@ -132,41 +137,72 @@ __device__ __forceinline__ void kahan_add(float &sum, float &comp, float v)
   sum = t;
 }
 
-// Pads a list to a multiple of eight with massless entries far from every
-// target (finite terms, so the evaluation loops need no guard); returns the
+// A massless entry far from every target (finite terms, so the evaluation
+// loops need no guard).
+constexpr float kFarAway = 3e18f;
+
+// Pads a list to a multiple of eight with massless entries; returns the
 // padded length.  The caller leaves room for seven more entries.
 __device__ __forceinline__ int pad8(float4 *ent, unsigned *msk, int n, int lane)
 {
   const int padded = (n + 7) & ~7;
   if (n + lane < padded)
   {
-    ent[n + lane] = make_float4(3e18f, 3e18f, 3e18f, 0.f);
+    ent[n + lane] = make_float4(kFarAway, kFarAway, kFarAway, 0.f);
     msk[n + lane] = 0u;
   }
   __syncwarp();
   return padded;
 }
 
-// Far list: every target is at least one softening length from every entry.
-template <bool Wrap>
-__device__ __forceinline__ void eval_far(const float4 *ent, const unsigned *msk, int n, unsigned lanebit, float tx,
-                                         float ty, float tz, const KParams &K, float &sum, float &comp)
+// Writes far-list entry k (pair layout).
+__device__ __forceinline__ void far_put(float4 *fa, float4 *fb, uint2 *fm, int k, float x, float y, float z, float m,
+                                        unsigned mask)
 {
+  float *A = reinterpret_cast<float *>(fa + (k >> 1)), *B = reinterpret_cast<float *>(fb + (k >> 1));
+  const int h = k & 1;
+  A[h] = x;
+  A[2 + h] = y;
+  B[h] = z;
+  B[2 + h] = m;
+  reinterpret_cast<unsigned *>(fm + (k >> 1))[h] = mask;
+}
+
+__device__ __forceinline__ int pad8_far(float4 *fa, float4 *fb, uint2 *fm, int n, int lane)
+{
+  const int padded = (n + 7) & ~7;
+  if (n + lane < padded)
+    far_put(fa, fb, fm, n + lane, kFarAway, kFarAway, kFarAway, 0.f, 0u);
+  __syncwarp();
+  return padded;
+}
+
+// Far list: every target is at least one softening length from every entry
+// (never used for wrapped subhaloes).  Two entries per packed operation.
+__device__ __forceinline__ void eval_far(const float4 *fa, const float4 *fb, const uint2 *fm, int n, unsigned lanebit,
+                                         float tx, float ty, float tz, float &sum, float &comp)
+{
+  const float2 ntx = make_float2(-tx, -tx), nty = make_float2(-ty, -ty), ntz = make_float2(-tz, -tz);
   for (int i = 0; i < n; i += 8)
   {
-    float p0 = 0.f, p1 = 0.f;
+    float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
-    for (int u = 0; u < 8; u++)
+    for (int q = 0; q < 4; q++)
     {
-      const float4 e = ent[i + u];
-      const float m = (msk[i + u] & lanebit) ? e.w : 0.f;
-      const float r2 = dist2(sep<Wrap>(e.x, tx, K), sep<Wrap>(e.y, ty, K), sep<Wrap>(e.z, tz, K));
-      if (u & 1)
-        p1 = __fmaf_rn(-m, rsqrtf(r2), p1);
-      else
-        p0 = __fmaf_rn(-m, rsqrtf(r2), p0);
+      const int pp = (i >> 1) + q;
+      const float4 A = fa[pp], B = fb[pp];
+      const uint2 mk = fm[pp];
+      const float2 dx = __fadd2_rn(make_float2(A.x, A.y), ntx); // entry - target, exact as a subtraction
+      const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nty);
+      const float2 dz = __fadd2_rn(make_float2(B.x, B.y), ntz);
+      float2 r2 = __fmul2_rn(dx, dx);
+      r2 = __ffma2_rn(dy, dy, r2);
+      r2 = __ffma2_rn(dz, dz, r2);
+      const float2 rs = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+      const float2 nm = make_float2((mk.x & lanebit) ? -B.z : 0.f, (mk.y & lanebit) ? -B.w : 0.f);
+      acc = __ffma2_rn(nm, rs, acc);
     }
-    kahan_add(sum, comp, p0 + p1);
+    kahan_add(sum, comp, acc.x + acc.y);
   }
 }
 
@@ -234,8 +270,9 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
                                            unsigned long long &cnt)
 {
   const float4 *__restrict__ T = D.nodes;
-  float4 *far = sh.far[w], *nea = sh.near[w];
-  unsigned *fmsk = sh.fmsk[w], *nmsk = sh.nmsk[w];
+  float4 *fa = sh.fa[w], *fb = sh.fb[w], *nea = sh.near[w];
+  uint2 *fm = sh.fm[w];
+  unsigned *nmsk = sh.nmsk[w];
   int *ia = sh.ia[w], *ie = sh.ie[w];
   unsigned *im = sh.im[w];
   const unsigned full = 0xffffffffu, lanebit = 1u << lane, below = lanebit - 1u;
@@ -352,11 +389,7 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
         nmsk[at] = A;
       }
       else
-      {
-        const int at = nf + __popc(bf & below);
-        far[at] = en;
-        fmsk[at] = A;
-      }
+        far_put(fa, fb, fm, nf + __popc(bf & below), en.x, en.y, en.z, en.w, A);
       if (Count)
         cnt += __popc(A);
     }
@@ -382,7 +415,7 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
     __syncwarp();
     if (nf > kWalkFar - kFlushMargin)
     {
-      eval_far<Wrap>(far, fmsk, pad8(far, fmsk, nf, lane), lanebit, x.x, x.y, x.z, K, sum, comp);
+      eval_far(fa, fb, fm, pad8_far(fa, fb, fm, nf, lane), lanebit, x.x, x.y, x.z, sum, comp);
       nf = 0;
       __syncwarp();
     }
@@ -393,7 +426,7 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
       __syncwarp();
     }
   }
-  eval_far<Wrap>(far, fmsk, pad8(far, fmsk, nf, lane), lanebit, x.x, x.y, x.z, K, sum, comp);
+  eval_far(fa, fb, fm, pad8_far(fa, fb, fm, nf, lane), lanebit, x.x, x.y, x.z, sum, comp);
   eval_near<Wrap>(nea, nmsk, pad8(nea, nmsk, nn, lane), lanebit, x.x, x.y, x.z, K, h2, sum, comp);
   __syncwarp();
   if (valid)
