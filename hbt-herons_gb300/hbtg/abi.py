@@ -132,6 +132,33 @@ class CStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class CProps(C.Structure):
+    """hbtg_props."""
+    _fields_ = [(k, C.c_void_p) for k in ("rmax", "vmax", "rhalf", "renclose", "r200", "m200", "last_vmax",
+                                          "rmax_last", "snap_last", "inertia", "inertia_w", "nsource")]
+
+
+PROPS_FLOAT = ("rmax", "vmax", "rhalf", "renclose", "r200", "m200", "last_vmax", "rmax_last")
+
+
+class Props:
+    """Host arrays of hbtg_props for `n_sub` subhaloes; in/out fields start
+    from `init` (a dict of arrays) or zero."""
+
+    def __init__(self, n_sub, init=None, want_nsource=True):
+        init = init or {}
+        for k in PROPS_FLOAT:
+            setattr(self, k, np.array(init.get(k, np.zeros(n_sub)), np.float32))
+        self.snap_last = np.array(init.get("snap_last", np.full(n_sub, -1)), np.int32)
+        self.inertia = np.zeros((n_sub, 6), np.float32)
+        self.inertia_w = np.zeros((n_sub, 6), np.float32)
+        self.nsource = np.zeros(n_sub, np.int64) if want_nsource else None
+        self.c = CProps(*[_ptr(getattr(self, k)) for k, _ in CProps._fields_])
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in CProps._fields_ if getattr(self, k) is not None}
+
+
 class CPrior(C.Structure):
     """hbtg_prior."""
     _fields_ = [("nbound_prev", _P), ("energy_prev", _P)]

@@ -37,6 +37,8 @@ def port_lib():
         lib.oracle_unbind_batch.restype = C.c_int
         lib.oracle_last_interactions.restype = C.c_int64
         lib.oracle_last_cells.restype = C.c_int64
+        lib.oracle_subhalo_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+        lib.oracle_subhalo_properties.restype = C.c_int
         for fn in (lib.oracle_tree_potential, lib.oracle_direct_potential):
             fn.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                            C.c_void_p]
@@ -59,6 +61,8 @@ def reference_lib(variant):
         lib = C.CDLL(path)
         lib.ref_unbind_batch.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int]
         lib.ref_unbind_batch.restype = C.c_int
+        lib.ref_subhalo_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
+        lib.ref_subhalo_properties.restype = C.c_int
         _libs[key] = lib
     return _libs[key]
 
@@ -98,3 +102,35 @@ def tree_potential(params, src_pos, src_mass, tgt_pos, tgt_mass=None, direct=Fal
     if rc != 0:
         raise RuntimeError("oracle potential returned %d" % rc)
     return out
+
+
+def _props_batch(inp: Inputs, out):
+    """A CBatch over the inputs and an unbinding call's outputs."""
+    from .abi import _ptr
+    buf = CallBuffers(inp, want_energy=False)
+    for k in ("order", "nbound", "mbound", "mostbound_pos"):
+        setattr(buf.out, k, np.ascontiguousarray(getattr(out, k)))
+    buf.c.order, buf.c.nbound = _ptr(buf.out.order), _ptr(buf.out.nbound)
+    buf.c.mbound, buf.c.mostbound_pos = _ptr(buf.out.mbound), _ptr(buf.out.mostbound_pos)
+    return buf
+
+
+def subhalo_properties(inp: Inputs, out, params: Params, snapshot_id=1, source_relax=3.0, init=None,
+                       reference=False):
+    """CalculateProfileProperties / CalculateShape / TruncateSource of every
+    subhalo from an unbinding call's outputs: the restatement, or with
+    `reference` the reference's own functions (oracle/_ref)."""
+    from .abi import Props
+    buf = _props_batch(inp, out)
+    props = Props(inp.n_sub, init)
+    if reference:
+        lib = reference_lib("dmo" if params.dm_only else "hydro")
+        if lib is None:
+            raise FileNotFoundError("reference oracle not built (reference sources absent)")
+        fn = lib.ref_subhalo_properties
+    else:
+        fn = port_lib().oracle_subhalo_properties
+    rc = fn(C.byref(params), C.byref(buf.c), int(snapshot_id), float(source_relax), C.byref(props.c))
+    if rc != 0:
+        raise RuntimeError("subhalo properties returned %d" % rc)
+    return props

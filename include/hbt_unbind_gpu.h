@@ -233,6 +233,42 @@ int hbtg_tree_potential_device(hbtg_handle *handle, const hbtg_params *params, i
                                const float *mass, int64_t n_tgt, const int64_t *tgt_index, float *potential,
                                void *cuda_stream);
 
+/* ------------------------------------------------------------------------
+ * Properties of the unbound subhaloes (the steps after Unbind that read the
+ * bound set; the fields are Subhalo_t members, src/subhalo.h:55-77).
+ * ------------------------------------------------------------------------ */
+typedef struct hbtg_props
+{
+  float *rmax;        /* RmaxComoving */
+  float *vmax;        /* VmaxPhysical */
+  float *rhalf;       /* RHalfComoving */
+  float *renclose;    /* REncloseComoving */
+  float *r200;        /* BoundR200CritComoving (in/out: kept where no radius qualifies, as the reference) */
+  float *m200;        /* BoundM200Crit (in/out, likewise) */
+  float *last_vmax;   /* LastMaxVmaxPhysical (in/out) */
+  float *rmax_last;   /* RmaxComovingOfLastMaxVmax (in/out) */
+  int32_t *snap_last; /* SnapshotOfLastMaxVmax (in/out) */
+  float *inertia;     /* InertialTensor, 6 per subhalo: xx, xy, xz, yy, yz, zz */
+  float *inertia_w;   /* InertialTensorWeighted, 6 per subhalo */
+  int64_t *nsource;   /* particles TruncateSource keeps (or NULL) */
+} hbtg_props;
+
+/* Subhalo_t::CalculateProfileProperties (src/subhalo.cpp:175-243, with
+ * Snapshot_t::SphericalOverdensitySize, src/snapshot.cpp:258-282),
+ * Subhalo_t::CalculateShape (src/subhalo.cpp:245-309) and
+ * Subhalo_t::TruncateSource (src/subhalo_unbind.cpp:843-853) for every
+ * subhalo of a batch, from the bound set an unbinding call returned: `batch`
+ * holds the input particles (pos, mass; offsets on the host) and that call's
+ * order, nbound, mbound and mostbound_pos.  Uses params' softening, box,
+ * periodic flag, G, scale_factor and hubble; snapshot_id is the current
+ * snapshot (SnapshotOfLastMaxVmax); source_relax is SourceSubRelaxFactor.
+ * The _device form takes device arrays and queues on cuda_stream; the other
+ * takes host arrays. */
+int hbtg_subhalo_properties_device(hbtg_handle *handle, const hbtg_params *params, const hbtg_batch *batch,
+                                   int32_t snapshot_id, double source_relax, hbtg_props *props, void *cuda_stream);
+int hbtg_subhalo_properties(hbtg_handle *handle, const hbtg_params *params, const hbtg_batch *batch,
+                            int32_t snapshot_id, double source_relax, hbtg_props *props);
+
 /* Measurement utility, no counterpart in the reference: FP32 FMA throughput
  * of the device in TFLOP/s (the roofline denominator of the tree walk). */
 int hbtg_measure_fp32_peak(int device, double *tflops);

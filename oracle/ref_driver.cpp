@@ -33,14 +33,14 @@ class EpochSnapshot_t : public Snapshot_t
   HBTxyz dummy{{0.f, 0.f, 0.f}};
 
 public:
-  EpochSnapshot_t(double a, double hz)
+  EpochSnapshot_t(double a, double hz, int snapshot_id = 1)
   {
     Cosmology.ScaleFactor = a;
     Cosmology.Hz = hz;
     Cosmology.OmegaM0 = 0.3;
     Cosmology.OmegaLambda0 = 0.7;
-    SnapshotIndex = 1;
-    SnapshotId = 1;
+    SnapshotIndex = snapshot_id;
+    SnapshotId = snapshot_id;
   }
   HBTInt size() const override { return 0; }
   const HBTxyz &GetComovingPosition(const HBTInt) const override { return dummy; }
@@ -221,6 +221,69 @@ extern "C" int ref_unbind_batch(const hbtg_params *p, hbtg_batch *b, int nthread
     {
       omp_set_num_threads(1); /* the inner loops stay serial even when the team has one thread */
       unbind_one(p, b, epoch, s);
+    }
+  }
+  return HBTG_OK;
+}
+
+/* The reference's own CalculateProfileProperties, CalculateShape and
+ * TruncateSource on the bound sets of an unbinding call's outputs (see
+ * hbtg_subhalo_properties in include/hbt_unbind_gpu.h). */
+extern "C" int ref_subhalo_properties(const hbtg_params *p, const hbtg_batch *b, int snapshot_id, double source_relax,
+                                      hbtg_props *o)
+{
+  if (!p || !b || !o || b->n_sub < 0)
+    return HBTG_ERR_INVALID;
+  set_config(p, b);
+  HBTConfig.SourceSubRelaxFactor = source_relax;
+  EpochSnapshot_t epoch(p->scale_factor, p->hubble, snapshot_id);
+  omp_set_num_threads(1); /* the inner OpenMP reductions in a fixed order */
+  for (int64_t s = 0; s < b->n_sub; s++)
+  {
+    const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+    Subhalo_t sub;
+    sub.Particles.resize(n);
+    for (int64_t k = 0; k < n; k++)
+    {
+      const int64_t g = off + b->order[off + k];
+      Particle_t &q = sub.Particles[k];
+      q.Id = b->id ? b->id[g] : g;
+      for (int d = 0; d < 3; d++)
+      {
+        q.ComovingPosition[d] = b->pos[3 * g + d];
+        q.PhysicalVelocity[d] = b->vel ? b->vel[3 * g + d] : 0.f;
+      }
+      q.Mass = b->mass[g];
+    }
+    sub.Nbound = b->nbound[s];
+    sub.Mbound = b->mbound[s];
+    for (int d = 0; d < 3; d++)
+      sub.ComovingMostBoundPosition[d] = b->mostbound_pos[3 * s + d];
+    sub.BoundR200CritComoving = o->r200[s];
+    sub.BoundM200Crit = o->m200[s];
+    sub.LastMaxVmaxPhysical = o->last_vmax[s];
+    sub.RmaxComovingOfLastMaxVmax = o->rmax_last[s];
+    sub.SnapshotOfLastMaxVmax = o->snap_last[s];
+    sub.CalculateProfileProperties(epoch);
+    sub.CalculateShape();
+    o->rmax[s] = sub.RmaxComoving;
+    o->vmax[s] = sub.VmaxPhysical;
+    o->rhalf[s] = sub.RHalfComoving;
+    o->renclose[s] = sub.REncloseComoving;
+    o->r200[s] = sub.BoundR200CritComoving;
+    o->m200[s] = sub.BoundM200Crit;
+    o->last_vmax[s] = sub.LastMaxVmaxPhysical;
+    o->rmax_last[s] = sub.RmaxComovingOfLastMaxVmax;
+    o->snap_last[s] = sub.SnapshotOfLastMaxVmax;
+    for (int q = 0; q < 6; q++)
+    {
+      o->inertia[6 * s + q] = sub.InertialTensor[q];
+      o->inertia_w[6 * s + q] = sub.InertialTensorWeighted[q];
+    }
+    if (o->nsource)
+    {
+      sub.TruncateSource();
+      o->nsource[s] = (int64_t)sub.Particles.size();
     }
   }
   return HBTG_OK;

@@ -19,6 +19,10 @@
  *   Snapshot_t::RelativeVelocity          src/snapshot.h:135-148
  *   Subhalo_t::CountParticleTypes         src/subhalo.cpp:311-393
  *   Subhalo_t::GetCorePhaseSpaceProperties src/subhalo_merge.cpp:94-181
+ *   Subhalo_t::CalculateProfileProperties src/subhalo.cpp:175-243 (with
+ *     Snapshot_t::SphericalOverdensitySize src/snapshot.cpp:258-282)
+ *   Subhalo_t::CalculateShape             src/subhalo.cpp:245-309
+ *   Subhalo_t::TruncateSource             src/subhalo_unbind.cpp:843-853
  * and potential subsampling (MaxSampleSizeOfPotentialEstimate > 0):
  *   PrepareParticlesForSubsampling        src/subhalo_unbind.cpp:430-443
  *   Get/SetMassUpscaleFactor[PerType]     src/subhalo_unbind.cpp:290-391
@@ -959,5 +963,150 @@ extern "C" int oracle_direct_potential(const hbtg_params *p, int64_t ns, const f
     }
     out[i] = pot * (double)c.G / (double)c.a;
   }
+  return HBTG_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * Properties of the bound sets of an unbinding call's outputs (see
+ * hbtg_subhalo_properties in include/hbt_unbind_gpu.h), in the reference's
+ * float/double arithmetic.
+ * ------------------------------------------------------------------------ */
+namespace
+{
+struct Prof
+{
+  float r, m, v;
+};
+
+/* PeriodicDistance (src/config_parser.h:220-231): float differences, NEAREST
+ * in float, float sum of squares, correctly rounded square root. */
+float periodic_distance(const float *a, const float *b, const Cfg &c)
+{
+  float d[3];
+  for (int k = 0; k < 3; k++)
+  {
+    d[k] = a[k] - b[k];
+    if (c.periodic)
+      d[k] = wrap_f(d[k], c);
+  }
+  return std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+}
+
+void properties_one(const hbtg_batch *b, int64_t s, int snapshot_id, double source_relax, const Cfg &c,
+                    hbtg_props *o)
+{
+  const int64_t off = b->offsets[s], n = b->offsets[s + 1] - off;
+  const int64_t nb = b->nbound[s];
+  const float *cen = b->mostbound_pos + 3 * s;
+  auto pos_of = [&](int64_t k) { return b->pos + 3 * (off + b->order[off + k]); };
+  auto mass_of = [&](int64_t k) { return b->mass[off + b->order[off + k]]; };
+  /* CalculateProfileProperties (src/subhalo.cpp:175-243) */
+  if (nb <= 1)
+  {
+    o->rmax[s] = o->vmax[s] = o->rhalf[s] = o->renclose[s] = 0.f;
+    o->r200[s] = o->m200[s] = 0.f;
+  }
+  else
+  {
+    const float velocity_unit = c.G / c.a;
+    std::vector<Prof> prof(nb);
+    for (int64_t i = 0; i < nb; i++)
+    {
+      prof[i].r = periodic_distance(cen, pos_of(i), c);
+      prof[i].m = mass_of(i);
+    }
+    std::stable_sort(prof.begin(), prof.end(), [](const Prof &x, const Prof &y) { return x.r < y.r; });
+    double m_cum = 0.;
+    for (auto &q : prof)
+      q.m = (float)(m_cum += q.m);
+    for (auto &q : prof)
+    {
+      if (q.r < c.soft)
+        q.r = c.soft;
+      q.v = q.m / q.r;
+    }
+    int64_t imax = 0;
+    for (int64_t i = 1; i < nb; i++)
+      if (prof[imax].v < prof[i].v)
+        imax = i;
+    o->rmax[s] = prof[imax].r;
+    o->vmax[s] = std::sqrt(prof[imax].v * velocity_unit);
+    o->rhalf[s] = prof[nb / 2].r;
+    o->renclose[s] = prof[nb - 1].r;
+    /* SphericalOverdensitySize (src/snapshot.cpp:258-282), VirialFactor 200 */
+    const float rho = (float)((double)((200.f * c.hz) * c.hz) / 2.0 / (double)c.G * (double)c.a * (double)c.a *
+                              (double)c.a);
+    for (int64_t i = nb - 1; i >= 0; i--)
+      if (prof[i].m > rho * prof[i].r * prof[i].r * prof[i].r)
+      {
+        o->m200[s] = prof[i].m;
+        o->r200[s] = (float)std::pow((double)(prof[i].m / rho), 1.0 / 3);
+        break;
+      }
+    if (o->vmax[s] >= o->last_vmax[s])
+    {
+      o->snap_last[s] = snapshot_id;
+      o->last_vmax[s] = o->vmax[s];
+      o->rmax_last[s] = o->rmax[s];
+    }
+  }
+  /* CalculateShape (src/subhalo.cpp:245-309) */
+  double I[6] = {0, 0, 0, 0, 0, 0}, W[6] = {0, 0, 0, 0, 0, 0};
+  if (nb > 1)
+  {
+    for (int64_t i = 1; i < nb; i++)
+    {
+      const float m = mass_of(i);
+      const float *x = pos_of(i);
+      float dx = x[0] - cen[0], dy = x[1] - cen[1], dz = x[2] - cen[2];
+      if (c.periodic)
+      {
+        dx = wrap_f(dx, c);
+        dy = wrap_f(dy, c);
+        dz = wrap_f(dz, c);
+      }
+      const float dx2 = dx * dx, dy2 = dy * dy, dz2 = dz * dz;
+      I[0] += dx2 * m;
+      I[3] += dy2 * m;
+      I[5] += dz2 * m;
+      I[1] += dx * dy * m;
+      I[2] += dx * dz * m;
+      I[4] += dy * dz * m;
+      float dr2 = dx2 + dy2 + dz2;
+      dr2 /= m;
+      W[0] += dx2 / dr2;
+      W[3] += dy2 / dr2;
+      W[5] += dz2 / dr2;
+      W[1] += dx * dy / dr2;
+      W[2] += dx * dz / dr2;
+      W[4] += dy * dz / dr2;
+    }
+    for (int q = 0; q < 6; q++)
+    {
+      o->inertia[6 * s + q] = (float)I[q] / b->mbound[s];
+      o->inertia_w[6 * s + q] = (float)W[q] / b->mbound[s];
+    }
+  }
+  else
+    for (int q = 0; q < 6; q++)
+      o->inertia[6 * s + q] = o->inertia_w[6 * s + q] = 0.f;
+  /* TruncateSource (src/subhalo_unbind.cpp:843-853) */
+  if (o->nsource)
+  {
+    int64_t ns = nb <= 1 ? nb : (int64_t)((float)nb * (float)source_relax);
+    o->nsource[s] = ns > n ? n : ns;
+  }
+}
+} // namespace
+
+extern "C" int oracle_subhalo_properties(const hbtg_params *p, const hbtg_batch *b, int snapshot_id,
+                                         double source_relax, hbtg_props *o)
+{
+  if (!p || !b || !o || b->n_sub < 0)
+    return HBTG_ERR_INVALID;
+  const Cfg c = make_cfg(p, b);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t s = 0; s < b->n_sub; s++)
+    properties_one(b, s, snapshot_id, source_relax, c, o);
   return HBTG_OK;
 }

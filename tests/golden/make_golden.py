@@ -28,7 +28,27 @@ CASES = {
                        dict(dm_only=1, box_size=500.0, max_sample_size=1000)),
     "subsampled_hydro": (lambda: synthetic.hydro(seed=9, n_sub=8, nmin=1500, nmax=8000, box=300.0),
                          dict(thermal=1, box_size=300.0, max_sample_size=1000)),
+    # with the Hubble flow on (Hz such that 200 times the critical density is
+    # the synthetic haloes' mean density within r_200): also the post-unbind
+    # properties (prop_*) of the reference's CalculateProfileProperties,
+    # CalculateShape and TruncateSource
+    "properties_dmo": (lambda: synthetic.batched(n_sub=150, seed=5, nmax=20_000, box=500.0),
+                       dict(dm_only=1, box_size=500.0, hubble=31.6)),
+    "properties_hydro": (lambda: synthetic.hydro(seed=3, n_sub=20, nmin=100, nmax=8000, box=300.0),
+                         dict(thermal=1, box_size=300.0, hubble=31.6)),
 }
+
+PROPS_SNAPSHOT = 7
+PROPS_RELAX = 3.0
+
+
+def props_init(n_sub):
+    """In/out property values before the call (a previous snapshot's Vmax and
+    SO values, as the reference keeps them in Subhalo_t)."""
+    rng = np.random.default_rng(n_sub)
+    return {"last_vmax": rng.uniform(0.0, 80.0, n_sub).astype(np.float32),
+            "rmax_last": np.full(n_sub, 0.5, np.float32), "snap_last": np.full(n_sub, 3, np.int32),
+            "r200": np.full(n_sub, -1.0, np.float32), "m200": np.full(n_sub, -1.0, np.float32)}
 
 
 def make(name):
@@ -47,9 +67,26 @@ def make(name):
     for k, v in out.__dict__.items():
         if v is not None:
             d["out_" + k] = v
+    if name.startswith("properties"):
+        init = props_init(inp.n_sub)
+        props = oracle.subhalo_properties(inp, out, prm, snapshot_id=PROPS_SNAPSHOT, source_relax=PROPS_RELAX,
+                                          init=init, reference=True)
+        for k, v in init.items():
+            d["init_" + k] = v
+        for k, v in props.as_dict().items():
+            d["prop_" + k] = v
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")
     np.savez_compressed(path, **d)
     return path
+
+
+def load_props(path):
+    """(initial in/out property values, reference properties, snapshot id,
+    SourceSubRelaxFactor) of a properties fixture."""
+    z = np.load(path)
+    init = {k[5:]: z[k] for k in z.files if k.startswith("init_")}
+    props = {k[5:]: z[k] for k in z.files if k.startswith("prop_")}
+    return init, props, PROPS_SNAPSHOT, PROPS_RELAX
 
 
 def load(path):
@@ -64,5 +101,8 @@ def load(path):
 
 
 if __name__ == "__main__":
+    only = sys.argv[1:]
     for name in CASES:
+        if only and name not in only:
+            continue
         print(make(name), os.path.getsize(os.path.join(os.path.dirname(os.path.abspath(__file__)), name + ".npz")))

@@ -12,12 +12,16 @@ from hbtg import oracle
 GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz")))
 
 
-def _load(path):
+def _module(path):
     import importlib.util
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(os.path.dirname(path), "make_golden.py"))
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
-    return mod.load(path)
+    return mod
+
+
+def _load(path):
+    return _module(path).load(path)
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
@@ -35,3 +39,21 @@ def test_port_matches_reference_golden(path):
 def test_golden_fixtures_present():
     names = {os.path.basename(p) for p in GOLDEN}
     assert {"small_dmo.npz", "small_hydro.npz", "nfw_10k.npz", "batched_200.npz"} <= names
+
+
+PROPS = [p for p in GOLDEN if os.path.basename(p).startswith("properties")]
+
+
+@pytest.mark.parametrize("path", PROPS, ids=[os.path.basename(p)[:-4] for p in PROPS])
+def test_port_properties_match_reference_golden(path):
+    """CalculateProfileProperties, CalculateShape and TruncateSource of the
+    restatement, from the reference's own unbinding outputs, equal the
+    reference's (bit for bit)."""
+    mod = _module(path)
+    inp, prm, ref = mod.load(path)
+    init, props, snap, relax = mod.load_props(path)
+    got = oracle.subhalo_properties(inp, ref, prm, snapshot_id=snap, source_relax=relax, init=init)
+    for k, v in props.items():
+        assert np.array_equal(getattr(got, k), v), (k, np.nonzero(getattr(got, k) != v))
+    assert np.isfinite(props["r200"]).all() and (props["r200"] > 0).any()
+    assert (props["snap_last"] == snap).any() and (props["snap_last"] != snap).any()
