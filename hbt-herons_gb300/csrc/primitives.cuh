@@ -46,6 +46,27 @@ struct I3
   __host__ __device__ I3 operator+(const I3 &o) const { return I3{a + o.a, b + o.b, c + o.c}; }
 };
 
+// Segmented double sum: head marks the first item of a segment, where the
+// running sum restarts.  Associative, not commutative.
+struct SegD
+{
+  double v;
+  int head;
+  __host__ __device__ SegD operator+(const SegD &o) const { return o.head ? o : SegD{v + o.v, head}; }
+};
+
+// Types whose + is not commutative: the reduce pass keeps item order.
+template <typename T>
+struct ordered_sum
+{
+  static constexpr bool value = false;
+};
+template <>
+struct ordered_sum<SegD>
+{
+  static constexpr bool value = true;
+};
+
 template <typename T>
 __device__ __forceinline__ T zero_of();
 template <>
@@ -56,6 +77,8 @@ template <>
 __device__ __forceinline__ I4 zero_of<I4>() { return I4{0, 0, 0, 0}; }
 template <>
 __device__ __forceinline__ I3 zero_of<I3>() { return I3{0, 0, 0}; }
+template <>
+__device__ __forceinline__ SegD zero_of<SegD>() { return SegD{0., 0}; }
 
 template <typename T>
 __device__ __forceinline__ T shfl_up(T v, int d)
@@ -73,6 +96,12 @@ __device__ __forceinline__ I4 shfl_up<I4>(I4 v, int d)
 {
   return I4{__shfl_up_sync(0xffffffffu, v.m, d), __shfl_up_sync(0xffffffffu, v.x, d),
             __shfl_up_sync(0xffffffffu, v.y, d), __shfl_up_sync(0xffffffffu, v.z, d)};
+}
+
+template <>
+__device__ __forceinline__ SegD shfl_up<SegD>(SegD v, int d)
+{
+  return SegD{__shfl_up_sync(0xffffffffu, v.v, d), __shfl_up_sync(0xffffffffu, v.head, d)};
 }
 
 template <typename T>
@@ -93,6 +122,8 @@ __device__ __forceinline__ I4 shfl_idx<I4>(I4 v, int src)
             __shfl_sync(0xffffffffu, v.y, src), __shfl_sync(0xffffffffu, v.z, src)};
 }
 
+// Every combine in the scans below is (earlier items) + (later items), so a
+// non-commutative associative + (the segmented sum SegD) scans correctly.
 template <typename T>
 __device__ __forceinline__ T warp_inclusive_scan(T v, int lane)
 {
@@ -101,9 +132,15 @@ __device__ __forceinline__ T warp_inclusive_scan(T v, int lane)
   {
     const T o = shfl_up(v, d);
     if (lane >= d)
-      v = v + o;
+      v = o + v;
   }
   return v;
+}
+
+template <>
+__device__ __forceinline__ SegD shfl_idx<SegD>(SegD v, int src)
+{
+  return SegD{__shfl_sync(0xffffffffu, v.v, src), __shfl_sync(0xffffffffu, v.head, src)};
 }
 
 // Scan input read straight from an array, output written to one.
@@ -134,14 +171,27 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(Load load, T *__re
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const long long wbase = (long long)blockIdx.x * kTile + (long long)warp * kWarp * kRows;
   T acc = zero_of<T>();
+  if constexpr (ordered_sum<T>::value)
+  { // row by row, in item order
 #pragma unroll
-  for (int k = 0; k < kRows; k++)
-  {
-    const long long i = wbase + k * kWarp + lane;
-    if (i < n)
-      acc = acc + load(i);
+    for (int k = 0; k < kRows; k++)
+    {
+      const long long i = wbase + k * kWarp + lane;
+      const T x = (i < n) ? load(i) : zero_of<T>();
+      acc = acc + shfl_idx(warp_inclusive_scan(x, lane), 31);
+    }
   }
-  acc = warp_inclusive_scan(acc, lane);
+  else
+  {
+#pragma unroll
+    for (int k = 0; k < kRows; k++)
+    {
+      const long long i = wbase + k * kWarp + lane;
+      if (i < n)
+        acc = acc + load(i);
+    }
+    acc = warp_inclusive_scan(acc, lane);
+  }
   if (lane == 31)
     warp_tot[warp] = acc;
   __syncthreads();

@@ -17,6 +17,7 @@
 #include "../../include/hbt_unbind_gpu.h"
 #include "common.cuh"
 #include "driver.cuh"
+#include "props.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
 #include "warm.cuh"
@@ -135,6 +136,8 @@ enum Slot
   S_NODES, S_TABLE, S_SCRATCH, S_CELLS, S_LVL, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
   S_POTI, S_WCTR, S_FRAMEW,
+  S_PR_OFF, S_PR_CNT, S_PR_FIN, S_PR_RR, S_PR_MM, S_PR_K, S_PR_V, S_PR_KA, S_PR_VA, S_PR_MC, S_PR_VK, S_PR_SO,
+  S_PR_SH, S_PR_SCR, S_PR_POS, S_PR_MASS, S_PR_ORD, S_PR_NB, S_PR_MBND, S_PR_MBP, S_PR_OUTF, S_PR_OUTI, S_PR_OUTL,
   S_NUM
 };
 
@@ -860,6 +863,200 @@ int dev_call(void *arg)
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Properties of the unbound subhaloes (props.cuh)
+// ---------------------------------------------------------------------------
+struct PropsCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  const hbtg_batch *b;
+  int snapshot;
+  double relax;
+  hbtg_props *o;
+  cudaStream_t st;
+  bool host = false;
+};
+
+// The property kernels over device arrays (b: positions, masses, order,
+// nbound, mbound, mostbound_pos; offsets on the host), outputs into o.
+int props_run(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, int snapshot, double relax,
+              const hbtg_props *o, cudaStream_t st, int64_t &launches)
+{
+  const int S = (int)b->n_sub;
+  Pool &P = H->pool;
+  PropState Q;
+  Q.S = S;
+  long long *off = P.get<long long>(S_PR_OFF, (size_t)S + 1);
+  HBTG_CUDA(cudaMemcpyAsync(off, b->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
+  Q.off = off;
+  Q.pos = b->pos;
+  Q.mass = b->mass;
+  Q.order = reinterpret_cast<const long long *>(b->order);
+  Q.nbound = reinterpret_cast<const long long *>(b->nbound);
+  Q.mbound = b->mbound;
+  Q.mb_pos = b->mostbound_pos;
+  Q.cnt = P.get<int>(S_PR_CNT, (size_t)S + 1);
+  Q.fin_off = P.get<int>(S_PR_FIN, (size_t)S + 1);
+  Q.vkey = P.get<unsigned long long>(S_PR_VK, (size_t)S);
+  Q.so_rank = P.get<int>(S_PR_SO, (size_t)S);
+  Q.shape = P.get<double>(S_PR_SH, (size_t)S * 12);
+  Q.box = (float)p->box_size;
+  Q.half = (float)((double)Q.box / 2.);
+  Q.periodic = p->periodic != 0;
+  Q.soft = (float)p->softening;
+  const float G = (float)p->G, a = (float)p->scale_factor, hz = (float)p->hubble;
+  Q.velocity_unit = G / a; // PhysicalConst::G / ScaleFactor in float
+  // SphericalOverdensitySize's RhoVirial for VirialFactor 200, in the reference's mixed float/double order
+  Q.rho_vir = (float)((double)((200.f * hz) * hz) / 2.0 / (double)G * (double)a * (double)a * (double)a);
+  Q.relax = (float)relax;
+  Q.snapshot = snapshot;
+  k_prop_init<<<blocks_for(S + 1, 256), 256, 0, st>>>(Q);
+  launches++;
+  HBTG_CUDA(cudaGetLastError());
+  scan<int, false>(Q.cnt, Q.fin_off, S + 1, P.get<int>(S_SCRATCH, scan_scratch_elems<int>(S + 1)), st, &launches);
+  const int T = read_int(Q.fin_off + S, st);
+  const size_t t1 = (size_t)std::max(T, 1);
+  Q.rr = P.get<float>(S_PR_RR, t1);
+  Q.mm = P.get<float>(S_PR_MM, t1);
+  Q.k32 = P.get<uint32_t>(S_PR_K, t1);
+  Q.val = P.get<uint32_t>(S_PR_V, t1);
+  Q.k32_alt = P.get<uint32_t>(S_PR_KA, t1);
+  Q.val_alt = P.get<uint32_t>(S_PR_VA, t1);
+  Q.mcum = P.get<double>(S_PR_MC, t1);
+  const uint32_t *sorted = Q.val;
+  if (T > 0)
+  {
+    k_prop_items<<<blocks_for(((long long)T + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(Q, T);
+    launches++;
+    HBTG_CUDA(cudaGetLastError());
+    // by distance, then stably by subhalo
+    int *table = P.get<int>(S_TABLE, radix_table_elems(T));
+    int *scr = P.get<int>(S_SCRATCH, scan_scratch_elems<int>(std::max<long long>(radix_table_elems(T) + 1,
+                                                                                      256LL * 4096)));
+    const bool f1 = radix_sort_pairs<uint32_t>(Q.k32, Q.val, Q.k32_alt, Q.val_alt, T, 0, 32, table, scr, st,
+                                               &launches);
+    uint32_t *v = f1 ? Q.val_alt : Q.val, *v_other = f1 ? Q.val : Q.val_alt;
+    int bits = 0;
+    while ((1LL << bits) < S)
+      bits++;
+    if (bits > 0)
+    {
+      k_prop_segkeys<<<blocks_for(T, 256), 256, 0, st>>>(Q, v, Q.k32, T);
+      launches++;
+      const bool f2 = radix_sort_pairs<uint32_t>(Q.k32, v, Q.k32_alt, v_other, T, 0, bits, table, scr, st,
+                                                 &launches);
+      v = f2 ? v_other : v;
+    }
+    sorted = v;
+    SegD *sscr = P.get<SegD>(S_PR_SCR, scan_scratch_elems<SegD>(T));
+    scan_load_store<SegD, true>(PropMassLoad{Q, sorted}, PropMassStore{Q.mcum}, T, sscr, st, &launches);
+    k_prop_profile<<<blocks_for(T, 256), 256, 0, st>>>(Q, sorted, T);
+    launches++;
+    HBTG_CUDA(cudaGetLastError());
+  }
+  PropOut O;
+  O.rmax = o->rmax;
+  O.vmax = o->vmax;
+  O.rhalf = o->rhalf;
+  O.renclose = o->renclose;
+  O.r200 = o->r200;
+  O.m200 = o->m200;
+  O.last_vmax = o->last_vmax;
+  O.rmax_last = o->rmax_last;
+  O.snap_last = o->snap_last;
+  O.inertia = o->inertia;
+  O.inertia_w = o->inertia_w;
+  O.nsource = reinterpret_cast<long long *>(o->nsource);
+  k_prop_finish<<<blocks_for(S, 256), 256, 0, st>>>(Q, sorted, O);
+  launches++;
+  HBTG_CUDA(cudaGetLastError());
+  return HBTG_OK;
+}
+
+int props_call(void *arg)
+{
+  PropsCall &c = *static_cast<PropsCall *>(arg);
+  hbtg_handle *H = c.H;
+  const hbtg_batch *b = c.b;
+  const hbtg_props *o = c.o;
+  if (!c.p || !b || !o || b->n_sub < 0 || (b->n_sub > 0 && !b->offsets))
+    return HBTG_ERR_INVALID;
+  if (!o->rmax || !o->vmax || !o->rhalf || !o->renclose || !o->r200 || !o->m200 || !o->last_vmax ||
+      !o->rmax_last || !o->snap_last || !o->inertia || !o->inertia_w)
+    return HBTG_ERR_INVALID;
+  const long long S = b->n_sub;
+  if (S == 0)
+    return HBTG_OK;
+  if (S >= (1LL << 30) || b->offsets[0] != 0)
+    return HBTG_ERR_INVALID;
+  for (long long s = 0; s < S; s++)
+    if (b->offsets[s + 1] < b->offsets[s])
+      return HBTG_ERR_INVALID;
+  const long long N = b->offsets[S];
+  if (N >= (1LL << 30) || (N > 0 && (!b->pos || !b->mass || !b->order)) || !b->nbound || !b->mbound ||
+      !b->mostbound_pos)
+    return HBTG_ERR_INVALID;
+  HBTG_CUDA(cudaSetDevice(H->device));
+  cudaStream_t st = c.st;
+  int64_t launches = 0, h2d = 0, d2h = 0;
+  if (!c.host)
+  {
+    const int rc = props_run(H, c.p, b, c.snapshot, c.relax, o, st, launches);
+    HBTG_CUDA(cudaStreamSynchronize(st));
+    H->stats.kernel_launches = launches;
+    return rc;
+  }
+  for (long long s = 0; s < S; s++)
+    if (b->nbound[s] < 0 || b->nbound[s] > b->offsets[s + 1] - b->offsets[s])
+      return HBTG_ERR_INVALID;
+  Pool &P = H->pool;
+  hbtg_batch d = *b;
+  d.pos = upload(P, S_PR_POS, b->pos, 3 * (size_t)N, st, h2d);
+  d.mass = upload(P, S_PR_MASS, b->mass, (size_t)N, st, h2d);
+  d.order = upload(P, S_PR_ORD, b->order, (size_t)N, st, h2d);
+  d.nbound = upload(P, S_PR_NB, b->nbound, (size_t)S, st, h2d);
+  d.mbound = upload(P, S_PR_MBND, b->mbound, (size_t)S, st, h2d);
+  d.mostbound_pos = upload(P, S_PR_MBP, b->mostbound_pos, 3 * (size_t)S, st, h2d);
+  float *of = P.get<float>(S_PR_OUTF, 20 * (size_t)S);
+  int32_t *oi = P.get<int32_t>(S_PR_OUTI, (size_t)S);
+  int64_t *ol = P.get<int64_t>(S_PR_OUTL, (size_t)S);
+  hbtg_props dp;
+  dp.rmax = of;
+  dp.vmax = of + S;
+  dp.rhalf = of + 2 * S;
+  dp.renclose = of + 3 * S;
+  dp.r200 = of + 4 * S;
+  dp.m200 = of + 5 * S;
+  dp.last_vmax = of + 6 * S;
+  dp.rmax_last = of + 7 * S;
+  dp.inertia = of + 8 * S;
+  dp.inertia_w = of + 14 * S;
+  dp.snap_last = oi;
+  dp.nsource = o->nsource ? ol : nullptr;
+  const size_t fs = sizeof(float) * (size_t)S;
+  // in/out members start from the caller's values
+  HBTG_CUDA(cudaMemcpyAsync(dp.r200, o->r200, fs, cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(dp.m200, o->m200, fs, cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(dp.last_vmax, o->last_vmax, fs, cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(dp.rmax_last, o->rmax_last, fs, cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(dp.snap_last, o->snap_last, sizeof(int32_t) * (size_t)S, cudaMemcpyHostToDevice, st));
+  const int rc = props_run(H, c.p, &d, c.snapshot, c.relax, &dp, st, launches);
+  float *const hf[8] = {o->rmax, o->vmax, o->rhalf, o->renclose, o->r200, o->m200, o->last_vmax, o->rmax_last};
+  for (int q = 0; q < 8; q++)
+    download(hf[q], of + (size_t)q * S, (size_t)S, st, d2h);
+  download(o->inertia, dp.inertia, 6 * (size_t)S, st, d2h);
+  download(o->inertia_w, dp.inertia_w, 6 * (size_t)S, st, d2h);
+  download(o->snap_last, dp.snap_last, (size_t)S, st, d2h);
+  if (o->nsource)
+    download(o->nsource, dp.nsource, (size_t)S, st, d2h);
+  HBTG_CUDA(cudaStreamSynchronize(st));
+  H->stats.kernel_launches = launches;
+  H->stats.h2d_bytes = h2d;
+  H->stats.d2h_bytes = d2h;
+  return rc;
+}
+
 struct ModelCall
 {
   hbtg_handle *H;
@@ -982,6 +1179,24 @@ int hbtg_destroy(hbtg_handle *h)
     cudaStreamDestroy(h->stream);
   delete h;
   return HBTG_OK;
+}
+
+int hbtg_subhalo_properties_device(hbtg_handle *h, const hbtg_params *p, const hbtg_batch *b, int32_t snapshot_id,
+                                   double source_relax, hbtg_props *props, void *cuda_stream)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  PropsCall c{h, p, b, snapshot_id, source_relax, props, static_cast<cudaStream_t>(cuda_stream), false};
+  return guarded(props_call, &c);
+}
+
+int hbtg_subhalo_properties(hbtg_handle *h, const hbtg_params *p, const hbtg_batch *b, int32_t snapshot_id,
+                            double source_relax, hbtg_props *props)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  PropsCall c{h, p, b, snapshot_id, source_relax, props, h->stream, true};
+  return guarded(props_call, &c);
 }
 
 int hbtg_unbind_batch(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b)

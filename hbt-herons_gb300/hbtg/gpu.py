@@ -12,7 +12,7 @@ import os
 import numpy as np
 
 from .abi import (CallBuffers, CBatch, CModel, CPrior, CStats, Inputs, MLP_PARAMS, NUM_FEATURES, Outputs, Params,
-                  STATUS_NAMES)
+                  STATUS_NAMES, _ptr)
 from .build import LIB
 
 _lib = None
@@ -179,6 +179,25 @@ class Unbinder:
         if rc != 0:
             raise UnbindError(rc, "hbtg_features_device")
         return f[:n]
+
+    def subhalo_properties(self, inp: Inputs, out, params: Params, snapshot_id=1, source_relax=3.0, init=None):
+        """CalculateProfileProperties / CalculateShape / TruncateSource of
+        every subhalo from an unbinding call's outputs (host arrays, through
+        hbtg_subhalo_properties).  Returns an abi.Props."""
+        from .abi import Props
+        buf = CallBuffers(inp, want_energy=False)
+        for k in ("order", "nbound", "mbound", "mostbound_pos"):
+            setattr(buf.out, k, np.ascontiguousarray(getattr(out, k)))
+        buf.c.order, buf.c.nbound = _ptr(buf.out.order), _ptr(buf.out.nbound)
+        buf.c.mbound, buf.c.mostbound_pos = _ptr(buf.out.mbound), _ptr(buf.out.mostbound_pos)
+        props = Props(inp.n_sub, init)
+        fn = self.lib.hbtg_subhalo_properties
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_void_p]
+        fn.restype = C.c_int
+        rc = fn(self.h, C.byref(params), C.byref(buf.c), int(snapshot_id), float(source_relax), C.byref(props.c))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_subhalo_properties")
+        return props
 
     def tree_potential(self, params: Params, pos, mass, targets, device="cuda:0"):
         """G/a * tree potential at the listed particles of one set
