@@ -63,6 +63,9 @@ def reference_lib(variant):
         lib.ref_unbind_batch.restype = C.c_int
         lib.ref_subhalo_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
         lib.ref_subhalo_properties.restype = C.c_int
+        lib.ref_recursive_unbind.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int64] + \
+            [C.c_void_p] * 6
+        lib.ref_recursive_unbind.restype = C.c_int
         _libs[key] = lib
     return _libs[key]
 
@@ -134,3 +137,37 @@ def subhalo_properties(inp: Inputs, out, params: Params, snapshot_id=1, source_r
     if rc != 0:
         raise RuntimeError("subhalo properties returned %d" % rc)
     return props
+
+
+def reference_recursive_unbind(parts, members, parent, frames, params: Params, merge_trapped=True, snapshot_id=1):
+    """The reference's own Subhalo_t::RecursiveUnbind (with MergeRecursively)
+    from every root of a nesting forest (oracle/_ref).  Returns a dict of
+    per-subhalo arrays: nbound, mbound, most_bound_id, sink_track, snap_sink,
+    snap_death, and ids (list of the final Particles' IDs)."""
+    from .abi import _ptr
+    lib = reference_lib("dmo" if params.dm_only else "hydro")
+    if lib is None:
+        raise FileNotFoundError("reference oracle not built (reference sources absent)")
+    S = len(members)
+    idx = np.concatenate(members) if S else np.zeros(0, np.int64)
+    offsets = np.zeros(S + 1, np.int64)
+    np.cumsum([len(m) for m in members], out=offsets[1:])
+    pick = lambda a: None if a is None else np.ascontiguousarray(a[idx])
+    f = lambda k: np.ascontiguousarray(np.asarray(frames[k]))
+    inp = Inputs(offsets, pick(parts.pos), pick(parts.vel), pick(parts.mass), pick(parts.id), pick(parts.type),
+                 pick(parts.u), f("ref_pos"), f("ref_vel"), f("mostbound_pos"), f("mostbound_vel"), f("most_bound_id"))
+    buf = CallBuffers(inp, want_energy=False)
+    cap = int(offsets[-1]) * 8 + 16
+    out_off, out_count = np.zeros(S, np.int64), np.zeros(S, np.int64)
+    out_ids = np.zeros(cap, np.int64)
+    sink = np.zeros(S, np.int64)
+    ssink, sdeath = np.zeros(S, np.int32), np.zeros(S, np.int32)
+    par = np.ascontiguousarray(parent, np.int64)
+    rc = lib.ref_recursive_unbind(C.byref(params), C.byref(buf.c), _ptr(par), int(merge_trapped), int(snapshot_id),
+                                  cap, _ptr(out_off), _ptr(out_count), _ptr(out_ids), _ptr(sink), _ptr(ssink),
+                                  _ptr(sdeath))
+    if rc != 0:
+        raise RuntimeError("ref_recursive_unbind returned %d" % rc)
+    return dict(nbound=buf.out.nbound.copy(), mbound=buf.out.mbound.copy(), most_bound_id=buf.out.most_bound_id.copy(),
+                sink_track=sink, snap_sink=ssink, snap_death=sdeath,
+                ids=[out_ids[out_off[s]:out_off[s] + out_count[s]].copy() for s in range(S)])

@@ -359,12 +359,16 @@ def stripped(n_sub=20_000, seed=0, nmin=20, nmax=1_000_000, box=500.0, flip=0.05
     return inp
 
 
-def nested_system(seed=0, n_host=20_000, n_sat=6, n_subsat=3, box=100.0):
+def nested_system(seed=0, n_host=20_000, n_sat=6, n_subsat=3, box=100.0, n_merge=0):
     """A FoF-like subhalo tree for nested unbinding: a host NFW halo (c=6),
     n_sat satellites (NFW, 300-3000 particles, 20 % heated) on orbits inside it,
     and n_subsat sub-satellites (NFW, 60-300 particles) inside the first
     satellites.  Every subhalo's source is its own particles; the host centre
     sits near a box corner so the system straddles the periodic boundary.
+    With n_merge > 0, compact satellites that overlap a subhalo in phase
+    space are added (MergeRecursively's case): the first at the host's centre
+    with the host's velocity, the second at the first satellite's centre with
+    its velocity (nested in it), alternating.
     Returns (nested.Particles, members, parent, frames)."""
     from .nested import Particles
     rng = np.random.Generator(np.random.PCG64(seed))
@@ -396,6 +400,17 @@ def nested_system(seed=0, n_host=20_000, n_sat=6, n_subsat=3, box=100.0):
                                            False, box, c, v0, do_wrap=False)
         comps.append((p, vel))
         parent.append(1 + (j % len(sat_centres)))
+    for k in range(n_merge):
+        n = int(rng.integers(200, 600))
+        if k % 2 == 0 or not sat_centres:
+            c, v, host = centre, np.zeros((1, 3)), 0
+        else:
+            c, v, _ = sat_centres[0]
+            host = 1
+        p, vel, _, _ = _nfw_halo_particles(rng, np.array([n]), np.array([15.0]), 1.0, np.array([0.0]), 1.5, 3.0,
+                                           False, box, c + 1e-4 * _random_dirs(rng, 1), v, do_wrap=False)
+        comps.append((p, vel))
+        parent.append(host)
     counts = np.array([len(p) for p, _ in comps], np.int64)
     pos = _wrap(np.concatenate([p for p, _ in comps]), box)
     vel = np.concatenate([v for _, v in comps])

@@ -13,6 +13,17 @@
 // properties, binding energies and the death/sink bookkeeping exactly where
 // Unbind sets them (src/subhalo_unbind.cpp:647-707, 754-802).
 //
+// recursive_unbind() is SubhaloSnapshot_t::RefineParticles' nested part,
+//   Subhalo_t::RecursiveUnbind                             src/subhalo_unbind.cpp:810-841
+//   Subhalo_t::MergeRecursively / MergeTo / phase space    src/subhalo_merge.cpp:14-92, 183-230
+// run level-synchronously: the subhaloes of one nesting depth are one batch,
+// deepest first; after a level's call each subhalo checks the subhaloes of
+// its own subtree for phase-space overlap (and absorbs their bound sets when
+// MergeTrappedSubhalos is on, then is unbound again), and every child's
+// unbound tail is appended to its parent, children in NestedSubhalos order.
+// Subhaloes at one depth never feed one another, so this is the reference's
+// depth-first recursion batched.
+//
 // Requirements on the types (those of src/subhalo.h and src/snapshot.h):
 //   Subhalo: Particles (vector of Particle), Nbound, Mbound, MboundType[6],
 //            NboundType[6], TracerIndex, ComovingAveragePosition,
@@ -25,9 +36,12 @@
 //            ParticleBindingEnergies, ParticlePotentialEnergies
 //   Particle: Id, ComovingPosition[3], PhysicalVelocity[3], Mass, Type
 //            (InternalEnergy when thermal energy is used)
+// and, for recursive_unbind: Subhalo::NestedSubhalos (indices into the
+// subhalo list), TrackId.
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -47,6 +61,7 @@ struct Options
   int snapshot_id = 0;         // epoch.GetSnapshotId()
   int64_t null_snapshot = -1;  // SpecialConst::NullSnapshotId
   int64_t null_track = -1;     // SpecialConst::NullTrackId
+  bool merge_trapped = false;  // MergeTrappedSubhalos (recursive_unbind)
 };
 
 class Unbinder
@@ -96,7 +111,159 @@ public:
     run(params_in, subs, opt, true);
   }
 
+  // Subhalo_t::RecursiveUnbind from every root (src/subhalo_unbind.cpp:810-841)
+  // over a subhalo list whose NestedSubhalos hold indices into it.  The
+  // caller adds a FoF group's other heads to its central's NestedSubhalos
+  // first, as RefineParticles does (src/subhalo_unbind.cpp:874-880).
+  template <class SubhaloList>
+  void recursive_unbind(const hbtg_params &params, SubhaloList &subs, const std::vector<int64_t> &roots,
+                        const Options &opt)
+  {
+    using Subhalo = typename SubhaloList::value_type;
+    const int64_t n = (int64_t)subs.size();
+    std::vector<int> depth(n, -1);
+    std::vector<int64_t> parent(n, -1);
+    std::vector<std::vector<int64_t>> levels;
+    std::vector<int64_t> stack;
+    for (int64_t r : roots)
+    {
+      if (r < 0 || r >= n || depth[r] >= 0)
+        throw std::runtime_error("recursive_unbind: bad or repeated root");
+      depth[r] = 0;
+      stack.push_back(r);
+      while (!stack.empty())
+      {
+        const int64_t s = stack.back();
+        stack.pop_back();
+        if ((int64_t)levels.size() <= depth[s])
+          levels.resize(depth[s] + 1);
+        levels[depth[s]].push_back(s);
+        for (auto c : subs[s].NestedSubhalos)
+        {
+          if (c < 0 || c >= n || depth[c] >= 0)
+            throw std::runtime_error("recursive_unbind: a subhalo nested twice or in a cycle");
+          depth[c] = depth[s] + 1;
+          parent[c] = s;
+          stack.push_back((int64_t)c);
+        }
+      }
+    }
+    for (int d = (int)levels.size() - 1; d >= 0; d--)
+    {
+      std::vector<int64_t> level = levels[d];
+      std::sort(level.begin(), level.end());
+      std::vector<Subhalo *> batch;
+      for (int64_t s : level)
+        batch.push_back(&subs[s]);
+      run(params, batch, opt, false);
+      // MergeRecursively after each Unbind; a host that absorbed a resolved
+      // subhalo is unbound again when MergeTrappedSubhalos is on (:826-835)
+      std::vector<Subhalo *> again;
+      for (int64_t s : level)
+        if (merge_recursively(params, subs, s, subs[s], opt) && opt.merge_trapped)
+          again.push_back(&subs[s]);
+      if (!again.empty())
+        run(params, again, opt, false);
+      // each child's unbound tail to its parent, children in NestedSubhalos order (:819-823)
+      if (d == 0)
+        continue;
+      std::vector<int64_t> parents;
+      for (int64_t s : level)
+        parents.push_back(parent[s]);
+      std::sort(parents.begin(), parents.end());
+      parents.erase(std::unique(parents.begin(), parents.end()), parents.end());
+      for (int64_t p : parents)
+        for (auto c : subs[p].NestedSubhalos)
+        {
+          const Subhalo &child = subs[c];
+          subs[p].Particles.insert(subs[p].Particles.end(), child.Particles.begin() + child.Nbound,
+                                   child.Particles.end());
+        }
+    }
+  }
+
 private:
+  // Subhalo_t::MergeRecursively (src/subhalo_merge.cpp:46-92): the subtree of
+  // subs[self], depth first, against `ref`.
+  template <class SubhaloList, class Subhalo>
+  bool merge_recursively(const hbtg_params &params, SubhaloList &subs, int64_t self, Subhalo &ref,
+                         const Options &opt)
+  {
+    bool merged = false;
+    if (ref.Nbound <= 1)
+      return merged;
+    Subhalo &me = subs[self];
+    for (size_t i = 0; i < me.NestedSubhalos.size(); i++)
+      merged = merge_recursively(params, subs, (int64_t)me.NestedSubhalos[i], ref, opt) | merged;
+    if (me.SinkTrackId == opt.null_track && &me != &ref && phase_space_distance(params, me, ref) < 2.f)
+    {
+      // SetMergerInformation (src/subhalo_merge.cpp:30-41)
+      me.SnapshotOfSink = opt.snapshot_id;
+      me.SinkTrackId = ref.TrackId;
+      if (me.SnapshotOfDeath == opt.null_snapshot)
+        me.SnapshotOfDeath = opt.snapshot_id;
+      merged = (me.Nbound > 1) | merged;
+      if (opt.merge_trapped)
+        merge_to(me, ref);
+    }
+    return merged;
+  }
+
+  // Subhalo_t::PhaseSpaceDistance (src/subhalo_merge.cpp:14-20) in float:
+  // PeriodicDistance and Distance (src/config_parser.h:220-231, src/mymath.h:232-238).
+  template <class Subhalo>
+  static float phase_space_distance(const hbtg_params &params, const Subhalo &me, const Subhalo &ref)
+  {
+    const float box = (float)params.box_size, half = (float)((double)box / 2.);
+    float dx[3], dv[3];
+    for (int d = 0; d < 3; d++)
+    {
+      dx[d] = ref.CoreComovingPosition[d] - me.CoreComovingPosition[d];
+      if (params.periodic)
+        dx[d] = dx[d] > half ? dx[d] - box : (dx[d] < -half ? dx[d] + box : dx[d]);
+      dv[d] = ref.CorePhysicalVelocity[d] - me.CorePhysicalVelocity[d];
+    }
+    const float pos = std::sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+    const float vel = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+    return pos / ref.CoreComovingSigmaR + vel / ref.CorePhysicalSigmaV;
+  }
+
+  // Subhalo_t::MergeTo (src/subhalo_merge.cpp:183-230): the bound set moves
+  // to the host; the subhalo keeps its most-bound tracer as an orphan.
+  template <class Subhalo>
+  static void merge_to(Subhalo &me, Subhalo &host)
+  {
+    if (me.Nbound <= 1)
+      return;
+    host.Particles.insert(host.Particles.end(), me.Particles.begin(), me.Particles.begin() + me.Nbound);
+    const auto &t = me.Particles[me.TracerIndex];
+    me.MostBoundParticleId = t.Id;
+    for (int d = 0; d < 3; d++)
+    {
+      me.ComovingMostBoundPosition[d] = t.ComovingPosition[d];
+      me.PhysicalMostBoundVelocity[d] = t.PhysicalVelocity[d];
+      me.ComovingAveragePosition[d] = me.ComovingMostBoundPosition[d];
+      me.PhysicalAverageVelocity[d] = me.PhysicalMostBoundVelocity[d];
+    }
+    me.Nbound = 0;
+    me.Particles.resize(0);
+    me.Mbound = 0; // CountParticles over no particles
+    zero_types(me, 0);
+  }
+  template <class Subhalo>
+  static auto zero_types(Subhalo &sub, int) -> decltype((void)sub.NboundType[0])
+  {
+    for (int t = 0; t < HBTG_TYPE_MAX; t++)
+    {
+      sub.NboundType[t] = 0;
+      sub.MboundType[t] = 0;
+    }
+  }
+  template <class Subhalo>
+  static void zero_types(Subhalo &, ...)
+  {
+  }
+
   template <class Subhalo>
   void run(const hbtg_params &params_in, const std::vector<Subhalo *> &subs, const Options &opt, bool learned)
   {

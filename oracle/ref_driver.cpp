@@ -289,6 +289,62 @@ extern "C" int ref_subhalo_properties(const hbtg_params *p, const hbtg_batch *b,
   return HBTG_OK;
 }
 
+/* The reference's own Subhalo_t::RecursiveUnbind (src/subhalo_unbind.cpp:810-841,
+ * with MergeRecursively and the second Unbind of MergeTrappedSubhalos,
+ * src/subhalo_merge.cpp:46-92) from every root of a nesting forest.  Subhalo s
+ * starts from its own particles (batch segment s) and frame; parent[s] is the
+ * subhalo it is nested in (-1: a root), NestedSubhalos listing children in
+ * ascending index; TrackId = s.  Outputs per subhalo: nbound, mbound, the IDs
+ * of its final Particles (CSR: out_count[s], into out_ids from out_off[s],
+ * capacity out_cap), SinkTrackId, SnapshotOfSink, SnapshotOfDeath and
+ * MostBoundParticleId.  Returns HBTG_ERR_NOMEM when out_cap is too small. */
+extern "C" int ref_recursive_unbind(const hbtg_params *p, hbtg_batch *b, const int64_t *parent, int merge_trapped,
+                                    int snapshot_id, int64_t out_cap, int64_t *out_off, int64_t *out_count,
+                                    int64_t *out_ids, int64_t *sink_track, int32_t *snap_sink,
+                                    int32_t *snap_death)
+{
+  if (!p || !b || !parent || b->n_sub < 0)
+    return HBTG_ERR_INVALID;
+  set_config(p, b);
+  HBTConfig.MergeTrappedSubhalos = merge_trapped != 0;
+  EpochSnapshot_t epoch(p->scale_factor, p->hubble, snapshot_id);
+  srand48(p->seed);
+  srand((unsigned)p->seed);
+  omp_set_num_threads(1);
+  const int64_t S = b->n_sub;
+  SubhaloList_t subs(S);
+  for (int64_t s = 0; s < S; s++)
+  {
+    load_subhalo(p, b, s, subs[s]);
+    subs[s].TrackId = s;
+  }
+  for (int64_t s = 0; s < S; s++)
+    if (parent[s] >= 0)
+      subs[parent[s]].NestedSubhalos.push_back(s);
+  for (int64_t s = 0; s < S; s++)
+    if (parent[s] < 0)
+      subs[s].RecursiveUnbind(subs, epoch);
+  int64_t at = 0;
+  for (int64_t s = 0; s < S; s++)
+  {
+    const int64_t n = (int64_t)subs[s].Particles.size();
+    if (at + n > out_cap)
+      return HBTG_ERR_NOMEM;
+    out_off[s] = at;
+    out_count[s] = n;
+    for (int64_t k = 0; k < n; k++)
+      out_ids[at + k] = subs[s].Particles[k].Id;
+    at += n;
+    b->nbound[s] = subs[s].Nbound;
+    b->mbound[s] = subs[s].Mbound;
+    b->most_bound_id[s] = subs[s].MostBoundParticleId;
+    sink_track[s] = subs[s].SinkTrackId;
+    snap_sink[s] = subs[s].SnapshotOfSink;
+    snap_death[s] = subs[s].SnapshotOfDeath;
+  }
+  return HBTG_OK;
+}
+
 extern "C" const char *ref_variant()
 {
 #ifdef DM_ONLY

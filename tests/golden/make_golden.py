@@ -80,6 +80,34 @@ def make(name):
     return path
 
 
+NESTED_SNAPSHOT = 9
+
+
+def make_nested():
+    """A nesting forest with subhaloes that overlap in phase space, through the
+    reference's own RecursiveUnbind with MergeRecursively, with
+    MergeTrappedSubhalos on (ref1_*) and off (ref0_*)."""
+    parts, members, parent, frames = synthetic.nested_system(seed=3, n_host=20_000, n_sat=6, n_subsat=3, n_merge=2)
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    d = {"pos": parts.pos, "vel": parts.vel, "mass": parts.mass, "id": parts.id, "parent": parent,
+         "member_off": np.concatenate([[0], np.cumsum([len(m) for m in members])]).astype(np.int64),
+         "member_idx": np.concatenate(members).astype(np.int64)}
+    for k, v in frames.items():
+        d["frame_" + k] = np.asarray(v)
+    for k, v in prm.as_dict().items():
+        d["prm_" + k] = np.array(v)
+    for mt in (1, 0):
+        r = oracle.reference_recursive_unbind(parts, members, parent, frames, prm, merge_trapped=mt,
+                                              snapshot_id=NESTED_SNAPSHOT)
+        for k in ("nbound", "mbound", "most_bound_id", "sink_track", "snap_sink", "snap_death"):
+            d["ref%d_%s" % (mt, k)] = r[k]
+        d["ref%d_ids_off" % mt] = np.concatenate([[0], np.cumsum([len(x) for x in r["ids"]])]).astype(np.int64)
+        d["ref%d_ids" % mt] = np.concatenate(r["ids"]).astype(np.int64)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "nested_merge.npz")
+    np.savez_compressed(path, **d)
+    return path
+
+
 def load_props(path):
     """(initial in/out property values, reference properties, snapshot id,
     SourceSubRelaxFactor) of a properties fixture."""
@@ -102,6 +130,8 @@ def load(path):
 
 if __name__ == "__main__":
     only = sys.argv[1:]
+    if not only or "nested_merge" in only:
+        print(make_nested())
     for name in CASES:
         if only and name not in only:
             continue

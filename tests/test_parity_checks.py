@@ -25,7 +25,8 @@ def _fields(viol):
     return {v[0] for v in viol}
 
 
-@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(HERE, "golden", "*.npz"))),
+@pytest.mark.parametrize("path", sorted(p for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                                         if not os.path.basename(p).startswith("nested")),
                          ids=lambda p: os.path.basename(p)[:-4])
 def test_reference_passes_against_itself(path):
     spec = importlib.util.spec_from_file_location("make_golden", os.path.join(HERE, "golden", "make_golden.py"))
