@@ -206,3 +206,78 @@ def test_gpu_subsampling_requires_prepared_particles(unbinder):
     with pytest.raises(UnbindError) as e:
         unbinder.unbind(inp, prm)
     assert e.value.code == 5
+
+
+def _sphere(rng, n, radius):
+    """n points uniform in a sphere (rejection sampling, as make_test_subhalo)."""
+    out = []
+    while len(out) < n:
+        x = rng.uniform(-radius, radius, 3)
+        if x @ x <= radius * radius:
+            out.append(x)
+    return np.array(out)
+
+
+def test_gpu_core_phase_space_known_answer(unbinder):
+    """The reference's known-answer test of GetCorePhaseSpaceProperties
+    (unit_tests/test_build_pos_vel.cpp:76-164): 100-particle spheres of radius
+    2 around (10, 10, 10) with one coordinate moved to each of -3, -0.1, 0.1,
+    50, 99.9, 100.1, 103 in a periodic box of 100, velocities within 30 of
+    (20, 20, 20).  The masses are heavy enough that every particle stays
+    bound; the core (the first 20 bound particles, wrapped about the first)
+    must match the test's own mass-weighted formula to 1e-5, and its
+    dispersions to 1e-5 fractionally."""
+    rng = np.random.default_rng(0)
+    xs = [-3.0, -0.1, 0.1, 50.0, 99.9, 100.1, 103.0]
+    pos, vel, counts = [], [], []
+    for rep in range(5):
+        for x in xs:
+            for dim in range(3):
+                c = np.array([10.0, 10.0, 10.0])
+                c[dim] = x
+                p = _sphere(rng, 100, 2.0)
+                p = p[np.argsort((p * p).sum(1), kind="stable")] + c  # sorted by radius, as the fixture
+                pos.append(p)
+                vel.append(_sphere(rng, 100, 30.0) + 20.0)
+                counts.append(100)
+    pos = np.concatenate(pos).astype(np.float32)
+    vel = np.concatenate(vel).astype(np.float32)
+    n = len(pos)
+    offsets = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    S = len(counts)
+    first = offsets[:-1]
+    ref_pos = pos[first].copy()
+    ref_vel = np.array([vel[o:o + 100].mean(0) for o in first], np.float32)
+    inp = abi.Inputs(offsets, pos, vel, np.full(n, 1000.0, np.float32), np.arange(n, dtype=np.int64) * 3 + 1, None,
+                     None, ref_pos, ref_vel, pos[first].copy(), vel[first].copy(), (first * 3 + 1).astype(np.int64))
+    prm = abi.parity_params(dm_only=1, box_size=100.0)
+    got = unbinder.unbind(inp, prm)
+    assert np.all(got.nbound == 100)
+    box, half = 100.0, 50.0
+    for s in range(S):
+        o = offsets[s]
+        idx = o + got.order[o:o + 100]
+        x = pos[idx].astype(np.float64)
+        v = vel[idx].astype(np.float64)
+        core = idx[:20]  # DM only: every particle is a tracer; CoreSize = SubCoreSizeMin = 20
+        ref = x[0]
+        d = pos[core].astype(np.float64) - ref
+        d = np.where(d > half, d - box, np.where(d < -half, d + box, d))
+        w = ref + d  # wrap_position about the first bound particle
+        m = 1000.0
+        msum = m * len(core)
+        cp = (m * w).sum(0) / msum
+        cv = (m * vel[core].astype(np.float64)).sum(0) / msum
+        sr = np.sqrt(((m * w * w).sum(0) / msum - cp * cp).sum())
+        sv = np.sqrt(((m * vel[core].astype(np.float64) ** 2).sum(0) / msum - cv * cv).sum())
+        gc = got.core[s].astype(np.float64)
+        dpos = gc[:3] - cp
+        dpos = np.where(dpos > half, dpos - box, np.where(dpos < -half, dpos + box, dpos))
+        assert np.sqrt((dpos ** 2).sum()) < 1e-5, (s, gc[:3], cp)
+        assert np.all(np.abs(gc[3:6] - cv) < 1e-5), (s, gc[3:6], cv)
+        assert abs(gc[6] - sr) / sr < 1e-5 and abs(gc[7] - sv) / sv < 1e-5, (s, gc[6:], sr, sv)
+        # the sanity checks of the reference test
+        centre = pos[o:o + 100].mean(0)
+        dc = gc[:3] - centre
+        dc = np.where(dc > half, dc - box, np.where(dc < -half, dc + box, dc))
+        assert np.sqrt((dc ** 2).sum()) < 2.0 and gc[6] <= 2.0 and gc[7] <= 30.0

@@ -43,7 +43,8 @@ def test_gpu_nested_matches_oracle(unbinder):
         bg, br = set(parts.id[g.members[:g.nbound]]), set(parts.id[r.members[:r.nbound]])
         mism += len(bg ^ br)
         tot += len(br)
-    assert mism <= max(2, 1e-3 * tot), (mism, tot)
+    # the plain path's bars: membership 1e-4, bound mass 1e-5
+    assert mism <= max(1, 1e-4 * tot), (mism, tot)
     m_g = sum(g.mbound for g in gpu)
     m_r = sum(r.mbound for r in ref)
-    assert abs(m_g - m_r) <= 1e-3 * m_r
+    assert abs(m_g - m_r) <= 1e-5 * m_r
