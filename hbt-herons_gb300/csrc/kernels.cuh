@@ -97,7 +97,6 @@ struct DevState
   float *keyp;             // [12S] per-axis origin hi/lo, 2^21/side, exact levels, halvings (see k_root)
   int *fb_list, *fb_count; // packed items whose key needs the exact double descent
   double *com;             // [7S] M, sum m dx, sum m v (epilogue: kinematics sums)
-  double *tmass;           // [6S] bound mass per particle type (epilogue)
   double *com_part;        // [7 x blocks] per-block frame sums of single-subhalo k_com blocks
   // packed arrays
   unsigned long long *key, *key_alt;
@@ -1483,7 +1482,6 @@ __global__ void k_epi_init(DevState D)
   for (int t = 0; t < 6; t++)
   {
     reinterpret_cast<int *>(D.bb_lo)[6 * s + t] = 0;
-    D.tmass[6 * s + t] = 0.;
   }
   D.nb_new[s] = 0x7fffffff;
 }
@@ -1504,8 +1502,8 @@ __global__ void k_epi_order(DevState D, OutPtrs O)
 
 // Per-particle outputs of the bound sets (binding and potential energies) and
 // the FP64 sums of AverageKinematics (src/subhalo_unbind.cpp:200-249), the
-// per-type counts and masses of CountParticleTypes (src/subhalo.cpp:311-393)
-// and the first tracer position.  Items are the bound particles of finished
+// per-type counts of CountParticleTypes (src/subhalo.cpp:311-393) and the
+// first tracer position (the per-type masses are summed by k_epilogue).  Items are the bound particles of finished
 // subhaloes packed by fin_off; each thread takes 16 consecutive items.
 __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
 {
@@ -1515,7 +1513,6 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
   // carry one FP32 rounding each here), totals in double
   KahanF acc[6];
   int tn[6] = {0, 0, 0, 0, 0, 0};
-  double tm[6] = {0., 0., 0., 0., 0., 0.};
   int ft = 0x7fffffff;
   int s = -1;
   auto flush_types = [&](int seg) {
@@ -1523,9 +1520,7 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
       if (tn[t])
       {
         atomicAdd(&reinterpret_cast<int *>(D.bb_lo)[6 * seg + t], tn[t]);
-        atomicAdd(&D.tmass[6 * seg + t], tm[t]);
         tn[t] = 0;
-        tm[t] = 0.;
       }
     if (ft != 0x7fffffff)
       atomicMin(&D.nb_new[seg], ft);
@@ -1587,10 +1582,7 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
 #pragma unroll
       for (int q = 0; q < 6; q++)
         if ((t & 7) == q)
-        {
           tn[q]++;
-          tm[q] += (double)m;
-        }
       if (is_tracer_bits(t) && k < ft)
         ft = k;
     }
@@ -1630,12 +1622,23 @@ __global__ void k_epilogue(DevState D, KParams K, OutPtrs O)
     for (int q = 0; q < 5; q++)
       O.kinematics[5 * s + q] = kin[q];
   const int *tn = reinterpret_cast<const int *>(D.bb_lo) + 6 * s;
+  // MboundType as CountParticleTypes sums it (src/subhalo.cpp:311-393): float
+  // additions in bound order (the batch runs it on one thread per subhalo)
+  float mt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  if (O.mbound_type && !K.dm_only && resolved)
+    for (int i = 0; i < nb; i++)
+    {
+      const int p = D.ord[off + i];
+      const int t = D.ty[p] & 7;
+      if (t < 6)
+        mt[t] = __fadd_rn(mt[t], D.pm[p].w);
+    }
   for (int t = 0; t < 6; t++)
   {
     if (O.nbound_type)
       O.nbound_type[6 * s + t] = resolved ? tn[t] : 0;
     if (O.mbound_type)
-      O.mbound_type[6 * s + t] = (K.dm_only || !resolved) ? 0.f : (float)D.tmass[6 * s + t];
+      O.mbound_type[6 * s + t] = (K.dm_only || !resolved) ? 0.f : mt[t];
   }
   const int first_tracer = D.nb_new[s];
   long long ti;

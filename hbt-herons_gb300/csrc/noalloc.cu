@@ -74,7 +74,6 @@ constexpr size_t kScratchBytes =
   al(sizeof(double) * 4 * kS1) +             // root cubes
   al(sizeof(float) * 12 * kS1) +             // fast key-descent constants
   al(sizeof(double) * 7 * kS1) +             // frame sums
-  al(sizeof(double) * 6 * kS1) +             // per-type bound masses
   al(sizeof(double) * 7 * (kN1 / 4096 + 2)) + // per-block frame sums
   2 * al(sizeof(unsigned long long) * kN1) + // key, key_alt
   6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
@@ -293,7 +292,6 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.root = c.take<double>(4 * kS1);
   D.keyp = c.take<float>(12 * kS1);
   D.com = c.take<double>(7 * kS1);
-  D.tmass = c.take<double>(6 * kS1);
   D.com_part = c.take<double>(7 * (kN1 / (256 * kItemsPerThread) + 2));
   D.key = c.take<unsigned long long>(kN1);
   D.key_alt = c.take<unsigned long long>(kN1);

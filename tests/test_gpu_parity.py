@@ -71,7 +71,7 @@ def test_gpu_hydro_thermal_vs_oracle(unbinder):
     # per-type bound counts and masses
     assert np.abs(got.nbound_type - ref.nbound_type).sum() <= max(2, 1e-4 * ref.nbound.sum())
     rel = np.abs(got.mbound_type.sum(0) - ref.mbound_type.sum(0)) / np.maximum(ref.mbound_type.sum(0), 1e-30)
-    assert np.all(rel < 1e-4), rel
+    assert np.all(rel < 1e-6), rel  # the same float sums in the same order (CountParticleTypes)
 
 
 def test_gpu_mass_dynamic_range_vs_oracle(unbinder):
