@@ -159,6 +159,12 @@ class Props:
         return {k: getattr(self, k) for k, _ in CProps._fields_ if getattr(self, k) is not None}
 
 
+class CReassign(C.Structure):
+    """hbtg_reassign."""
+    _fields_ = [("n_groups", C.c_int64), ("group_off", C.c_void_p), ("n_sub", C.c_int64), ("offsets", C.c_void_p),
+                ("pos", C.c_void_p), ("type", C.c_void_p), ("dest", C.c_void_p)]
+
+
 class CPrior(C.Structure):
     """hbtg_prior."""
     _fields_ = [("nbound_prev", _P), ("energy_prev", _P)]

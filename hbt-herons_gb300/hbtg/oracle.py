@@ -39,6 +39,8 @@ def port_lib():
         lib.oracle_last_cells.restype = C.c_int64
         lib.oracle_subhalo_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_void_p]
         lib.oracle_subhalo_properties.restype = C.c_int
+        lib.oracle_reassign.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        lib.oracle_reassign.restype = C.c_int
         for fn in (lib.oracle_tree_potential, lib.oracle_direct_potential):
             fn.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
                            C.c_void_p]
@@ -66,6 +68,8 @@ def reference_lib(variant):
         lib.ref_recursive_unbind.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int64] + \
             [C.c_void_p] * 6
         lib.ref_recursive_unbind.restype = C.c_int
+        lib.ref_reassign.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+        lib.ref_reassign.restype = C.c_int
         _libs[key] = lib
     return _libs[key]
 
@@ -171,3 +175,29 @@ def reference_recursive_unbind(parts, members, parent, frames, params: Params, m
     return dict(nbound=buf.out.nbound.copy(), mbound=buf.out.mbound.copy(), most_bound_id=buf.out.most_bound_id.copy(),
                 sink_track=sink, snap_sink=ssink, snap_death=sdeath,
                 ids=[out_ids[out_off[s]:out_off[s] + out_count[s]].copy() for s in range(S)])
+
+
+def reassign(inp: Inputs, group_off, params: Params, num_neighbours=10, reference=False):
+    """The moves of ReassignParticles for FoF groups given as ranges of
+    subhaloes (group_off): dest[i] = the subhalo particle i moves to, or -1.
+    The restatement, or with `reference` the reference's own neighbour search
+    (oracle/_ref, hydro build)."""
+    from .abi import CReassign
+    dest = np.full(inp.n_particles, -1, np.int64)
+    go = np.ascontiguousarray(group_off, np.int64)
+    offs = np.ascontiguousarray(inp.offsets, np.int64)
+    pos = np.ascontiguousarray(inp.pos, np.float32)
+    typ = np.ascontiguousarray(inp.type, np.uint8)
+    r = CReassign(len(go) - 1, go.ctypes.data, inp.n_sub, offs.ctypes.data, pos.ctypes.data, typ.ctypes.data,
+                  dest.ctypes.data)
+    if reference:
+        lib = reference_lib("hydro")
+        if lib is None:
+            raise FileNotFoundError("reference oracle not built (reference sources absent)")
+        fn = lib.ref_reassign
+    else:
+        fn = port_lib().oracle_reassign
+    rc = fn(C.byref(params), C.byref(r), int(num_neighbours))
+    if rc != 0:
+        raise RuntimeError("reassign returned %d" % rc)
+    return dest

@@ -458,3 +458,51 @@ def small_cases(seed=0, box=100.0):
 def small_hydro(seed=0, n_sub=12, box=200.0):
     """A small mixed-species batch for parity tests."""
     return hydro(seed=seed, n_sub=n_sub, nmin=100, nmax=3000, box=box)
+
+
+def fof_groups(seed=0, n_groups=6, n_sat=3, box=300.0, swap=0.1):
+    """FoF groups for particle reassignment: each group is a hydro host halo
+    (2,000-8,000 particles) and `n_sat` satellites (200-1,000) placed inside
+    it, with a fraction `swap` of every subhalo's gas particles exchanged with
+    another subhalo of the same group (gas listed in the wrong source).
+    Returns (Inputs with the subhaloes grouped, group_off)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    per = 1 + n_sat
+    counts = np.concatenate([[rng.integers(2000, 8000)] + list(rng.integers(200, 1000, n_sat)) for _ in range(n_groups)])
+    base = hydro(seed=seed + 1000, n_sub=len(counts), nmin=200, nmax=8000, box=box)
+    # resample each subhalo to its planned size by taking its first particles (its own profile)
+    sizes = np.diff(base.offsets)
+    take = np.minimum(sizes, counts)
+    rows = [np.arange(base.offsets[s], base.offsets[s] + take[s]) for s in range(len(counts))]
+    pos = [base.pos[r].astype(np.float64) for r in rows]
+    for g in range(n_groups):
+        h = g * per
+        hc = pos[h].mean(0)
+        spread = np.std(pos[h] - hc) + 1e-3
+        for k in range(1, per):
+            c = pos[h + k].mean(0)
+            pos[h + k] += hc + rng.normal(0, 0.6 * spread, 3) - c
+    members = [list(range(len(r))) for r in rows]
+    pos_all = [p for p in pos]
+    src = [(s, i) for s in range(len(rows)) for i in range(len(rows[s]))]
+    lists = [[(s, i) for i in range(len(rows[s]))] for s in range(len(rows))]
+    for g in range(n_groups):
+        subs = list(range(g * per, (g + 1) * per))
+        for s in subs:
+            gas = [t for t in lists[s] if base.type[rows[t[0]][t[1]]] == 0]
+            n_move = int(swap * len(gas))
+            pick = rng.choice(len(gas), n_move, replace=False) if n_move else []
+            for q in pick:
+                other = int(rng.choice([u for u in subs if u != s]))
+                lists[s].remove(gas[q])
+                lists[other].append(gas[q])
+    P = np.concatenate([[pos_all[s][i] for (s, i) in L] for L in lists if L]).astype(np.float32)
+    V = np.concatenate([[base.vel[rows[s][i]] for (s, i) in L] for L in lists if L]).astype(np.float32)
+    M = np.concatenate([[base.mass[rows[s][i]] for (s, i) in L] for L in lists if L]).astype(np.float32)
+    T = np.concatenate([[base.type[rows[s][i]] for (s, i) in L] for L in lists if L]).astype(np.uint8)
+    U = np.concatenate([[base.u[rows[s][i]] for (s, i) in L] for L in lists if L]).astype(np.float32)
+    cnt = np.array([len(L) for L in lists], np.int64)
+    P = _wrap(P.astype(np.float64), box).astype(np.float32)
+    inp = _finish(P, V, M, cnt, box, rng, typ=T, u=U, meta=dict(workload="fof_groups", seed=seed))
+    group_off = np.arange(0, len(cnt) + 1, per, dtype=np.int64)
+    return inp, group_off

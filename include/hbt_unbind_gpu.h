@@ -269,6 +269,37 @@ int hbtg_subhalo_properties_device(hbtg_handle *handle, const hbtg_params *param
 int hbtg_subhalo_properties(hbtg_handle *handle, const hbtg_params *params, const hbtg_batch *batch,
                             int32_t snapshot_id, double source_relax, hbtg_props *props);
 
+/* ------------------------------------------------------------------------
+ * Particle reassignment before unbinding (hydro runs): each non-tracer
+ * particle looks up its NumNeighboursForReassignment nearest tracer particles
+ * of its FoF group; if none of them belongs to its own subhalo, it moves to
+ * the subhalo of the nearest one (SubhaloSnapshot_t::ReassignParticles,
+ * src/subhalo_reassign_gas.cpp:65-197, with GeoTree_t::NearestNeighbours,
+ * src/geometric_tree.cpp:108-142, whose widening searches count a particle
+ * once per search that finds it).
+ * ------------------------------------------------------------------------ */
+typedef struct hbtg_reassign
+{
+  int64_t n_groups;         /* FoF groups */
+  const int64_t *group_off; /* [n_groups+1] each group's subhaloes as a range of subhalo indices (host) */
+  int64_t n_sub;
+  const int64_t *offsets;   /* [n_sub+1] each subhalo's particles (host) */
+  const float *pos;         /* [3N] comoving positions */
+  const uint8_t *type;      /* [N] particle types (tracers: params.tracer_type_mask) */
+  int64_t *dest;            /* [N] out: the subhalo the particle moves to, or -1 to stay */
+} hbtg_reassign;
+
+/* Decides every move of a batch of FoF groups (the caller appends each moved
+ * particle to its destination's source, in subhalo then particle order, and
+ * drops it from its own, as ReassignParticles does).  Uses params' box,
+ * periodic flag, softening (SofteningHalo: the first search radius is a tenth
+ * of it) and tracer_type_mask; num_neighbours is NumNeighboursForReassignment
+ * (at most 32).  The _device form takes device pos, type and dest. */
+int hbtg_reassign_particles_device(hbtg_handle *handle, const hbtg_params *params, const hbtg_reassign *batch,
+                                   int num_neighbours, void *cuda_stream);
+int hbtg_reassign_particles(hbtg_handle *handle, const hbtg_params *params, const hbtg_reassign *batch,
+                            int num_neighbours);
+
 /* Measurement utility, no counterpart in the reference: FP32 FMA throughput
  * of the device in TFLOP/s (the roofline denominator of the tree walk). */
 int hbtg_measure_fp32_peak(int device, double *tflops);

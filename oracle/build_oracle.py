@@ -24,7 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
 REF_ROOT = os.environ.get("HBTG_REFERENCE_ROOT", "/root/reference")
 REF_SOURCES = ["subhalo_unbind", "gravity_tree", "config_parser", "mymath", "mpi_wrapper",
-               "subhalo", "subhalo_merge", "snapshot"]
+               "subhalo", "subhalo_merge", "snapshot", "geometric_tree"]
 COMMON = ["-std=c++14", "-O3", "-fopenmp", "-fPIC", "-ffp-contract=off", "-DHBT_INT8", "-DINPUT_INT8"]
 VARIANTS = {
     "dmo": ["-DDM_ONLY", "-DMEASURE_UNBINDING_TIME"],

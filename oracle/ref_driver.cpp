@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "config_parser.h"
+#include "geometric_tree.h"
 #include "snapshot.h"
 #include "subhalo.h"
 
@@ -341,6 +342,83 @@ extern "C" int ref_recursive_unbind(const hbtg_params *p, hbtg_batch *b, const i
     sink_track[s] = subs[s].SinkTrackId;
     snap_sink[s] = subs[s].SnapshotOfSink;
     snap_death[s] = subs[s].SnapshotOfDeath;
+  }
+  return HBTG_OK;
+}
+
+namespace
+{
+/* Positions only: what GeoTree_t needs of a snapshot. */
+class PositionSnapshot_t : public Snapshot_t
+{
+  HBTxyz zero{{0.f, 0.f, 0.f}};
+
+public:
+  std::vector<HBTxyz> x;
+  HBTInt size() const override { return (HBTInt)x.size(); }
+  const HBTxyz &GetComovingPosition(const HBTInt i) const override { return x[i]; }
+  const HBTxyz GetPhysicalVelocity(const HBTInt) const override { return zero; }
+  HBTReal GetMass(const HBTInt) const override { return 1.f; }
+};
+} // namespace
+
+/* The moves of ReassignParticles (src/subhalo_reassign_gas.cpp:65-197) for a
+ * batch of FoF groups, with the reference's own GeoTree_t::NearestNeighbours
+ * (src/geometric_tree.cpp:108-142) over the tracers of each group. */
+extern "C" int ref_reassign(const hbtg_params *p, hbtg_reassign *r, int num_neighbours)
+{
+  if (!p || !r || r->n_groups < 0)
+    return HBTG_ERR_INVALID;
+  HBTConfig.BoxSize = p->box_size;
+  HBTConfig.BoxHalf = HBTConfig.BoxSize / 2.;
+  HBTConfig.PeriodicBoundaryOn = p->periodic != 0;
+  HBTConfig.SofteningHalo = p->softening;
+  HBTConfig.TreeNodeResolution = p->tree_node_resolution;
+  HBTConfig.TreeNodeResolutionHalf = HBTConfig.TreeNodeResolution / 2.;
+  HBTConfig.TracerParticleBitMask = p->tracer_type_mask;
+  srand48(p->seed);
+  auto is_tracer = [&](int64_t g) { return ((1 << (int)r->type[g]) & p->tracer_type_mask) != 0; };
+  for (int64_t g = 0; g < r->offsets[r->n_sub]; g++)
+    r->dest[g] = -1;
+  for (int64_t h = 0; h < r->n_groups; h++)
+  {
+    PositionSnapshot_t tracers;
+    std::vector<int64_t> tracer_sub;
+    int64_t non_tracers = 0;
+    for (int64_t s = r->group_off[h]; s < r->group_off[h + 1]; s++)
+      for (int64_t g = r->offsets[s]; g < r->offsets[s + 1]; g++)
+        if (is_tracer(g))
+        {
+          tracers.x.push_back(HBTxyz{{r->pos[3 * g], r->pos[3 * g + 1], r->pos[3 * g + 2]}});
+          tracer_sub.push_back(s);
+        }
+        else
+          non_tracers++;
+    if (non_tracers == 0 || tracers.x.empty())
+      continue;
+    GeoTree_t tree;
+    tree.Build(tracers);
+    for (int64_t s = r->group_off[h]; s < r->group_off[h + 1]; s++)
+      for (int64_t g = r->offsets[s]; g < r->offsets[s + 1]; g++)
+      {
+        if (is_tracer(g))
+          continue;
+        const HBTxyz centre{{r->pos[3 * g], r->pos[3 * g + 1], r->pos[3 * g + 2]}};
+        const std::vector<HBTInt> ngb = tree.NearestNeighbours(centre, num_neighbours, HBTConfig.SofteningHalo * 0.1);
+        bool found = false;
+        for (auto i : ngb)
+          if (tracer_sub[i] == s)
+          {
+            found = true;
+            break;
+          }
+        if (!found && !ngb.empty())
+        {
+          const int64_t to = tracer_sub[ngb.back()];
+          if (to >= 0 && to != s)
+            r->dest[g] = to;
+        }
+      }
   }
   return HBTG_OK;
 }

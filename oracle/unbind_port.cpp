@@ -23,6 +23,8 @@
  *     Snapshot_t::SphericalOverdensitySize src/snapshot.cpp:258-282)
  *   Subhalo_t::CalculateShape             src/subhalo.cpp:245-309
  *   Subhalo_t::TruncateSource             src/subhalo_unbind.cpp:843-853
+ *   SubhaloSnapshot_t::ReassignParticles  src/subhalo_reassign_gas.cpp:65-197 (with
+ *     GeoTree_t::NearestNeighbours        src/geometric_tree.cpp:108-142)
  * and potential subsampling (MaxSampleSizeOfPotentialEstimate > 0):
  *   PrepareParticlesForSubsampling        src/subhalo_unbind.cpp:430-443
  *   Get/SetMassUpscaleFactor[PerType]     src/subhalo_unbind.cpp:290-391
@@ -1108,5 +1110,120 @@ extern "C" int oracle_subhalo_properties(const hbtg_params *p, const hbtg_batch 
 #pragma omp parallel for schedule(dynamic, 1)
   for (int64_t s = 0; s < b->n_sub; s++)
     properties_one(b, s, snapshot_id, source_relax, c, o);
+  return HBTG_OK;
+}
+
+/* ------------------------------------------------------------------------
+ * ReassignParticles (src/subhalo_reassign_gas.cpp:65-197).  The neighbour
+ * list of GeoTree_t::NearestNeighbours (src/geometric_tree.cpp:108-142)
+ * follows from the distances alone: searches j = 0, 1, ... with radius R_j
+ * (R_0 = SofteningHalo / 10 in float, each 1.26 times the last, rounded to
+ * float) collect every tracer with |dx|, |dy|, |dz| <= R_j and
+ * r^2 < R_j * R_j (float product) into one collector, until it holds
+ * min(tracers, k); the collector keeps the k smallest r^2 of everything it
+ * was given, so a tracer found by m searches counts m times.  The list is
+ * the distinct tracers of those k, its last entry the nearest.
+ * ------------------------------------------------------------------------ */
+namespace
+{
+struct Cand
+{
+  double d2;
+  int64_t i;
+  int jmin;
+};
+} // namespace
+
+extern "C" int oracle_reassign(const hbtg_params *p, hbtg_reassign *r, int k)
+{
+  if (!p || !r || r->n_groups < 0 || k <= 0)
+    return HBTG_ERR_INVALID;
+  const float boxf = (float)p->box_size, halff = (float)((double)boxf / 2.);
+  const bool periodic = p->periodic != 0;
+  const float r0 = (float)((double)(float)p->softening * 0.1);
+  auto is_tracer = [&](int64_t g) { return ((1 << (int)r->type[g]) & p->tracer_type_mask) != 0; };
+  auto nearest = [&](double x) {
+    return x > (double)halff ? x - (double)boxf : (x < -(double)halff ? x + (double)boxf : x);
+  };
+  for (int64_t g = 0; g < r->offsets[r->n_sub]; g++)
+    r->dest[g] = -1;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t h = 0; h < r->n_groups; h++)
+  {
+    std::vector<int64_t> tr, tr_sub;
+    int64_t non_tracers = 0;
+    for (int64_t s = r->group_off[h]; s < r->group_off[h + 1]; s++)
+      for (int64_t g = r->offsets[s]; g < r->offsets[s + 1]; g++)
+        if (is_tracer(g))
+        {
+          tr.push_back(g);
+          tr_sub.push_back(s);
+        }
+        else
+          non_tracers++;
+    if (non_tracers == 0 || tr.empty())
+      continue;
+    const int64_t nt = (int64_t)tr.size();
+    const int64_t to_find = nt < k ? nt : k;
+    std::vector<Cand> c(nt);
+    for (int64_t s = r->group_off[h]; s < r->group_off[h + 1]; s++)
+      for (int64_t g = r->offsets[s]; g < r->offsets[s + 1]; g++)
+      {
+        if (is_tracer(g))
+          continue;
+        for (int64_t i = 0; i < nt; i++)
+        {
+          double d[3];
+          double dmax = 0.;
+          for (int q = 0; q < 3; q++)
+          {
+            d[q] = (double)r->pos[3 * tr[i] + q] - (double)r->pos[3 * g + q];
+            if (periodic)
+              d[q] = nearest(d[q]);
+            dmax = std::max(dmax, std::fabs(d[q]));
+          }
+          const double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          int j = 0;
+          for (float R = r0;; R = (float)((double)R * 1.26), j++)
+            if (dmax <= (double)R && d2 < (double)(R * R))
+              break;
+          c[i] = Cand{d2, i, j};
+        }
+        std::stable_sort(c.begin(), c.end(), [](const Cand &a, const Cand &b) { return a.d2 < b.d2; });
+        /* the last search J: the first with sum over j <= J of N_j >= to_find,
+           N_j = tracers that search j collects (jmin <= j) */
+        int J = 0;
+        for (int64_t cum = 0;; J++)
+        {
+          for (const Cand &q : c)
+            if (q.jmin <= J)
+              cum++;
+          if (std::min<int64_t>(cum, k) >= to_find)
+            break;
+        }
+        /* the k smallest r^2 of the collected multiset (a tracer counts J - jmin + 1 times) */
+        int64_t taken = 0;
+        bool found = false;
+        int64_t first = -1;
+        for (const Cand &q : c)
+        {
+          if (q.jmin > J)
+            continue;
+          if (taken >= k)
+            break;
+          if (first < 0)
+            first = q.i;
+          if (tr_sub[q.i] == s)
+            found = true;
+          taken += J - q.jmin + 1;
+        }
+        if (!found && first >= 0)
+        {
+          const int64_t to = tr_sub[first];
+          if (to >= 0 && to != s)
+            r->dest[g] = to;
+        }
+      }
+  }
   return HBTG_OK;
 }

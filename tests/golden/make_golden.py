@@ -108,6 +108,42 @@ def make_nested():
     return path
 
 
+REASSIGN_K = (1, 10, 32)
+
+
+def make_reassign():
+    """FoF groups with gas listed in the wrong subhalo, and the moves of the
+    reference's ReassignParticles logic over its own GeoTree_t neighbour
+    search for NumNeighboursForReassignment in REASSIGN_K."""
+    inp, group_off = synthetic.fof_groups(seed=1)
+    prm = abi.parity_params(thermal=1, box_size=300.0)
+    d = {"group_off": group_off}
+    for k in ("offsets", "pos", "type"):
+        d["in_" + k] = getattr(inp, k)
+    for k, v in prm.as_dict().items():
+        d["prm_" + k] = np.array(v)
+    for k in REASSIGN_K:
+        d["dest_%d" % k] = oracle.reassign(inp, group_off, prm, k, reference=True)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reassign_fof.npz")
+    np.savez_compressed(path, **d)
+    return path
+
+
+def load_reassign(path):
+    """(Inputs with offsets, pos and type; group_off; params; {k: reference dest})."""
+    z = np.load(path)
+    n = int(z["in_offsets"][-1])
+    S = len(z["in_offsets"]) - 1
+    zero3 = np.zeros((S, 3), np.float32)
+    inp = abi.Inputs(z["in_offsets"], z["in_pos"], np.zeros((n, 3), np.float32), np.ones(n, np.float32),
+                     np.arange(n, dtype=np.int64), z["in_type"], None, zero3, zero3, zero3, zero3,
+                     np.zeros(S, np.int64))
+    prm = abi.Params()
+    for k, _ in abi.Params._fields_:
+        setattr(prm, k, z["prm_" + k].item())
+    return inp, z["group_off"], prm, {k: z["dest_%d" % k] for k in REASSIGN_K}
+
+
 def load_props(path):
     """(initial in/out property values, reference properties, snapshot id,
     SourceSubRelaxFactor) of a properties fixture."""
@@ -132,6 +168,8 @@ if __name__ == "__main__":
     only = sys.argv[1:]
     if not only or "nested_merge" in only:
         print(make_nested())
+    if not only or "reassign_fof" in only:
+        print(make_reassign())
     for name in CASES:
         if only and name not in only:
             continue

@@ -14,7 +14,7 @@ from parity import assert_full_parity, assert_parity, check_invariants, compare
 pytestmark = pytest.mark.gpu
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("nested"))
+                if not os.path.basename(p).startswith(("nested", "reassign")))
 
 
 def _load_golden(path):

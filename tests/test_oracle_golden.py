@@ -10,7 +10,7 @@ import pytest
 from hbtg import oracle
 
 GOLDEN = sorted(p for p in glob.glob(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "*.npz"))
-                if not os.path.basename(p).startswith("nested"))
+                if not os.path.basename(p).startswith(("nested", "reassign")))
 
 
 def _module(path):
@@ -58,3 +58,15 @@ def test_port_properties_match_reference_golden(path):
         assert np.array_equal(getattr(got, k), v), (k, np.nonzero(getattr(got, k) != v))
     assert np.isfinite(props["r200"]).all() and (props["r200"] > 0).any()
     assert (props["snap_last"] == snap).any() and (props["snap_last"] != snap).any()
+
+
+def test_port_reassignment_matches_reference_golden():
+    """ReassignParticles' moves from the restatement's multiplicity reading of
+    NearestNeighbours equal those of the reference's own neighbour search."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reassign_fof.npz")
+    mod = _module(path)
+    inp, group_off, prm, ref = mod.load_reassign(path)
+    for k, dest in ref.items():
+        got = oracle.reassign(inp, group_off, prm, k)
+        assert np.array_equal(got, dest), (k, np.nonzero(got != dest))
+    assert (ref[10] >= 0).sum() > 100
