@@ -161,7 +161,9 @@ struct IterationDriver
     check();
   }
 
-  void build_tree(int src_total)
+  // geometric: per-cell bounding boxes and leaf source indices (k_tree_bounds,
+  // k_tree_leaf_ids) instead of mass moments.
+  void build_tree(int src_total, bool geometric = false)
   {
     const unsigned sb = grid_for(S + 1, 256);
     mem.check(cudaMemsetAsync(D.fb_count, 0, sizeof(int), st));
@@ -190,7 +192,15 @@ struct IterationDriver
     {
       if (L > 21)
         continue; // keys have 21 digits: no cell below level 21
-      k_tree_moments<<<mg, 256, 0, st>>>(D, L);
+      if (geometric)
+        k_tree_bounds<<<mg, 256, 0, st>>>(D, L);
+      else
+        k_tree_moments<<<mg, 256, 0, st>>>(D, L);
+      launches++;
+    }
+    if (geometric)
+    {
+      k_tree_leaf_ids<<<grid_for(src_total, 256), 256, 0, st>>>(D, src_total);
       launches++;
     }
     check();

@@ -993,6 +993,71 @@ __global__ void k_tree_moments(DevState D, int L)
   }
 }
 
+// Geometric trees (neighbour searches): each cell's bounding box of its
+// particles instead of its mass moments, from its children, deepest level
+// first.  Slots of a cell: (lo.x, lo.y, lo.z, -threshold), (hi.x, skip,
+// hi.y, hi.z); a leaf's w holds its source index (int bits) once
+// k_tree_leaf_ids has run.
+__global__ void k_tree_bounds(DevState D, int L)
+{
+  int off = 0;
+  for (int l = 0; l < L; l++)
+    off += D.lvl[l];
+  const int n = D.lvl[L];
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
+  {
+    const int slot = D.cell_list[off + c];
+    const int end = __float_as_int(D.nodes[slot + 1].y);
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    int ch = slot + 2;
+    while (ch < end)
+    {
+      const float4 a = D.nodes[ch];
+      int nx;
+      if (slot_is_cell(a.w))
+      {
+        const float4 b = D.nodes[ch + 1];
+        lo[0] = fminf(lo[0], a.x);
+        lo[1] = fminf(lo[1], a.y);
+        lo[2] = fminf(lo[2], a.z);
+        hi[0] = fmaxf(hi[0], b.x);
+        hi[1] = fmaxf(hi[1], b.z);
+        hi[2] = fmaxf(hi[2], b.w);
+        nx = __float_as_int(b.y);
+      }
+      else
+      {
+        lo[0] = fminf(lo[0], a.x);
+        lo[1] = fminf(lo[1], a.y);
+        lo[2] = fminf(lo[2], a.z);
+        hi[0] = fmaxf(hi[0], a.x);
+        hi[1] = fmaxf(hi[1], a.y);
+        hi[2] = fmaxf(hi[2], a.z);
+        nx = ch + 1;
+      }
+      ch = max(nx, ch + 1); // strictly increasing
+    }
+    float *c0 = reinterpret_cast<float *>(&D.nodes[slot]);
+    float *c1 = reinterpret_cast<float *>(&D.nodes[slot + 1]);
+    c0[0] = lo[0];
+    c0[1] = lo[1];
+    c0[2] = lo[2];
+    c1[0] = hi[0];
+    c1[2] = hi[1];
+    c1[3] = hi[2];
+  }
+}
+
+// Leaf slots of a geometric tree carry their source index in w.
+__global__ void k_tree_leaf_ids(DevState D, int total)
+{
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total)
+    return;
+  const int slot = j + 2 * D.X[j] + 2 * D.cnt[j];
+  reinterpret_cast<int *>(&D.nodes[slot])[3] = (int)D.val[j];
+}
+
 // ---------------------------------------------------------------------------
 // Softened potential kernel of the tree walk (walk.cuh)
 // ---------------------------------------------------------------------------

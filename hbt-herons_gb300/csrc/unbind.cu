@@ -18,6 +18,7 @@
 #include "common.cuh"
 #include "driver.cuh"
 #include "props.cuh"
+#include "reassign.cuh"
 #include "kernels.cuh"
 #include "primitives.cuh"
 #include "warm.cuh"
@@ -138,6 +139,7 @@ enum Slot
   S_POTI, S_WCTR, S_FRAMEW,
   S_PR_OFF, S_PR_CNT, S_PR_FIN, S_PR_RR, S_PR_MM, S_PR_K, S_PR_V, S_PR_KA, S_PR_VA, S_PR_MC, S_PR_VK, S_PR_SO,
   S_PR_SH, S_PR_SCR, S_PR_POS, S_PR_MASS, S_PR_ORD, S_PR_NB, S_PR_MBND, S_PR_MBP, S_PR_OUTF, S_PR_OUTI, S_PR_OUTL,
+  S_RE_OFF, S_RE_SG, S_RE_GP, S_RE_FL, S_RE_RK, S_RE_TG, S_RE_TS, S_RE_GO, S_RE_POS, S_RE_TY, S_RE_DEST,
   S_NUM
 };
 
@@ -1056,6 +1058,179 @@ int props_call(void *arg)
   return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Particle reassignment (reassign.cuh)
+// ---------------------------------------------------------------------------
+struct ReassignCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  const hbtg_reassign *r;
+  int k;
+  cudaStream_t st;
+  bool host = false;
+};
+
+int reassign_run(hbtg_handle *H, const hbtg_params *p, const hbtg_reassign *r, int k, cudaStream_t st,
+                 int64_t &launches)
+{
+  const int S = (int)r->n_sub, G = (int)r->n_groups;
+  const long long N = r->offsets[S];
+  Pool &P = H->pool;
+  std::vector<int> sub_group(std::max(S, 1));
+  std::vector<long long> gpart(G + 1);
+  for (int h = 0; h < G; h++)
+    for (long long s = r->group_off[h]; s < r->group_off[h + 1]; s++)
+      sub_group[s] = h;
+  for (int h = 0; h <= G; h++)
+    gpart[h] = r->offsets[r->group_off[h]];
+  ReState Q;
+  Q.S = S;
+  Q.G = G;
+  long long *off = P.get<long long>(S_RE_OFF, (size_t)S + 1);
+  int *sg = P.get<int>(S_RE_SG, (size_t)std::max(S, 1));
+  long long *gp = P.get<long long>(S_RE_GP, (size_t)G + 1);
+  HBTG_CUDA(cudaMemcpyAsync(off, r->offsets, sizeof(long long) * (S + 1), cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(sg, sub_group.data(), sizeof(int) * S, cudaMemcpyHostToDevice, st));
+  HBTG_CUDA(cudaMemcpyAsync(gp, gpart.data(), sizeof(long long) * (G + 1), cudaMemcpyHostToDevice, st));
+  Q.off = off;
+  Q.sub_group = sg;
+  Q.gpart = gp;
+  Q.pos = r->pos;
+  Q.type = r->type;
+  Q.dest = reinterpret_cast<long long *>(r->dest);
+  Q.flags = P.get<int>(S_RE_FL, (size_t)N + 1);
+  Q.rank = P.get<int>(S_RE_RK, (size_t)N + 1);
+  Q.tracer_mask = p->tracer_type_mask;
+  Q.box = (float)p->box_size;
+  Q.half = (float)((double)Q.box / 2.);
+  Q.periodic = p->periodic != 0;
+  Q.r0 = (float)((double)(float)p->softening * 0.1); // HBTConfig.SofteningHalo * 0.1 as a float radius
+  Q.eps = 16.f * std::ldexp(std::max(Q.box, 1.f), -23); // float rounding of unwrapped coordinates
+  Q.k = k;
+  k_re_flags<<<blocks_for(N + 1, 256), 256, 0, st>>>(Q, N);
+  launches++;
+  HBTG_CUDA(cudaGetLastError());
+  scan<int, false>(Q.flags, Q.rank, N + 1, P.get<int>(S_SCRATCH, scan_scratch_elems<int>(N + 1)), st, &launches);
+  const int T = read_int(Q.rank + N, st);
+  const size_t t1 = (size_t)std::max(T, 1);
+  Q.tg = P.get<int>(S_RE_TG, t1);
+  Q.tsub = P.get<int>(S_RE_TS, t1);
+
+  PoolMem mem{H, st, {}};
+  IterationDriver<PoolMem> R(mem, st);
+  R.K = make_kparams(p, false);
+  R.S = G;
+  int bits = 0;
+  while ((1LL << bits) < G)
+    bits++;
+  R.seg_bits = bits;
+  R.sm_count = H->sm_count;
+  DevState &D = R.D;
+  D.S = G;
+  D.N = T;
+  long long *goff = P.get<long long>(S_RE_GO, (size_t)G + 1);
+  k_re_goff<<<blocks_for(G + 1, 256), 256, 0, st>>>(Q, goff);
+  launches++;
+  D.off = goff;
+  D.pm = P.get<float4>(S_PM, t1);
+  D.ty = P.get<uint8_t>(S_TY, t1);
+  D.seg_of = P.get<int>(S_SEG, t1);
+  D.ord = P.get<int>(S_ORD, t1);
+  int *subi = P.get<int>(S_SUBI, (size_t)(G + 1) * 28);
+  int q = 0;
+  auto nexti = [&]() { return subi + (size_t)(G + 1) * (q++); };
+  D.n_s = nexti(); D.nbound = nexti(); D.nlast = nexti(); D.state = nexti(); D.corr = nexti(); D.iter = nexti();
+  D.wrap = nexti(); D.tracers = nexti(); D.nb_new = nexti(); D.src_begin = nexti(); D.src_cnt = nexti();
+  D.src_off = nexti(); D.tgt_cnt = nexti(); D.chunk_cnt = nexti(); D.chunk_off = nexti(); D.part_cnt = nexti();
+  D.part_off = nexti(); D.tail_cnt = nexti(); D.tail_off = nexti(); D.fin_cnt = nexti(); D.fin_off = nexti();
+  D.sp_cnt = nexti(); D.sp_off = nexti(); D.sp_len = nexti(); D.nunsample = nexti(); D.ngrav = nexti();
+  D.factor = P.get<float>(S_FACTOR, (size_t)G * 6 + 6);
+  unsigned *bb = P.get<unsigned>(S_BB, (size_t)G * 7 + 7);
+  D.bb_lo = bb;
+  D.bb_hi = bb + 3 * (size_t)G;
+  D.root = P.get<double>(S_ROOT, (size_t)G * 4 + 4);
+  D.keyp = P.get<float>(S_KEYP, (size_t)G * 12 + 12);
+  D.key = P.get<unsigned long long>(S_KEY, t1);
+  D.key_alt = P.get<unsigned long long>(S_KEYA, t1);
+  D.val = P.get<uint32_t>(S_VAL, t1);
+  D.val_alt = P.get<uint32_t>(S_VALA, t1);
+  D.k32 = P.get<uint32_t>(S_K32, t1);
+  D.k32_alt = P.get<uint32_t>(S_K32A, t1);
+  D.perm = P.get<uint32_t>(S_PERM, t1);
+  D.perm_alt = P.get<uint32_t>(S_PERMA, t1);
+  D.fb_list = P.get<int>(S_FBL, t1);
+  D.fb_count = P.get<int>(S_FBC, 1);
+  D.cnt = P.get<int>(S_CNT, t1 + 1);
+  D.X = P.get<int>(S_X, t1 + 1);
+  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  if (T > 0)
+  {
+    k_re_pack<<<blocks_for(N, 256), 256, 0, st>>>(Q, D, N);
+    k_re_unwrap<<<blocks_for(T, 256), 256, 0, st>>>(Q, D, T);
+    launches += 2;
+  }
+  k_re_plan<<<blocks_for(G + 1, 256), 256, 0, st>>>(Q, D);
+  launches++;
+  R.check();
+  const int src_total = R.scan_counts(D.src_cnt, D.src_off, G);
+  if (src_total > 0)
+    R.build_tree(src_total, true);
+  if (N > 0)
+  {
+    k_re_query<<<blocks_for(N, 128), 128, 0, st>>>(Q, D, N);
+    launches++;
+  }
+  R.check();
+  launches += R.launches;
+  return HBTG_OK;
+}
+
+int reassign_call(void *arg)
+{
+  ReassignCall &c = *static_cast<ReassignCall *>(arg);
+  hbtg_handle *H = c.H;
+  const hbtg_reassign *r = c.r;
+  if (!c.p || !r || r->n_groups < 0 || r->n_sub < 0 || !r->group_off || !r->offsets || c.k < 1 ||
+      c.k > kMaxNeighbours)
+    return HBTG_ERR_INVALID;
+  const long long S = r->n_sub, G = r->n_groups;
+  if (r->offsets[0] != 0 || r->group_off[0] != 0 || r->group_off[G] != S || S >= (1LL << 30))
+    return HBTG_ERR_INVALID;
+  for (long long s = 0; s < S; s++)
+    if (r->offsets[s + 1] < r->offsets[s])
+      return HBTG_ERR_INVALID;
+  for (long long h = 0; h < G; h++)
+    if (r->group_off[h + 1] < r->group_off[h])
+      return HBTG_ERR_INVALID;
+  const long long N = r->offsets[S];
+  if (N >= (1LL << 30) || (N > 0 && (!r->pos || !r->type || !r->dest)))
+    return HBTG_ERR_INVALID;
+  if (N == 0)
+    return HBTG_OK;
+  HBTG_CUDA(cudaSetDevice(H->device));
+  cudaStream_t st = c.st;
+  int64_t launches = 0, h2d = 0, d2h = 0;
+  int rc;
+  if (!c.host)
+    rc = reassign_run(H, c.p, r, c.k, st, launches);
+  else
+  {
+    Pool &P = H->pool;
+    hbtg_reassign d = *r;
+    d.pos = upload(P, S_RE_POS, r->pos, 3 * (size_t)N, st, h2d);
+    d.type = upload(P, S_RE_TY, r->type, (size_t)N, st, h2d);
+    d.dest = P.get<int64_t>(S_RE_DEST, (size_t)N);
+    rc = reassign_run(H, c.p, &d, c.k, st, launches);
+    download(r->dest, d.dest, (size_t)N, st, d2h);
+  }
+  HBTG_CUDA(cudaStreamSynchronize(st));
+  H->stats.kernel_launches = launches;
+  H->stats.h2d_bytes = h2d;
+  H->stats.d2h_bytes = d2h;
+  return rc;
+}
+
 struct ModelCall
 {
   hbtg_handle *H;
@@ -1196,6 +1371,23 @@ int hbtg_subhalo_properties(hbtg_handle *h, const hbtg_params *p, const hbtg_bat
     return HBTG_ERR_INVALID;
   PropsCall c{h, p, b, snapshot_id, source_relax, props, h->stream, true};
   return guarded(props_call, &c);
+}
+
+int hbtg_reassign_particles_device(hbtg_handle *h, const hbtg_params *p, const hbtg_reassign *r, int num_neighbours,
+                                   void *cuda_stream)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  ReassignCall c{h, p, r, num_neighbours, static_cast<cudaStream_t>(cuda_stream), false};
+  return guarded(reassign_call, &c);
+}
+
+int hbtg_reassign_particles(hbtg_handle *h, const hbtg_params *p, const hbtg_reassign *r, int num_neighbours)
+{
+  if (!h)
+    return HBTG_ERR_INVALID;
+  ReassignCall c{h, p, r, num_neighbours, h->stream, true};
+  return guarded(reassign_call, &c);
 }
 
 int hbtg_unbind_batch(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b)

@@ -199,6 +199,26 @@ class Unbinder:
             raise UnbindError(rc, "hbtg_subhalo_properties")
         return props
 
+    def reassign(self, inp: Inputs, group_off, params: Params, num_neighbours=10):
+        """ReassignParticles' moves for FoF groups given as ranges of subhaloes
+        (through hbtg_reassign_particles): dest[i] = the subhalo particle i
+        moves to, or -1."""
+        from .abi import CReassign
+        dest = np.full(inp.n_particles, -1, np.int64)
+        go = np.ascontiguousarray(group_off, np.int64)
+        offs = np.ascontiguousarray(inp.offsets, np.int64)
+        pos = np.ascontiguousarray(inp.pos, np.float32)
+        typ = np.ascontiguousarray(inp.type, np.uint8)
+        r = CReassign(len(go) - 1, go.ctypes.data, inp.n_sub, offs.ctypes.data, pos.ctypes.data, typ.ctypes.data,
+                      dest.ctypes.data)
+        fn = self.lib.hbtg_reassign_particles
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
+        fn.restype = C.c_int
+        rc = fn(self.h, C.byref(params), C.byref(r), int(num_neighbours))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_reassign_particles")
+        return dest
+
     def tree_potential(self, params: Params, pos, mass, targets, device="cuda:0"):
         """G/a * tree potential at the listed particles of one set
         (hbtg_tree_potential_device); numpy in, numpy float32 out."""
