@@ -182,7 +182,204 @@ public:
     }
   }
 
+  // Subhalo_t::CalculateProfileProperties and Subhalo_t::CalculateShape
+  // (src/subhalo.cpp:175-309) for every subhalo of `subs` in one GPU call,
+  // from the bound set that Unbind left (the first Nbound Particles, most
+  // bound first, ComovingMostBoundPosition the centre); with `truncate`,
+  // Subhalo_t::TruncateSource (src/subhalo_unbind.cpp:843-853) as well.
+  // source_relax is SourceSubRelaxFactor.
+  template <class Subhalo>
+  void properties(const hbtg_params &params, const std::vector<Subhalo *> &subs, const Options &opt,
+                  double source_relax, bool truncate)
+  {
+    const int64_t ns = (int64_t)subs.size();
+    std::vector<int64_t> offsets(ns + 1, 0);
+    for (int64_t s = 0; s < ns; s++)
+      offsets[s + 1] = offsets[s] + (int64_t)subs[s]->Particles.size();
+    const int64_t n = offsets[ns];
+    std::vector<float> pos(3 * n), mass(n), mbound(ns), mb_pos(3 * ns);
+    std::vector<int64_t> order(n), nbound(ns), nsource(ns);
+    std::vector<float> rmax(ns), vmax(ns), rhalf(ns), renclose(ns), r200(ns), m200(ns), last_vmax(ns),
+      rmax_last(ns), inertia(6 * ns), inertia_w(6 * ns);
+    std::vector<int32_t> snap_last(ns);
+    for (int64_t s = 0; s < ns; s++)
+    {
+      const Subhalo &sub = *subs[s];
+      for (int64_t k = 0; k < (int64_t)sub.Particles.size(); k++)
+      {
+        const auto &p = sub.Particles[k];
+        const int64_t g = offsets[s] + k;
+        for (int d = 0; d < 3; d++)
+          pos[3 * g + d] = p.ComovingPosition[d];
+        mass[g] = p.Mass;
+        order[g] = k;
+      }
+      nbound[s] = (int64_t)sub.Nbound;
+      mbound[s] = sub.Mbound;
+      for (int d = 0; d < 3; d++)
+        mb_pos[3 * s + d] = sub.ComovingMostBoundPosition[d];
+      r200[s] = sub.BoundR200CritComoving;
+      m200[s] = sub.BoundM200Crit;
+      last_vmax[s] = sub.LastMaxVmaxPhysical;
+      rmax_last[s] = sub.RmaxComovingOfLastMaxVmax;
+      snap_last[s] = sub.SnapshotOfLastMaxVmax;
+    }
+    hbtg_batch b{};
+    b.n_sub = ns;
+    b.offsets = offsets.data();
+    b.pos = pos.data();
+    b.mass = mass.data();
+    b.mostbound_pos = mb_pos.data();
+    b.order = order.data();
+    b.nbound = nbound.data();
+    b.mbound = mbound.data();
+    hbtg_props pr{rmax.data(),      vmax.data(),      rhalf.data(),   renclose.data(),
+                  r200.data(),      m200.data(),      last_vmax.data(), rmax_last.data(),
+                  snap_last.data(), inertia.data(),   inertia_w.data(), nsource.data()};
+    const int rc = hbtg_subhalo_properties(h_, &params, &b, opt.snapshot_id, source_relax, &pr);
+    if (rc != HBTG_OK)
+      throw std::runtime_error(std::string("hbtg_subhalo_properties: ") + hbtg_status_string(rc));
+    for (int64_t s = 0; s < ns; s++)
+    {
+      Subhalo &sub = *subs[s];
+      sub.RmaxComoving = rmax[s];
+      sub.VmaxPhysical = vmax[s];
+      sub.RHalfComoving = rhalf[s];
+      sub.REncloseComoving = renclose[s];
+      sub.BoundR200CritComoving = r200[s];
+      sub.BoundM200Crit = m200[s];
+      sub.LastMaxVmaxPhysical = last_vmax[s];
+      sub.RmaxComovingOfLastMaxVmax = rmax_last[s];
+      sub.SnapshotOfLastMaxVmax = snap_last[s];
+      for (int q = 0; q < 6; q++)
+      {
+        sub.InertialTensor[q] = inertia[6 * s + q];
+        sub.InertialTensorWeighted[q] = inertia_w[6 * s + q];
+      }
+      if (truncate)
+        sub.Particles.resize((size_t)nsource[s]);
+    }
+  }
+
+  // SubhaloSnapshot_t::ReassignParticles (src/subhalo_reassign_gas.cpp:65-197)
+  // over a list of FoF groups, each the subhaloes of one
+  // MemberTable.SubGroups entry in its order.  One GPU call decides every
+  // move; each moved particle is then appended to its destination's
+  // Particles (subhaloes in group order, particles in their order) and
+  // dropped from its own; each subhalo's Nbound is clamped to its particle
+  // count, the dropped particles are removed keeping the bound/unbound split
+  // (Subhalo_t::KickNullParticles, src/subhalo.cpp:394-430) and NboundType,
+  // MboundType and TracerIndex are counted again (Subhalo_t::CountParticleTypes,
+  // src/subhalo.cpp:311-392).  num_neighbours is NumNeighboursForReassignment.
+  // Returns the number of particles moved.
+  template <class Subhalo>
+  int64_t reassign(const hbtg_params &params, const std::vector<std::vector<Subhalo *>> &groups,
+                   int num_neighbours)
+  {
+    std::vector<Subhalo *> subs;
+    std::vector<int64_t> group_off(1, 0);
+    for (const auto &g : groups)
+    {
+      subs.insert(subs.end(), g.begin(), g.end());
+      group_off.push_back((int64_t)subs.size());
+    }
+    const int64_t ns = (int64_t)subs.size();
+    std::vector<int64_t> offsets(ns + 1, 0);
+    for (int64_t s = 0; s < ns; s++)
+      offsets[s + 1] = offsets[s] + (int64_t)subs[s]->Particles.size();
+    const int64_t n = offsets[ns];
+    std::vector<float> pos(3 * n);
+    std::vector<uint8_t> type(n, 0);
+    std::vector<int64_t> dest(n, -1);
+    Options with_types;
+    for (int64_t s = 0; s < ns; s++)
+      for (int64_t k = 0; k < (int64_t)subs[s]->Particles.size(); k++)
+      {
+        const auto &p = subs[s]->Particles[k];
+        const int64_t g = offsets[s] + k;
+        for (int d = 0; d < 3; d++)
+          pos[3 * g + d] = p.ComovingPosition[d];
+        set_type(type, g, p, with_types);
+      }
+    hbtg_reassign r{(int64_t)groups.size(), group_off.data(), ns, offsets.data(), pos.data(), type.data(),
+                    dest.data()};
+    const int rc = hbtg_reassign_particles(h_, &params, &r, num_neighbours);
+    if (rc != HBTG_OK)
+      throw std::runtime_error(std::string("hbtg_reassign_particles: ") + hbtg_status_string(rc));
+    int64_t moved = 0;
+    for (int64_t s = 0; s < ns; s++)
+      for (int64_t k = 0; k < offsets[s + 1] - offsets[s]; k++)
+        if (dest[offsets[s] + k] >= 0)
+        {
+          subs[dest[offsets[s] + k]]->Particles.push_back(subs[s]->Particles[k]);
+          moved++;
+        }
+    // the tidy-up runs over every group that has a non-tracer particle
+    std::vector<char> tidy(ns, 0);
+    for (size_t h = 0; h + 1 < group_off.size(); h++)
+    {
+      bool any = false;
+      for (int64_t g = offsets[group_off[h]]; g < offsets[group_off[h + 1]] && !any; g++)
+        any = ((1 << (int)type[g]) & params.tracer_type_mask) == 0;
+      for (int64_t s = group_off[h]; s < group_off[h + 1]; s++)
+        tidy[s] = any;
+    }
+    for (int64_t s = 0; s < ns; s++)
+    {
+      if (!tidy[s])
+        continue;
+      Subhalo &sub = *subs[s];
+      const int64_t len = offsets[s + 1] - offsets[s], np = (int64_t)sub.Particles.size();
+      if ((int64_t)sub.Nbound > np)
+        sub.Nbound = np;
+      int64_t keep = 0, nb = 0;
+      for (int64_t k = 0; k < np; k++)
+      {
+        if (k < len && dest[offsets[s] + k] >= 0)
+          continue;
+        if (k < (int64_t)sub.Nbound)
+          nb++;
+        if (keep != k)
+          sub.Particles[keep] = std::move(sub.Particles[k]);
+        keep++;
+      }
+      sub.Particles.resize((size_t)keep);
+      sub.Nbound = nb;
+      count_particle_types(sub, params, 0);
+    }
+    return moved;
+  }
+
 private:
+  // Subhalo_t::CountParticleTypes (src/subhalo.cpp:311-392): per-type counts
+  // and masses of the bound set (float sums in bound order) and the first
+  // tracer's index (0 when there is none).
+  template <class Subhalo>
+  static auto count_particle_types(Subhalo &sub, const hbtg_params &params, int)
+    -> decltype((void)sub.NboundType[0], (void)sub.Particles[0].Type)
+  {
+    for (int t = 0; t < HBTG_TYPE_MAX; t++)
+    {
+      sub.NboundType[t] = 0;
+      sub.MboundType[t] = 0;
+    }
+    int64_t tracer = -1;
+    for (int64_t k = 0; k < (int64_t)sub.Nbound; k++)
+    {
+      const auto &p = sub.Particles[k];
+      sub.NboundType[p.Type]++;
+      sub.MboundType[p.Type] += p.Mass;
+      if (tracer < 0 && ((1 << (int)p.Type) & params.tracer_type_mask))
+        tracer = k;
+    }
+    sub.TracerIndex = tracer < 0 ? 0 : tracer;
+  }
+  template <class Subhalo>
+  static void count_particle_types(Subhalo &sub, const hbtg_params &, ...)
+  {
+    sub.TracerIndex = 0;
+  }
+
   // Subhalo_t::MergeRecursively (src/subhalo_merge.cpp:46-92): the subtree of
   // subs[self], depth first, against `ref`.
   template <class SubhaloList, class Subhalo>

@@ -1,7 +1,8 @@
 """The C++ host shim (hbtg_unbind_shim.hpp) instantiates against types shaped
 like HBT-HERONS' Subhalo_t / Particle_t (src/subhalo.h, src/snapshot.h): with
 particle types and thermal energy (hydro build) and without them (DM_ONLY),
-for both the plain and the learned call.  A syntax-only compile, no GPU."""
+for every entry: the plain and the learned call, the nested recursion, the
+properties and the reassignment.  Syntax-only compiles, no GPU."""
 import os
 import shutil
 import subprocess
@@ -40,6 +41,9 @@ struct Subhalo
   float CoreComovingPosition[3], CorePhysicalVelocity[3], CoreComovingSigmaR, CorePhysicalSigmaV;
   int SnapshotOfDeath, SnapshotOfSink;
   std::vector<float> ParticleBindingEnergies, ParticlePotentialEnergies;
+  float RmaxComoving, VmaxPhysical, RHalfComoving, REncloseComoving, BoundR200CritComoving, BoundM200Crit;
+  float LastMaxVmaxPhysical, RmaxComovingOfLastMaxVmax, InertialTensor[6], InertialTensorWeighted[6];
+  int SnapshotOfLastMaxVmax;
   int64_t TrackId;
   std::vector<int64_t> NestedSubhalos;
 };
@@ -57,6 +61,9 @@ void use(hbtg_shim::Unbinder &u, std::vector<Subhalo<P> *> &subs, bool types)
   std::vector<Subhalo<P>> list(3);
   list[0].NestedSubhalos = {1, 2};
   u.recursive_unbind(p, list, std::vector<int64_t>{0}, o);
+  u.properties(p, subs, o, 3.0, true);
+  std::vector<std::vector<Subhalo<P> *>> groups{subs};
+  u.reassign(p, groups, 10);
 }
 
 void all(hbtg_shim::Unbinder &u, std::vector<Subhalo<HydroParticle> *> &h, std::vector<Subhalo<DmoParticle> *> &d)
@@ -100,6 +107,9 @@ void use_real(hbtg_shim::Unbinder &u, SubhaloList_t &subs, std::vector<Subhalo_t
   u.unbind_learned(p, batch, o);
   std::vector<int64_t> roots{0};
   u.recursive_unbind(p, subs, roots, o);
+  u.properties(p, batch, o, HBTConfig.SourceSubRelaxFactor, true);
+  std::vector<std::vector<Subhalo_t *>> groups{batch};
+  u.reassign(p, groups, HBTConfig.NumNeighboursForReassignment);
 }
 """
 
@@ -127,9 +137,10 @@ def test_shim_compiles_against_the_reference_headers(tmp_path, variant):
     assert r.returncode == 0, r.stderr[-4000:]
 
 
-def test_nested_driver_program_builds(tmp_path):
-    """The shim's recursive_unbind driver program (run on the GPU by
-    tests/test_shim_nested.py) compiles and links against libhbtg.so."""
+@pytest.mark.parametrize("program", ["shim_nested_driver.cpp", "shim_steps_driver.cpp"])
+def test_driver_programs_build(tmp_path, program):
+    """The shim's test programs (run on the GPU by tests/test_shim_nested.py
+    and tests/test_shim_steps.py) compile and link against libhbtg.so."""
     from hbtg.build import LIB, build_library
     build_library()
     cxx = shutil.which("g++")
@@ -137,7 +148,7 @@ def test_nested_driver_program_builds(tmp_path):
         pytest.skip("no C++ compiler")
     exe = str(tmp_path / "drv")
     cmd = [cxx, "-std=c++17", "-O2", "-Wall", "-Wno-deprecated-declarations", "-I", os.path.join(ROOT, "include"),
-           "-I", os.path.join(ROOT, "hbt-herons_gb300", "host"), os.path.join(ROOT, "tests", "shim_nested_driver.cpp"),
+           "-I", os.path.join(ROOT, "hbt-herons_gb300", "host"), os.path.join(ROOT, "tests", program),
            "-o", exe, "-L", os.path.dirname(LIB), "-lhbtg", "-Wl,-rpath," + os.path.dirname(LIB)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-4000:]
