@@ -118,24 +118,14 @@ def cpu_model():
     return platform.processor() or platform.machine()
 
 
-def sample_parity(inp, picked, gpu_out, cpu_out, prm):
-    """GPU outputs of the sampled subhaloes (from the full-batch call) against
-    the CPU leg's outputs on the same subhaloes: membership, raw bound mass,
-    most-bound IDs, status (tests/parity.py)."""
+def sample_parity(sub, gpu_out, cpu_out, prm):
+    """The plain GPU path's outputs on the sampled subhaloes (one call over
+    the sample, potentials included) against the CPU leg's outputs on the
+    same subhaloes: membership, raw bound mass, most-bound IDs, status, and
+    every float output relative to its particle's potential (tests/parity.py)."""
     sys.path.insert(0, os.path.join(HERE, "tests"))
     from parity import compare, compare_full
-    from hbtg.abi import Outputs
-    sub = inp.subset(picked)
-    rows = np.concatenate([np.arange(inp.offsets[s], inp.offsets[s + 1]) for s in picked])
-    d = {}
-    for k, v in gpu_out.__dict__.items():
-        if v is None:
-            d[k] = None
-        elif k in ("order", "energy", "potential"):
-            d[k] = v[rows]
-        else:
-            d[k] = v[picked]
-    g = Outputs(**d)
+    g = gpu_out
     m = compare(sub, g, cpu_out)
     mf, viol = compare_full(sub, g, cpu_out, prm)
     return {"subhaloes": int(sub.n_sub), "particles": int(sub.n_particles), "membership": m["membership"],
@@ -147,7 +137,7 @@ def sample_parity(inp, picked, gpu_out, cpu_out, prm):
             "violations": [[v[0], int(v[1]), str(v[2])[:160]] for v in viol[:6]]}
 
 
-def run_cpu(inp, prm, threads, inner_parallel=False):
+def run_cpu(inp, prm, threads, inner_parallel=False, want_potential=False):
     from hbtg import oracle
     ref = None
     try:
@@ -158,9 +148,10 @@ def run_cpu(inp, prm, threads, inner_parallel=False):
         ref = None
     t0 = time.perf_counter()
     if ref == "reference":
-        out = oracle.run_reference(inp, prm, nthreads=threads, inner_parallel=inner_parallel)
+        out = oracle.run_reference(inp, prm, nthreads=threads, inner_parallel=inner_parallel,
+                                   want_potential=want_potential)
     else:
-        out = oracle.run_port(inp, prm, nthreads=threads, inner_parallel=inner_parallel)
+        out = oracle.run_port(inp, prm, nthreads=threads, inner_parallel=inner_parallel, want_potential=want_potential)
     dt = time.perf_counter() - t0
     return out, dt, ref or "port"
 
@@ -236,7 +227,7 @@ def bench_reference(args):
         run_cpu(sample, prm, threads)
     times, bounds, kind = [], [], "port"
     for _ in range(args.steps):
-        out, dt, kind = run_cpu(sample, prm, threads)
+        out, dt, kind = run_cpu(sample, prm, threads, want_potential=True)
         times.append(dt)
         bounds.append(int(out.nbound.sum()))
     rate = float(np.sum(bounds) / np.sum(times))
@@ -435,7 +426,7 @@ def bench_gpu(args):
     if rank == 0 and not args.skip_cpu:
         sample, picked = cpu_sample(inp, args.cpu_sample, seed=args.seed)
         threads = os.cpu_count() or 1
-        out, dt, kind = run_cpu(sample, prm, threads)
+        out, dt, kind = run_cpu(sample, prm, threads, want_potential=True)
         # one thread on about 1e5 particles (the same stratification; decades
         # whose subhaloes exceed their share are left out)
         small, _ = cpu_sample(inp, 100_000, seed=args.seed + 1, strict=True)
@@ -446,7 +437,8 @@ def bench_gpu(args):
                               "subhaloes": int(small.n_sub), "largest": int(np.diff(small.offsets).max()),
                               "seconds": dt1}}
         if plain_out is not None:
-            parity = sample_parity(inp, picked, plain_out, out, prm)
+            g = u.unbind(sample, prm, want_potential=True)
+            parity = sample_parity(sample, g, out, prm)
             parity["against"] = "plain GPU path vs CPU %s on the sampled subhaloes" % kind
 
     if rank == 0:
@@ -469,6 +461,11 @@ def bench_gpu(args):
                                              "plain": plain and plain["counted"]["global_iterations"]},
                        "interactions_per_step": {"learned": cw["interactions"],
                                                  "plain": plain and plain["counted"]["interactions"]},
+                       "walk_traversal_per_step": {k[5:]: cw[k] for k in (
+                           "walk_steps", "walk_nodes", "walk_pending_batches", "walk_entries_full",
+                           "walk_entries_part", "walk_entries_near", "walk_drained")},
+                       "walk_cycles_per_step": dict(zip(("pop", "resolve", "write", "eval_full", "eval_far",
+                                                         "eval_near", "drain", "groups"), cw["walk_cycles"])),
                        "arm": args.arm, "parallelism": "dp%d" % world},
             "plain": plain and {"value": plain["value"], "ms_per_step": plain["t_max"] / args.steps,
                                 "bound_per_step": plain["total_bound"] / args.steps,
@@ -484,6 +481,7 @@ def bench_gpu(args):
                     "ms_per_call": 1e3 * float(np.mean(e2e_times)),
                     "ms_device_part": float(np.mean(e2e_device)), "ms_uploads": h2d_ms, "ms_downloads": d2h_ms},
             "gpu_launches": warm["kernel_launches"] // args.steps,
+            "host_syncs_per_step": warm["last"].get("host_syncs"),
             "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
                          "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
                          "peak_source": "FP32 FMA throughput measured in-process (hbtg_measure_fp32_peak)",

@@ -50,6 +50,7 @@ struct IterationDriver
   int64_t launches = 0;
   int64_t walk_launches = 0;
   int64_t tree_nodes = 0;
+  int64_t host_syncs = 0; // stream synchronisations for host reads of device totals
   int global_iter = 0;
 
   IterationDriver(Mem &m, cudaStream_t s) : mem(m), st(s)
@@ -71,6 +72,7 @@ struct IterationDriver
     int h = 0;
     mem.check(cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, st));
     mem.check(cudaStreamSynchronize(st));
+    host_syncs++;
     return h;
   }
 
@@ -102,6 +104,7 @@ struct IterationDriver
     mem.check(cudaMemcpyAsync(&tot[1], o1 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
     mem.check(cudaMemcpyAsync(&tot[2], o2 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
     mem.check(cudaStreamSynchronize(st));
+    host_syncs++;
   }
 
   // Exclusive scan of n counts plus a trailing zero; returns the total.
@@ -165,6 +168,8 @@ struct IterationDriver
   // k_tree_leaf_ids) instead of mass moments.
   void build_tree(int src_total, bool geometric = false)
   {
+    if (src_total <= 0)
+      return;
     const unsigned sb = grid_for(S + 1, 256);
     mem.check(cudaMemsetAsync(D.fb_count, 0, sizeof(int), st));
     D.lvl = mem.level_counts();
@@ -186,12 +191,10 @@ struct IterationDriver
     tree_nodes += internal;
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
     launches++;
-    // cell multipoles bottom-up, one launch per level (deepest first)
+    // cell multipoles (or bounding boxes) bottom-up, one launch per level, deepest first
     const unsigned mg = std::max(1u, std::min(grid_for(internal, 256), (unsigned)sm_count * 8u));
-    for (int L = kLevels - 1; L >= 0; L--)
+    for (int L = 21; L >= 0; L--) // keys have 21 digits: no cell below level 21
     {
-      if (L > 21)
-        continue; // keys have 21 digits: no cell below level 21
       if (geometric)
         k_tree_bounds<<<mg, 256, 0, st>>>(D, L);
       else
@@ -378,6 +381,16 @@ struct IterationDriver
       launches++;
     }
     k_epilogue<<<sb, 256, 0, st>>>(D, K, O);
+    if (O.mbound_type)
+    {
+      if (K.dm_only)
+        mem.check(cudaMemsetAsync(O.mbound_type, 0, sizeof(float) * 6 * (size_t)S, st));
+      else
+      {
+        k_type_masses<<<grid_for((long long)S * kWarp, 256), 256, 0, st>>>(D, O.mbound_type);
+        launches++;
+      }
+    }
     launches++;
     check();
     mem.mark(5);

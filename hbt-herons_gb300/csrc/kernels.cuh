@@ -102,10 +102,10 @@ struct DevState
   unsigned long long *key, *key_alt;
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
   int *cnt, *X, *flags, *F;
-  int *cell_list; // tree cells (first slot) grouped by level (k_tree_emit), for the multipole pass
+  int *cell_list; // tree cells (first slot) grouped by level (k_tree_emit), for the bottom-up passes
   int *lvl;       // [2 kLevels]: cells per level (k_tree_count), fill cursors (k_tree_emit)
   float4 *nodes; // tree slots (see slot_is_cell)
-  unsigned long long *interactions;
+  unsigned long long *interactions; // [kWalkCounters]: interactions, then the walk's traversal counters
   int *nb1 = nullptr; // Nbound after the first iteration (training traces), or null
   unsigned *walk_ctr = nullptr; // per-SM chunk counters of the walk (zeroed before each walk), or null
   // warm start (null on the plain path)
@@ -120,6 +120,12 @@ struct DevState
 
 // Tree levels: keys hold 21 digits, so cells sit at levels 0..21.
 constexpr int kLevels = 32;
+// walk counters (with counting on): interactions, traversal steps, nodes
+// popped, pending-cell batches, entries of the three lists, drained ranges,
+// then warp clock cycles spent in: popping and classifying, resolving
+// pending cells, list and stack writes, the three list evaluations,
+// draining, and whole target groups
+constexpr int kWalkCounters = 16;
 
 __device__ __forceinline__ int lcp_levels(unsigned long long a, unsigned long long b)
 {
@@ -927,13 +933,66 @@ __global__ void k_tree_emit(DevState D, KParams K, int total)
   }
 }
 
-// Mass and centre of mass of the cells of level L, from their children
+// Mass and centre of mass of a cell from its children
 // (GravityTree_t::UpdateInternalNodes / ProcessNode / FillNodeCenter,
 // src/gravity_tree.cpp:18-80): children in octant order (their slot order),
 // each child's float mass and float position (a leaf) or float centre (a
 // cell) accumulated in double, then stored as float -- the reference's own
 // rounding, so a cell's centre carries its children's roundings as in the
-// reference.  Levels are processed deepest first, one launch per level.
+// reference.
+// The multipoles of the cell at `slot` from its children.
+__device__ __forceinline__ void cell_moments(const DevState &D, int slot)
+{
+  const int end = __float_as_int(D.nodes[slot + 1].y);
+  double M = 0., X = 0., Y = 0., Z = 0.;
+  float fx = 0.f, fy = 0.f, fz = 0.f; // first child's position (a massless cell)
+  int ch = slot + 2;
+  while (ch < end)
+  {
+    const float4 a = D.nodes[ch];
+    float m;
+    int nx;
+    if (slot_is_cell(a.w))
+    {
+      const float4 b = D.nodes[ch + 1];
+      m = b.x;
+      nx = __float_as_int(b.y);
+    }
+    else
+    {
+      m = a.w;
+      nx = ch + 1;
+    }
+    if (ch == slot + 2)
+    {
+      fx = a.x;
+      fy = a.y;
+      fz = a.z;
+    }
+    const double md = (double)m;
+    M = __dadd_rn(M, md);
+    X = __fma_rn((double)a.x, md, X); // the product is exact in double
+    Y = __fma_rn((double)a.y, md, Y);
+    Z = __fma_rn((double)a.z, md, Z);
+    ch = max(nx, ch + 1); // strictly increasing
+  }
+  float *cs = reinterpret_cast<float *>(&D.nodes[slot]);
+  if (M > 0.)
+  {
+    cs[0] = __double2float_rn(__ddiv_rn(X, M));
+    cs[1] = __double2float_rn(__ddiv_rn(Y, M));
+    cs[2] = __double2float_rn(__ddiv_rn(Z, M));
+  }
+  else
+  {
+    cs[0] = fx;
+    cs[1] = fy;
+    cs[2] = fz;
+  }
+  reinterpret_cast<float *>(&D.nodes[slot + 1])[0] = __double2float_rn(M);
+}
+
+// The cells of level L (deepest level first, one launch per level).
 __global__ void k_tree_moments(DevState D, int L)
 {
   int off = 0;
@@ -941,56 +1000,7 @@ __global__ void k_tree_moments(DevState D, int L)
     off += D.lvl[l];
   const int n = D.lvl[L];
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x)
-  {
-    const int slot = D.cell_list[off + c];
-    const int end = __float_as_int(D.nodes[slot + 1].y);
-    double M = 0., X = 0., Y = 0., Z = 0.;
-    float fx = 0.f, fy = 0.f, fz = 0.f; // first child's position (a massless cell)
-    int ch = slot + 2;
-    while (ch < end)
-    {
-      const float4 a = D.nodes[ch];
-      float m;
-      int nx;
-      if (slot_is_cell(a.w))
-      {
-        const float2 b = *reinterpret_cast<const float2 *>(&D.nodes[ch + 1]);
-        m = b.x;
-        nx = __float_as_int(b.y);
-      }
-      else
-      {
-        m = a.w;
-        nx = ch + 1;
-      }
-      if (ch == slot + 2)
-      {
-        fx = a.x;
-        fy = a.y;
-        fz = a.z;
-      }
-      const double md = (double)m;
-      M = __dadd_rn(M, md);
-      X = __fma_rn((double)a.x, md, X); // the product is exact in double
-      Y = __fma_rn((double)a.y, md, Y);
-      Z = __fma_rn((double)a.z, md, Z);
-      ch = max(nx, ch + 1); // strictly increasing
-    }
-    float *cs = reinterpret_cast<float *>(&D.nodes[slot]);
-    if (M > 0.)
-    {
-      cs[0] = __double2float_rn(__ddiv_rn(X, M));
-      cs[1] = __double2float_rn(__ddiv_rn(Y, M));
-      cs[2] = __double2float_rn(__ddiv_rn(Z, M));
-    }
-    else
-    {
-      cs[0] = fx;
-      cs[1] = fy;
-      cs[2] = fz;
-    }
-    reinterpret_cast<float *>(&D.nodes[slot + 1])[0] = __double2float_rn(M);
-  }
+    cell_moments(D, D.cell_list[off + c]);
 }
 
 // Geometric trees (neighbour searches): each cell's bounding box of its
@@ -1658,6 +1668,56 @@ __global__ void k_epi_particles(DevState D, KParams K, OutPtrs O, int total)
   segmented_flush<7>(acc7, s, D.com);
 }
 
+// MboundType as CountParticleTypes sums it (src/subhalo.cpp:311-393): per
+// type, float additions in bound order.  One warp per subhalo: the lanes load
+// 32 bound particles at a time (the next 32 while the current ones are
+// added) and lane t replays the additions of type t in order, so the six
+// sums are the reference's sequential ones.
+__global__ void k_type_masses(DevState D, float *out)
+{
+  const int s = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (s >= D.S) // whole warps
+    return;
+  const unsigned full = 0xffffffffu;
+  const int st = D.state[s];
+  const int nb = (st == kConverged || st == kMaxIter) ? D.nbound[s] : 0;
+  const long long off = D.off[s];
+  float acc = 0.f;
+  int t = 7;
+  float m = 0.f;
+  if (lane < nb)
+  {
+    const int p = D.ord[off + lane];
+    t = D.ty[p] & 7;
+    m = D.pm[p].w;
+  }
+  for (int i0 = 0; i0 < nb; i0 += kWarp)
+  {
+    const int cur_t = t;
+    const float cur_m = m;
+    const int i = i0 + kWarp + lane;
+    t = 7;
+    m = 0.f;
+    if (i < nb)
+    {
+      const int p = D.ord[off + i];
+      t = D.ty[p] & 7;
+      m = D.pm[p].w;
+    }
+    const int cnt = min(kWarp, nb - i0);
+    for (int q = 0; q < cnt; q++)
+    {
+      const int tq = __shfl_sync(full, cur_t, q);
+      const float mq = __shfl_sync(full, cur_m, q);
+      if (tq == lane)
+        acc = __fadd_rn(acc, mq);
+    }
+  }
+  if (lane < 6)
+    out[6 * s + lane] = acc;
+}
+
 // Scalar outputs of each subhalo (one thread per subhalo): kinematics, type
 // counts, tracer index, most-bound particle and ID, core phase-space
 // properties (src/subhalo_merge.cpp:94-181), status and iterations.
@@ -1687,24 +1747,9 @@ __global__ void k_epilogue(DevState D, KParams K, OutPtrs O)
     for (int q = 0; q < 5; q++)
       O.kinematics[5 * s + q] = kin[q];
   const int *tn = reinterpret_cast<const int *>(D.bb_lo) + 6 * s;
-  // MboundType as CountParticleTypes sums it (src/subhalo.cpp:311-393): float
-  // additions in bound order (the batch runs it on one thread per subhalo)
-  float mt[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  if (O.mbound_type && !K.dm_only && resolved)
-    for (int i = 0; i < nb; i++)
-    {
-      const int p = D.ord[off + i];
-      const int t = D.ty[p] & 7;
-      if (t < 6)
-        mt[t] = __fadd_rn(mt[t], D.pm[p].w);
-    }
-  for (int t = 0; t < 6; t++)
-  {
-    if (O.nbound_type)
+  if (O.nbound_type)
+    for (int t = 0; t < 6; t++)
       O.nbound_type[6 * s + t] = resolved ? tn[t] : 0;
-    if (O.mbound_type)
-      O.mbound_type[6 * s + t] = (K.dm_only || !resolved) ? 0.f : mt[t];
-  }
   const int first_tracer = D.nb_new[s];
   long long ti;
   if (st == kEmpty)

@@ -84,7 +84,7 @@ constexpr size_t kScratchBytes =
   al(sizeof(int) * kScanScr) +               // scan scratch
   al(sizeof(int) * kCells) +                 // per-level cell lists
   al(sizeof(int) * 2 * kLevels) +            // cells per level, list cursors
-  al(sizeof(unsigned long long)) +           // interaction counter
+  al(sizeof(unsigned long long) * kWalkCounters) + // walk counters
   al(sizeof(float) * 12 * kS1) +             // working copies of the in/out frames
   al(sizeof(unsigned) * kMaxWalkRanges);     // per-SM walk chunk counters
 
@@ -313,7 +313,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   mem.scan_scr = c.take<int>(kScanScr);
   mem.cells = c.take<int>(kCells);
   mem.lvl = c.take<int>(2 * kLevels);
-  D.interactions = c.take<unsigned long long>(1);
+  D.interactions = c.take<unsigned long long>(kWalkCounters);
   float *frames = c.take<float>(12 * kS1);
   D.walk_ctr = c.take<unsigned>(kMaxWalkRanges);
   if (c.overflow || (size_t)scan_scratch_elems<int>(kN1 + kTable) > kScanScr)
@@ -334,7 +334,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
     ck(cudaMemcpyAsync(D.ref_vel, b->ref_vel, fbytes, cudaMemcpyDefault, st));
     ck(cudaMemcpyAsync(D.mb_pos, b->mostbound_pos, fbytes, cudaMemcpyDefault, st));
     ck(cudaMemcpyAsync(D.mb_vel, b->mostbound_vel, fbytes, cudaMemcpyDefault, st));
-    ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+    ck(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long) * kWalkCounters, st));
     if (N > 0)
       k_repack<<<nblocks(N, 256), 256, 0, st>>>(D, R.K, b->pos, b->vel, b->mass, b->u, b->type);
     k_init_subs<<<nblocks(S, 256), 256, 0, st>>>(D, R.K);

@@ -197,7 +197,8 @@ struct hbtg_handle
   int sm_count = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;              // uploads that only the epilogue needs (host-pointer calls)
-  cudaEvent_t copy_events[5] = {};          // host-pointer calls: copy phases and the side upload
+  cudaStream_t side2 = nullptr;             // a second copy stream: velocities up, energies down
+  cudaEvent_t copy_events[7] = {};          // host-pointer calls: copy phases and the side streams
   cudaEvent_t epilogue_wait = nullptr;      // set for one call: the epilogue waits for this event
   Pool pool;
   hbtg_stats stats{};
@@ -453,8 +454,8 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.flags = P.get<int>(S_FLAGS, n1 + 1);
   D.F = P.get<int>(S_F, n1 + 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
-  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
-  HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long), st));
+  D.interactions = P.get<unsigned long long>(S_COUNTER, kWalkCounters);
+  HBTG_CUDA(cudaMemsetAsync(D.interactions, 0, sizeof(unsigned long long) * kWalkCounters, st));
 
   if (N > 0)
   {
@@ -579,14 +580,24 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   H->stats.ms_total = ms;
   H->stats.kernel_launches = R.launches;
   H->stats.walk_launches = R.walk_launches;
+  H->stats.host_syncs = R.host_syncs;
   H->stats.walk_blocks_per_sm = R.walk_blocks_per_sm;
   H->stats.global_iterations = R.global_iter;
   H->stats.tree_nodes = R.tree_nodes;
   if (H->count_interactions)
   {
-    unsigned long long c = 0;
-    HBTG_CUDA(cudaMemcpy(&c, D.interactions, sizeof(c), cudaMemcpyDeviceToHost));
-    H->stats.interactions = (int64_t)c;
+    unsigned long long c[kWalkCounters] = {};
+    HBTG_CUDA(cudaMemcpy(c, D.interactions, sizeof(c), cudaMemcpyDeviceToHost));
+    H->stats.interactions = (int64_t)c[0];
+    H->stats.walk_steps = (int64_t)c[1];
+    H->stats.walk_nodes = (int64_t)c[2];
+    H->stats.walk_pending_batches = (int64_t)c[3];
+    H->stats.walk_entries_full = (int64_t)c[4];
+    H->stats.walk_entries_part = (int64_t)c[5];
+    H->stats.walk_entries_near = (int64_t)c[6];
+    H->stats.walk_drained = (int64_t)c[7];
+    for (int q = 0; q < 8; q++)
+      H->stats.walk_cycles[q] = (int64_t)c[8 + q];
   }
   // summary counters
   std::vector<long long> nb(S);
@@ -684,10 +695,13 @@ int host_call(void *arg)
   // the particle IDs are read only by the epilogue: their upload overlaps the iteration
   d.id = upload(P, S_ID, b->id, N, H->side, h2d);
   HBTG_CUDA(cudaEventRecord(ev[4], H->side));
+  // velocities (and thermal energies) on a second stream, concurrent with the positions
+  HBTG_CUDA(cudaStreamWaitEvent(H->side2, ev[0], 0));
+  d.vel = upload(P, S_VEL, b->vel, 3 * N, H->side2, h2d);
+  d.u = (c.p->thermal && b->u) ? upload(P, S_U, b->u, N, H->side2, h2d) : nullptr;
+  HBTG_CUDA(cudaEventRecord(ev[5], H->side2));
   d.pos = upload(P, S_POS, b->pos, 3 * N, st, h2d);
-  d.vel = upload(P, S_VEL, b->vel, 3 * N, st, h2d);
   d.mass = upload(P, S_MASS, b->mass, N, st, h2d);
-  d.u = (c.p->thermal && b->u) ? upload(P, S_U, b->u, N, st, h2d) : nullptr;
   d.type = (c.p->dm_only || !b->type) ? nullptr : upload(P, S_TYPE, b->type, N, st, h2d);
   d.ref_pos = upload(P, S_REFP, b->ref_pos, 3 * S, st, h2d);
   d.ref_vel = upload(P, S_REFV, b->ref_vel, 3 * S, st, h2d);
@@ -717,6 +731,7 @@ int host_call(void *arg)
         wa.e_prev = upload(P, S_PEN, c.prior->energy_prev, N, st, h2d);
     }
   }
+  HBTG_CUDA(cudaStreamWaitEvent(st, ev[5], 0));
   HBTG_CUDA(cudaEventRecord(ev[1], st));
   H->epilogue_wait = ev[4];
   rc = run_device(H, c.p, &d, st, c.learned ? &wa : nullptr);
@@ -724,9 +739,15 @@ int host_call(void *arg)
   if (rc != HBTG_OK && rc != HBTG_ERR_MAX_ITER)
   {
     cudaStreamSynchronize(H->side);
+    cudaStreamSynchronize(H->side2);
     return rc;
   }
   HBTG_CUDA(cudaEventRecord(ev[2], st));
+  // the per-particle energies on the second stream, concurrent with the order
+  HBTG_CUDA(cudaStreamWaitEvent(H->side2, ev[2], 0));
+  download(b->energy, d.energy, N, H->side2, d2h);
+  download(b->potential, d.potential, N, H->side2, d2h);
+  HBTG_CUDA(cudaEventRecord(ev[6], H->side2));
   download(b->order, d.order, N, st, d2h);
   download(b->nbound, d.nbound, S, st, d2h);
   download(b->mbound, d.mbound, S, st, d2h);
@@ -735,8 +756,6 @@ int host_call(void *arg)
   download(b->tracer_index, d.tracer_index, S, st, d2h);
   download(b->kinematics, d.kinematics, 5 * S, st, d2h);
   download(b->core, d.core, 8 * S, st, d2h);
-  download(b->energy, d.energy, N, st, d2h);
-  download(b->potential, d.potential, N, st, d2h);
   download(b->iterations, d.iterations, S, st, d2h);
   download(b->status, d.status, S, st, d2h);
   download(b->ref_pos, d.ref_pos, 3 * S, st, d2h);
@@ -744,6 +763,7 @@ int host_call(void *arg)
   download(b->mostbound_pos, d.mostbound_pos, 3 * S, st, d2h);
   download(b->mostbound_vel, d.mostbound_vel, 3 * S, st, d2h);
   download(b->most_bound_id, d.most_bound_id, S, st, d2h);
+  HBTG_CUDA(cudaStreamWaitEvent(st, ev[6], 0));
   HBTG_CUDA(cudaEventRecord(ev[3], st));
   HBTG_CUDA(cudaStreamSynchronize(st));
   H->stats.h2d_bytes = h2d;
@@ -828,7 +848,7 @@ int pot_call(void *arg)
   D.cnt = P.get<int>(S_CNT, n1 + 1);
   D.X = P.get<int>(S_X, n1 + 1);
   D.nodes = P.get<float4>(S_NODES, n1 * 3);
-  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  D.interactions = P.get<unsigned long long>(S_COUNTER, kWalkCounters);
   D.walk_ctr = P.get<unsigned>(S_WCTR, (size_t)std::max(H->sm_count, 1));
   HBTG_CUDA(cudaMemsetAsync(bad, 0, sizeof(int), st));
   k_pot_repack<<<blocks_for(c.ns, 256), 256, 0, st>>>(D, c.pos, c.mass);
@@ -1163,7 +1183,7 @@ int reassign_run(hbtg_handle *H, const hbtg_params *p, const hbtg_reassign *r, i
   D.fb_count = P.get<int>(S_FBC, 1);
   D.cnt = P.get<int>(S_CNT, t1 + 1);
   D.X = P.get<int>(S_X, t1 + 1);
-  D.interactions = P.get<unsigned long long>(S_COUNTER, 1);
+  D.interactions = P.get<unsigned long long>(S_COUNTER, kWalkCounters);
   if (T > 0)
   {
     k_re_pack<<<blocks_for(N, 256), 256, 0, st>>>(Q, D, N);
@@ -1319,7 +1339,8 @@ int hbtg_create(hbtg_handle **handle, int device)
       delete h;
       return HBTG_ERR_CUDA;
     }
-  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->side2, cudaStreamNonBlocking) != cudaSuccess)
   {
     delete h;
     return HBTG_ERR_CUDA;
@@ -1349,6 +1370,8 @@ int hbtg_destroy(hbtg_handle *h)
       cudaEventDestroy(e);
   if (h->side)
     cudaStreamDestroy(h->side);
+  if (h->side2)
+    cudaStreamDestroy(h->side2);
   if (h->stream)
     cudaStreamDestroy(h->stream);
   delete h;

@@ -16,9 +16,14 @@
 //               interaction list with the mask of the targets that accept it;
 //               the rest of the range and, if some targets open the node, its
 //               children (with the mask of those targets) go back on the stack.
-//   evaluation  Entries go to one of two lists: "far" entries, which every
-//               target sees beyond the softening length (box distance), and
-//               "near" ones.  Whenever a list fills, every lane reads each
+//               Nodes of the third kind wait in a pending list; once it holds
+//               32 (or the stack is empty) each lane takes one and runs every
+//               target's own test on it, two targets per packed FP32x2
+//               operation, which gives its entry mask and its children's.
+//   evaluation  Entries go to one of three lists: "far" entries, which every
+//               target sees beyond the softening length (box distance), split
+//               into those that every target takes (no selection at all) and
+//               the rest, and "near" ones.  Whenever a list fills, every lane reads each
 //               entry (a shared-memory broadcast) and adds the term of the
 //               entries its mask bit selects: -m / r for the far list with no
 //               branch, two entries at a time in packed FP32x2 arithmetic
@@ -40,12 +45,15 @@
 // disagree with a target's own test.
 //
 // Bounds.  Stack pushes happen only in steps that start with at most
-// kWalkStack - 64 ranges (a step pops k <= 32 ranges and pushes at most 2k);
-// above that the warp drains the stack one range at a time, each target
-// walking that range on its own with the reference's stackless walk (no
-// pushes).  A list holding more than its capacity - 40 entries after a step
-// (at most 32 added per step) is evaluated, so with its padding (at most 7)
-// it never exceeds its capacity.  Every loop advances a slot index strictly.
+// kWalkDrain = kWalkStack - 64 ranges (a step pops k <= 32 ranges and pushes
+// at most 2k, or resolves pending nodes and pushes at most 32); above that
+// the warp drains the stack one range at a time, each target walking that
+// range on its own with the reference's stackless walk (no pushes).  A list
+// holding more than its capacity - 40 entries after a step (at most 32 added
+// per step) is evaluated, so with its padding (at most 7) it never exceeds
+// its capacity.  Pending nodes are added only by steps that start with fewer
+// than 32 (at most 32 added), so at most 63 wait.  Every loop advances a slot
+// index strictly or shrinks the pending list.
 // A node's second slot is read for leaves too: the tree array carries one
 // padding slot after its last slot.
 #pragma once
@@ -58,11 +66,33 @@ namespace
 {
 
 constexpr int kWalkWarps = 4;   // warps per block
-constexpr int kWalkFar = 160;   // far-list entries per warp
+constexpr int kWalkFull = 96;   // far-list entries that every target takes, per warp
+constexpr int kWalkFar = 64;    // other far-list entries per warp
 constexpr int kWalkNear = 64;   // near-list entries per warp
 constexpr int kWalkStack = 256; // traversal ranges per warp
+constexpr int kWalkDrain = kWalkStack - 64; // a deeper stack is drained (a step pushes at most 2 per lane)
+constexpr int kWalkPending = 64; // cells waiting for the targets' own opening tests
+constexpr int kWalkWarp2 = 16;  // target pairs per warp
 constexpr int kFlushMargin = 40; // a list is evaluated once it holds more than capacity - this
 constexpr float kBandLo = 1.f - 1e-6f, kBandHi = 1.f + 1e-6f;
+
+// Per-lane walk counters (counted calls): see kWalkCounters.
+struct WalkCount
+{
+  unsigned long long v[kWalkCounters];
+};
+
+// Lane 0 adds the clock cycles since t to counter q (counted calls only).
+template <bool Count>
+__device__ __forceinline__ void tick(WalkCount &cnt, int q, long long &t, int lane)
+{
+  if (!Count)
+    return;
+  const long long now = clock64();
+  if (lane == 0)
+    cnt.v[q] += (unsigned long long)(now - t);
+  t = now;
+}
 
 struct WalkShared
 {
@@ -71,11 +101,19 @@ struct WalkShared
   float4 fa[kWalkWarps][kWalkFar / 2];
   float4 fb[kWalkWarps][kWalkFar / 2];
   uint2 fm[kWalkWarps][kWalkFar / 2];
+  // far list of entries that every target takes: ga = (x0, x1, y0, y1),
+  // gb = (z0, z1, -m0, -m1)
+  float4 ga[kWalkWarps][kWalkFull / 2];
+  float4 gb[kWalkWarps][kWalkFull / 2];
   float4 near[kWalkWarps][kWalkNear];
   unsigned nmsk[kWalkWarps][kWalkNear];
   int ia[kWalkWarps][kWalkStack];       // range: first slot
   int ie[kWalkWarps][kWalkStack];       //        end slot
   unsigned im[kWalkWarps][kWalkStack];  //        targets still walking it
+  int pa[kWalkWarps][kWalkPending];     // pending cell: slot
+  unsigned pm[kWalkWarps][kWalkPending]; //              targets that reach it
+  float4 txy[kWalkWarps][kWalkWarp2];   // targets, negated, in pairs: (x0, x1, y0, y1)
+  float2 tz[kWalkWarps][kWalkWarp2];    //                             (z0, z1)
 };
 
 // a - b, with the periodic wrap of NEAREST (src/config_parser.h:218-219)
@@ -121,6 +159,77 @@ __device__ __forceinline__ bool target_opens(float cx, float cy, float cz, float
   if (r2 > __fmul_rn(crit, kBandHi))
     return false;
   return opens_exact<Wrap>(cx, cy, cz, lenf, tx, ty, tz, K);
+}
+
+// Target t of the warp from the negated pairs.
+__device__ __forceinline__ void target_at(const float4 *txy, const float2 *tz, int t, float &x, float &y, float &z)
+{
+  const float4 P = txy[t >> 1];
+  const float2 Z = tz[t >> 1];
+  const bool h = (t & 1) != 0;
+  x = -(h ? P.y : P.x);
+  y = -(h ? P.w : P.z);
+  z = -(h ? Z.y : Z.x);
+}
+
+// Every target's own decision on one cell (centre c, threshold crit, side
+// lenf): bit t set when target t (of the mask m) opens it.  Without the wrap,
+// two targets per packed operation; each half is the FP32 operation of
+// target_opens (c + (-t) is c - t exactly), so the decisions are the same.
+template <bool Wrap>
+__device__ __forceinline__ unsigned opens_mask(const float4 *txy, const float2 *tz, float cx, float cy, float cz,
+                                               float crit, float lenf, unsigned m, const KParams &K)
+{
+  unsigned O = 0u;
+  if (Wrap)
+  {
+    for (unsigned r = m; r; r &= r - 1u)
+    {
+      const int t = __ffs(r) - 1;
+      float tx, ty, tzz;
+      target_at(txy, tz, t, tx, ty, tzz);
+      if (target_opens<true>(cx, cy, cz, crit, lenf, tx, ty, tzz, K))
+        O |= 1u << t;
+    }
+    return O;
+  }
+  const float lo = __fmul_rn(crit, kBandLo), hi = __fmul_rn(crit, kBandHi);
+  const float2 c_x = make_float2(cx, cx), c_y = make_float2(cy, cy), c_z = make_float2(cz, cz);
+  unsigned B = 0u; // not beyond the band's far edge
+#pragma unroll
+  for (int q = 0; q < kWalkWarp2; q++)
+  {
+    const float4 P = txy[q];
+    const float2 Z = tz[q];
+    const float2 dx = __fadd2_rn(c_x, make_float2(P.x, P.y));
+    const float2 dy = __fadd2_rn(c_y, make_float2(P.z, P.w));
+    const float2 dz = __fadd2_rn(c_z, Z);
+    float2 r2 = __fmul2_rn(dx, dx);
+    r2 = __ffma2_rn(dy, dy, r2);
+    r2 = __ffma2_rn(dz, dz, r2);
+    O |= (r2.x < lo ? 1u : 0u) << (2 * q) | (r2.y < lo ? 2u : 0u) << (2 * q);
+    B |= (r2.x > hi ? 0u : 1u) << (2 * q) | (r2.y > hi ? 0u : 2u) << (2 * q);
+  }
+  O &= m;
+  // inside the band: the reference's double arithmetic
+  for (unsigned r = B & m & ~O; r; r &= r - 1u)
+  {
+    const int t = __ffs(r) - 1;
+    float tx, ty, tzz;
+    target_at(txy, tz, t, tx, ty, tzz);
+    if (opens_exact<false>(cx, cy, cz, lenf, tx, ty, tzz, K))
+      O |= 1u << t;
+  }
+  return O;
+}
+
+// Squared distance from a point to the targets' bounding box.
+__device__ __forceinline__ float box_gap2(const float *lo, const float *hi, float x, float y, float z)
+{
+  const float g[3] = {fmaxf(fmaxf(__fsub_rn(lo[0], x), __fsub_rn(x, hi[0])), 0.f),
+                      fmaxf(fmaxf(__fsub_rn(lo[1], y), __fsub_rn(y, hi[1])), 0.f),
+                      fmaxf(fmaxf(__fsub_rn(lo[2], z), __fsub_rn(z, hi[2])), 0.f)};
+  return dist2(g[0], g[1], g[2]);
 }
 
 // The potential term of one entry for one target at squared distance r2.
@@ -206,11 +315,58 @@ __device__ __forceinline__ void eval_far(const float4 *fa, const float4 *fb, con
   }
 }
 
+// Writes entry k of the far list that every target takes.
+__device__ __forceinline__ void full_put(float4 *ga, float4 *gb, int k, float x, float y, float z, float m)
+{
+  float *A = reinterpret_cast<float *>(ga + (k >> 1)), *B = reinterpret_cast<float *>(gb + (k >> 1));
+  const int h = k & 1;
+  A[h] = x;
+  A[2 + h] = y;
+  B[h] = z;
+  B[2 + h] = -m;
+}
+
+__device__ __forceinline__ int pad8_full(float4 *ga, float4 *gb, int n, int lane)
+{
+  const int padded = (n + 7) & ~7;
+  if (n + lane < padded)
+    full_put(ga, gb, n + lane, kFarAway, kFarAway, kFarAway, 0.f);
+  __syncwarp();
+  return padded;
+}
+
+// The far list that every target takes: no per-entry selection.
+__device__ __forceinline__ void eval_full(const float4 *ga, const float4 *gb, int n, float tx, float ty, float tz,
+                                          float &sum, float &comp)
+{
+  const float2 ntx = make_float2(-tx, -tx), nty = make_float2(-ty, -ty), ntz = make_float2(-tz, -tz);
+  for (int i = 0; i < n; i += 8)
+  {
+    float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+    {
+      const int pp = (i >> 1) + q;
+      const float4 A = ga[pp], B = gb[pp];
+      const float2 dx = __fadd2_rn(make_float2(A.x, A.y), ntx);
+      const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nty);
+      const float2 dz = __fadd2_rn(make_float2(B.x, B.y), ntz);
+      float2 r2 = __fmul2_rn(dx, dx);
+      r2 = __ffma2_rn(dy, dy, r2);
+      r2 = __ffma2_rn(dz, dz, r2);
+      const float2 rs = make_float2(rsqrtf(r2.x), rsqrtf(r2.y));
+      acc = __ffma2_rn(make_float2(B.z, B.w), rs, acc);
+    }
+    kahan_add(sum, comp, acc.x + acc.y);
+  }
+}
+
 // Near list: the softened kernel where r < h (src/gravity_tree.cpp:150-162).
 template <bool Wrap>
 __device__ __forceinline__ void eval_near(const float4 *ent, const unsigned *msk, int n, unsigned lanebit, float tx,
                                           float ty, float tz, const KParams &K, float h2, float &sum, float &comp)
 {
+  const unsigned full = 0xffffffffu;
   for (int i = 0; i < n; i += 8)
   {
     float part = 0.f;
@@ -220,7 +376,14 @@ __device__ __forceinline__ void eval_near(const float4 *ent, const unsigned *msk
       const float4 e = ent[i + u];
       const float m = (msk[i + u] & lanebit) ? e.w : 0.f;
       const float r2 = dist2(sep<Wrap>(e.x, tx, K), sep<Wrap>(e.y, ty, K), sep<Wrap>(e.z, tz, K));
-      part += softened_term(m, r2, K, h2);
+      // the softened form only when some lane is inside the softening length
+      // (its square root and polynomial are skipped otherwise)
+      float t;
+      if (__any_sync(full, r2 < h2))
+        t = softened_term(m, r2, K, h2);
+      else
+        t = -m * rsqrtf(r2);
+      part += t;
     }
     kahan_add(sum, comp, part);
   }
@@ -230,8 +393,7 @@ __device__ __forceinline__ void eval_near(const float4 *ent, const unsigned *msk
 // one target (open: next slot; accept: interact and skip the subtree).
 template <bool Wrap>
 __device__ __forceinline__ void walk_range(const float4 *__restrict__ T, int a, int e, float tx, float ty, float tz,
-                                           const KParams &K, float h2, float &sum, float &comp,
-                                           unsigned long long &cnt)
+                                           const KParams &K, float h2, float &sum, float &comp, WalkCount &cnt)
 {
   int idx = a;
   while (idx < e)
@@ -258,7 +420,7 @@ __device__ __forceinline__ void walk_range(const float4 *__restrict__ T, int a, 
     }
     const float r2 = dist2(sep<Wrap>(n.x, tx, K), sep<Wrap>(n.y, ty, K), sep<Wrap>(n.z, tz, K));
     kahan_add(sum, comp, softened_term(m, r2, K, h2));
-    cnt++;
+    cnt.v[0]++;
     idx = max(next, idx + 1);
   }
 }
@@ -266,17 +428,17 @@ __device__ __forceinline__ void walk_range(const float4 *__restrict__ T, int a, 
 // Potentials of the (up to) 32 targets of chunk c.
 template <bool Wrap, bool Count>
 __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, int s, int root, int lane, bool valid,
-                                           int p, float4 x, float self, WalkShared &sh, int w,
-                                           unsigned long long &cnt)
+                                           int p, float4 x, float self, WalkShared &sh, int w, WalkCount &cnt)
 {
   const float4 *__restrict__ T = D.nodes;
-  float4 *fa = sh.fa[w], *fb = sh.fb[w], *nea = sh.near[w];
+  float4 *fa = sh.fa[w], *fb = sh.fb[w], *nea = sh.near[w], *ga = sh.ga[w], *gb = sh.gb[w];
   uint2 *fm = sh.fm[w];
   unsigned *nmsk = sh.nmsk[w];
   int *ia = sh.ia[w], *ie = sh.ie[w];
   unsigned *im = sh.im[w];
   const unsigned full = 0xffffffffu, lanebit = 1u << lane, below = lanebit - 1u;
   const float h2 = K.h * K.h;
+  long long t_all = Count ? clock64() : 0, t = t_all;
   const unsigned vmask = __ballot_sync(full, valid);
   // bounding box of the targets
   float lo[3] = {valid ? x.x : INFINITY, valid ? x.y : INFINITY, valid ? x.z : INFINITY};
@@ -290,18 +452,28 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
       hi[d] = fmaxf(hi[d], __shfl_xor_sync(full, hi[d], o));
     }
   float sum = valid ? self / K.soft : 0.f, comp = 0.f;
-  const int root_end = __float_as_int(__ldg(&T[root + 1]).y);
   if (lane == 0)
   {
     ia[0] = root;
-    ie[0] = root_end;
+    ie[0] = __float_as_int(__ldg(&T[root + 1]).y);
     im[0] = vmask;
   }
-  int sp = 1, nf = 0, nn = 0;
-  __syncwarp();
-  while (sp > 0)
+  // the targets, negated, in pairs (the pending cells' tests read them)
   {
-    if (sp > kWalkStack - 64)
+    float *X = reinterpret_cast<float *>(sh.txy[w]), *Z = reinterpret_cast<float *>(sh.tz[w]);
+    const int q = lane >> 1, hh = lane & 1;
+    X[4 * q + hh] = valid ? -x.x : 0.f;
+    X[4 * q + 2 + hh] = valid ? -x.y : 0.f;
+    Z[2 * q + hh] = valid ? -x.z : 0.f;
+  }
+  int *pa = sh.pa[w];
+  unsigned *pmk = sh.pm[w];
+  int sp = 1, np = 0, nf = 0, ng = 0, nn = 0;
+  __syncwarp();
+  tick<Count>(cnt, 8, t, lane);
+  while (sp > 0 || np > 0)
+  {
+    if (sp > kWalkDrain)
     { // drain: each target walks the top range on its own
       sp--;
       const int a = ia[sp], e = ie[sp];
@@ -309,76 +481,102 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
       __syncwarp();
       if (m & lanebit)
         walk_range<Wrap>(T, a, e, x.x, x.y, x.z, K, h2, sum, comp, cnt);
+      if (Count && lane == 0)
+        cnt.v[7]++;
+      tick<Count>(cnt, 14, t, lane);
       continue;
     }
-    const int k = min(sp, 32);
-    const int base = sp - k;
-    const bool act = lane < k;
+    bool act, cell = false, near = true;
     int a = 0, e = 0;
-    unsigned m = 0u;
-    if (act)
-    {
-      a = ia[base + lane];
-      e = ie[base + lane];
-      m = im[base + lane];
-    }
-    sp = base;
-    __syncwarp();
+    unsigned m = 0u, A = 0u, O = 0u;
     float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool cell = false, near = true;
-    int cls = 0; // 0: every target accepts, 1: every target opens, 2: each target decides
-    if (act)
-    {
-      na = __ldg(&T[a]);
-      nb = __ldg(&T[a + 1]); // a cell's mass, skip and side length (the tree has a padding slot)
-      cell = slot_is_cell(na.w);
-      if (Wrap)
-        cls = cell ? 2 : 0;
-      else
+    if (np >= kWarp || sp == 0)
+    { // resolve up to 32 pending cells, one per lane, each against every target
+      const int k = min(np, kWarp);
+      act = lane < k;
+      if (Count && lane == 0)
+        cnt.v[3]++;
+      if (act)
       {
-        const float g[3] = {fmaxf(fmaxf(__fsub_rn(lo[0], na.x), __fsub_rn(na.x, hi[0])), 0.f),
-                            fmaxf(fmaxf(__fsub_rn(lo[1], na.y), __fsub_rn(na.y, hi[1])), 0.f),
-                            fmaxf(fmaxf(__fsub_rn(lo[2], na.z), __fsub_rn(na.z, hi[2])), 0.f)};
-        const float rmin2 = dist2(g[0], g[1], g[2]);
-        near = rmin2 < h2;
-        if (cell)
+        a = pa[np - k + lane];
+        m = pmk[np - k + lane];
+      }
+      np -= k;
+      __syncwarp();
+      if (act)
+      {
+        na = __ldg(&T[a]);
+        nb = __ldg(&T[a + 1]);
+        cell = true;
+        e = __float_as_int(nb.y); // the cell's siblings are on the stack already
+        if (!Wrap)
+          near = box_gap2(lo, hi, na.x, na.y, na.z) < h2;
+        O = opens_mask<Wrap>(sh.txy[w], sh.tz[w], na.x, na.y, na.z,
+                             __uint_as_float(__float_as_uint(na.w) & 0x7fffffffu), nb.z, m, K);
+        A = m & ~O;
+      }
+      tick<Count>(cnt, 9, t, lane);
+    }
+    else
+    { // the first nodes of up to 32 ranges, one per lane
+      const int k = min(sp, kWarp);
+      const int base = sp - k;
+      act = lane < k;
+      if (Count && lane == 0)
+      {
+        cnt.v[1]++;
+        cnt.v[2] += k;
+      }
+      if (act)
+      {
+        a = ia[base + lane];
+        e = ie[base + lane];
+        m = im[base + lane];
+      }
+      sp = base;
+      __syncwarp();
+      int cls = 0; // 0: every target accepts, 1: every target opens, 2: each target decides
+      if (act)
+      {
+        na = __ldg(&T[a]);
+        nb = __ldg(&T[a + 1]); // a cell's mass, skip and side length (the tree has a padding slot)
+        cell = slot_is_cell(na.w);
+        if (Wrap)
+          cls = cell ? 2 : 0;
+        else
         {
-          const float crit = __uint_as_float(__float_as_uint(na.w) & 0x7fffffffu);
-          if (!(rmin2 > __fmul_rn(crit, kBandHi)))
+          const float rmin2 = box_gap2(lo, hi, na.x, na.y, na.z);
+          near = rmin2 < h2;
+          if (cell)
           {
-            const float G[3] = {fmaxf(fabsf(__fsub_rn(na.x, lo[0])), fabsf(__fsub_rn(na.x, hi[0]))),
-                                fmaxf(fabsf(__fsub_rn(na.y, lo[1])), fabsf(__fsub_rn(na.y, hi[1]))),
-                                fmaxf(fabsf(__fsub_rn(na.z, lo[2])), fabsf(__fsub_rn(na.z, hi[2])))};
-            cls = dist2(G[0], G[1], G[2]) < __fmul_rn(crit, kBandLo) ? 1 : 2;
+            const float crit = __uint_as_float(__float_as_uint(na.w) & 0x7fffffffu);
+            if (!(rmin2 > __fmul_rn(crit, kBandHi)))
+            {
+              const float G[3] = {fmaxf(fabsf(__fsub_rn(na.x, lo[0])), fabsf(__fsub_rn(na.x, hi[0]))),
+                                  fmaxf(fabsf(__fsub_rn(na.y, lo[1])), fabsf(__fsub_rn(na.y, hi[1]))),
+                                  fmaxf(fabsf(__fsub_rn(na.z, lo[2])), fabsf(__fsub_rn(na.z, hi[2])))};
+              cls = dist2(G[0], G[1], G[2]) < __fmul_rn(crit, kBandLo) ? 1 : 2;
+            }
           }
         }
       }
-    }
-    unsigned A = cls == 0 ? m : 0u, O = cls == 1 ? m : 0u;
-    // the targets decide the nodes near their opening distance, one node at a time
-    unsigned mix = __ballot_sync(full, act && cls == 2);
-    while (mix)
-    {
-      const int j = __ffs(mix) - 1;
-      mix &= mix - 1u;
-      const float cx = __shfl_sync(full, na.x, j), cy = __shfl_sync(full, na.y, j), cz = __shfl_sync(full, na.z, j);
-      const float cw = __shfl_sync(full, na.w, j), cl = __shfl_sync(full, nb.z, j);
-      const unsigned mj = __shfl_sync(full, m, j);
-      bool op = false;
-      if (mj & lanebit)
-        op = target_opens<Wrap>(cx, cy, cz, __uint_as_float(__float_as_uint(cw) & 0x7fffffffu), cl, x.x, x.y, x.z, K);
-      const unsigned oj = __ballot_sync(full, op);
-      if (lane == j)
+      A = cls == 0 ? m : 0u;
+      O = cls == 1 ? m : 0u;
+      // cells near the targets' opening distance wait for a batch of their own
+      const unsigned bp = __ballot_sync(full, act && cls == 2);
+      if (act && cls == 2)
       {
-        O = oj;
-        A = mj & ~oj;
+        const int at = np + __popc(bp & below);
+        pa[at] = a;
+        pmk[at] = m;
       }
+      np += __popc(bp);
+      tick<Count>(cnt, 8, t, lane);
     }
-    const int next = cell ? __float_as_int(nb.y) : a + 1;
-    const bool has_e = act && A != 0u, has_sib = act && next < e, has_kid = act && O != 0u;
-    const bool to_near = Wrap || near;
-    const unsigned bf = __ballot_sync(full, has_e && !to_near), bn = __ballot_sync(full, has_e && to_near),
-                   bs = __ballot_sync(full, has_sib), bk = __ballot_sync(full, has_kid);
+    const bool has_e = act && A != 0u;
+    const bool to_near = Wrap || near, every = A == vmask;
+    const unsigned bg = __ballot_sync(full, has_e && !to_near && every),
+                   bf = __ballot_sync(full, has_e && !to_near && !every), bn = __ballot_sync(full, has_e && to_near);
     if (has_e)
     {
       const float4 en = make_float4(na.x, na.y, na.z, cell ? nb.x : na.w);
@@ -388,14 +586,26 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
         nea[at] = en;
         nmsk[at] = A;
       }
+      else if (every)
+        full_put(ga, gb, ng + __popc(bg & below), en.x, en.y, en.z, en.w);
       else
         far_put(fa, fb, fm, nf + __popc(bf & below), en.x, en.y, en.z, en.w, A);
       if (Count)
-        cnt += __popc(A);
+        cnt.v[0] += __popc(A);
     }
+    if (Count && lane == 0)
+    {
+      cnt.v[4] += __popc(bg);
+      cnt.v[5] += __popc(bf);
+      cnt.v[6] += __popc(bn);
+    }
+    ng += __popc(bg);
     nf += __popc(bf);
     nn += __popc(bn);
     // the rest of each range, then the children of opened cells (popped first: depth first)
+    const int next = cell ? __float_as_int(nb.y) : a + 1;
+    const bool has_sib = act && next < e, has_kid = act && O != 0u;
+    const unsigned bs = __ballot_sync(full, has_sib), bk = __ballot_sync(full, has_kid);
     if (has_sib)
     {
       const int at = sp + __popc(bs & below);
@@ -413,22 +623,38 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
     }
     sp += __popc(bk);
     __syncwarp();
+    tick<Count>(cnt, 10, t, lane);
+    if (ng > kWalkFull - kFlushMargin)
+    {
+      eval_full(ga, gb, pad8_full(ga, gb, ng, lane), x.x, x.y, x.z, sum, comp);
+      ng = 0;
+      __syncwarp();
+      tick<Count>(cnt, 11, t, lane);
+    }
     if (nf > kWalkFar - kFlushMargin)
     {
       eval_far(fa, fb, fm, pad8_far(fa, fb, fm, nf, lane), lanebit, x.x, x.y, x.z, sum, comp);
       nf = 0;
       __syncwarp();
+      tick<Count>(cnt, 12, t, lane);
     }
     if (nn > kWalkNear - kFlushMargin)
     {
       eval_near<Wrap>(nea, nmsk, pad8(nea, nmsk, nn, lane), lanebit, x.x, x.y, x.z, K, h2, sum, comp);
       nn = 0;
       __syncwarp();
+      tick<Count>(cnt, 13, t, lane);
     }
   }
+  eval_full(ga, gb, pad8_full(ga, gb, ng, lane), x.x, x.y, x.z, sum, comp);
+  tick<Count>(cnt, 11, t, lane);
   eval_far(fa, fb, fm, pad8_far(fa, fb, fm, nf, lane), lanebit, x.x, x.y, x.z, sum, comp);
+  tick<Count>(cnt, 12, t, lane);
   eval_near<Wrap>(nea, nmsk, pad8(nea, nmsk, nn, lane), lanebit, x.x, x.y, x.z, K, h2, sum, comp);
   __syncwarp();
+  tick<Count>(cnt, 13, t, lane);
+  t = t_all;
+  tick<Count>(cnt, 15, t, lane);
   if (valid)
     D.pot[p] = (sum - comp) * K.G_over_a;
 }
@@ -438,7 +664,7 @@ __device__ __forceinline__ void walk_group(const DevState &D, const KParams &K, 
 // its own leaf, src/gravity_tree.cpp:98-101).
 template <bool Count>
 __device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, int c, int lane, WalkShared &sh,
-                                           int w, unsigned long long &cnt)
+                                           int w, WalkCount &cnt)
 {
   const int s = find_segment_warp(D.chunk_off, D.S, c); // c is the same on every lane
   const int t = (c - D.chunk_off[s]) * kWarp + lane;
@@ -475,7 +701,7 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_walk(DevState D, KParams K,
 {
   __shared__ WalkShared sh;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  unsigned long long cnt = 0;
+  WalkCount cnt = {};
   if (D.walk_ctr)
   {
     unsigned smid;
@@ -506,12 +732,14 @@ __global__ void __launch_bounds__(32 * kWalkWarps) k_walk(DevState D, KParams K,
       walk_chunk<Count>(D, K, c, lane, sh, w, cnt);
   }
   if (Count)
-  {
-    for (int o = 16; o > 0; o >>= 1)
-      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-    if (lane == 0)
-      atomicAdd(D.interactions, cnt);
-  }
+    for (int q = 0; q < kWalkCounters; q++)
+    {
+      unsigned long long v = cnt.v[q];
+      for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0)
+        atomicAdd(D.interactions + q, v);
+    }
 }
 
 } // namespace

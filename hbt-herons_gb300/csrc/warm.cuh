@@ -830,6 +830,7 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     std::vector<int> nex(S);
     R.mem.check(cudaMemcpyAsync(nex.data(), D.nexcl, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
     R.mem.check(cudaStreamSynchronize(st));
+    R.host_syncs++;
     for (int v : nex)
       C.excluded += v;
   }

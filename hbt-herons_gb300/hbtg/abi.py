@@ -53,7 +53,7 @@ class Params(C.Structure):
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: (list(v) if hasattr(v, "__len__") else v) for k, v in ((k, getattr(self, k)) for k, _ in self._fields_)}
 
 
 def default_params(**overrides) -> Params:
@@ -126,10 +126,13 @@ class CStats(C.Structure):
         ("ms_propose", C.c_double), ("warm_subhaloes", C.c_int64), ("excluded", C.c_int64),
         ("readmitted", C.c_int64), ("cold_restarts", C.c_int64), ("readmit_rounds", C.c_int64),
         ("walk_blocks_per_sm", C.c_int64), ("ms_h2d", C.c_double), ("ms_d2h", C.c_double),
+        ("walk_steps", C.c_int64), ("walk_nodes", C.c_int64), ("walk_pending_batches", C.c_int64),
+        ("walk_entries_full", C.c_int64), ("walk_entries_part", C.c_int64), ("walk_entries_near", C.c_int64),
+        ("walk_drained", C.c_int64), ("walk_cycles", C.c_int64 * 8), ("host_syncs", C.c_int64),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: (list(v) if hasattr(v, "__len__") else v) for k, v in ((k, getattr(self, k)) for k, _ in self._fields_)}
 
 
 class CProps(C.Structure):

@@ -154,6 +154,18 @@ typedef struct hbtg_stats
   int64_t walk_blocks_per_sm; /* resident tree-walk blocks per SM of the last call's launches */
   double ms_h2d;              /* host-pointer calls: uploads on the call's stream before the first kernel */
   double ms_d2h;              /* host-pointer calls: downloads after the last kernel */
+  /* tree-walk traversal counters (counted calls only, like interactions) */
+  int64_t walk_steps;           /* warp traversal steps */
+  int64_t walk_nodes;           /* nodes popped from the warps' range stacks */
+  int64_t walk_pending_batches; /* batches of cells resolved by every target's own test */
+  int64_t walk_entries_full;    /* far entries that every target of the warp takes */
+  int64_t walk_entries_part;    /* far entries for part of the targets */
+  int64_t walk_entries_near;    /* entries within a softening length of some target */
+  int64_t walk_drained;         /* ranges walked target by target (deep stacks) */
+  int64_t walk_cycles[8];       /* warp clock cycles: pop and classify, resolve pending cells, list and
+                                   stack writes, evaluate the full / masked far / near lists, drain,
+                                   whole target groups */
+  int64_t host_syncs;           /* stream synchronisations for host reads of device totals */
 } hbtg_stats;
 
 typedef struct hbtg_handle hbtg_handle;
