@@ -353,8 +353,10 @@ def bench_gpu(args):
                  pin(inp.ref_pos), pin(inp.ref_vel), pin(inp.mostbound_pos), pin(inp.mostbound_vel),
                  pin(inp.most_bound_id), {}, pin(inp.prior_nbound), pin(inp.prior_energy))
     buf = CallBuffers(hin, want_energy=True)
+    # every host array the call reads or writes is pinned (the in/out frames
+    # too: a pageable copy makes the driver stage it and can stall the stream)
     for name in ("order", "energy", "nbound", "mbound", "tracer_index", "iterations", "status", "kinematics", "core",
-                 "nbound_type", "mbound_type"):
+                 "nbound_type", "mbound_type", "ref_pos", "ref_vel", "mostbound_pos", "mostbound_vel", "most_bound_id"):
         setattr(buf.out, name, pin(getattr(buf.out, name)))
     buf = _rebind(buf)
     prior = CPrior(_ptr(hin.prior_nbound), _ptr(hin.prior_energy))
@@ -413,6 +415,15 @@ def bench_gpu(args):
         literal = {"n_sub": int(lit_inp.n_sub), "particles": int(lit_inp.n_particles), "learned": lit["learned"],
                    "plain": lit["plain"], "learned_vs_plain": lit["learned"] / lit["plain"]}
         del lit_db
+
+    # the other two workloads of the method at their own sizes (hydro mixed
+    # species with thermal energy; held-out stripped subhaloes with a
+    # previous-output prior), both arms, with parity against the CPU oracle
+    # on a sample of each
+    side = {}
+    if args.workload == "batched" and not args.skip_side and rank == 0:
+        for kind in ("hydro", "stripped"):
+            side[kind] = side_workload(kind, u, args, local, stream)
 
     # roofline of the dominant kernel (the tree walk) in the learned arm
     peak = measure_fp32_peak(local)
@@ -491,6 +502,8 @@ def bench_gpu(args):
             "cpu_baseline": cpu,
             "parity": parity,
             "literal_20000": literal,
+            "hydro": side.get("hydro"),
+            "stripped": side.get("stripped"),
             "clocks": warm["clocks"],
             "clocks_plain": plain and plain["clocks"],
         }
@@ -500,6 +513,60 @@ def bench_gpu(args):
         dist.destroy_process_group()
     u.close()
     return 0
+
+
+def side_workload(kind, u, args, local, stream):
+    """Both GPU arms on one more workload at its own size (device-resident
+    inputs, CUDA events over `args.steps` steps after 3 warm-up steps), the
+    learned arm's bound-mass and membership error against the plain arm, and
+    the plain arm's parity against the CPU oracle on a particle-weighted
+    sample of about 2e5 particles."""
+    import torch
+    from hbtg.gpu import DeviceBatch
+    total = {"stripped": 20000, "hydro": 4e6}[kind]
+    inp, prm = workload(total, args.seed, kind)
+    use_prior = inp.prior_nbound is not None
+    db = DeviceBatch(inp, device="cuda:%d" % local)
+    res = {"workload": WORKLOADS[kind] % total, "particles": int(inp.n_particles), "subhaloes": int(inp.n_sub)}
+    outs = {}
+    for arm in ("plain", "learned"):
+        def step(arm=arm):
+            db.reset_inout()
+            if arm == "plain":
+                u.unbind_device(prm, db.c, stream.cuda_stream)
+            else:
+                u.unbind_learned_device(prm, db, stream.cuda_stream, use_prior=use_prior)
+        for _ in range(3):
+            step()
+        bound = 0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            bound += u.stats()["total_bound"]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        res[arm] = {"value": bound / args.steps / (ms * 1e-3), "ms_per_step": ms,
+                    "global_iterations": u.stats()["global_iterations"]}
+        outs[arm] = db.outputs()
+    res["learned_vs_plain"] = res["learned"]["value"] / res["plain"]["value"]
+    m_plain = float(np.sum(outs["plain"].mbound.astype(np.float64)))
+    m_warm = float(np.sum(outs["learned"].mbound.astype(np.float64)))
+    res["dM_bound"] = abs(m_warm - m_plain) / max(m_plain, 1e-30)
+    res["membership_vs_plain"] = _membership(inp, outs["learned"], outs["plain"])
+    del db
+    if not args.skip_cpu:
+        sample, picked = cpu_sample(inp, 200_000, seed=args.seed + 2)
+        out, dt, kind_cpu = run_cpu(sample, prm, os.cpu_count() or 1, want_potential=True)
+        g = u.unbind(sample, prm, want_potential=True)
+        res["parity"] = sample_parity(sample, g, out, prm)
+        res["parity"]["against"] = "plain GPU path vs CPU %s on the sampled subhaloes" % kind_cpu
+        res["cpu"] = {"value": float(out.nbound.sum() / dt), "cores": os.cpu_count() or 1, "kind": kind_cpu,
+                      "sample": _sample_text(inp, sample, picked)}
+    return res
 
 
 def _membership(inp, got, ref):
@@ -524,6 +591,8 @@ def _rebind(buf):
     c.tracer_index, c.iterations, c.status = _ptr(o.tracer_index), _ptr(o.iterations), _ptr(o.status)
     c.kinematics, c.core, c.nbound_type, c.mbound_type = _ptr(o.kinematics), _ptr(o.core), _ptr(o.nbound_type), \
         _ptr(o.mbound_type)
+    c.ref_pos, c.ref_vel, c.mostbound_pos = _ptr(o.ref_pos), _ptr(o.ref_vel), _ptr(o.mostbound_pos)
+    c.mostbound_vel, c.most_bound_id = _ptr(o.mostbound_vel), _ptr(o.most_bound_id)
     return buf
 
 
@@ -579,6 +648,7 @@ def main():
     ap.add_argument("--ref-sample", type=float, default=4e5, help="particles per reference-arm step")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-literal", action="store_true", help="skip the literal 20,000-subhalo timing")
+    ap.add_argument("--skip-side", action="store_true", help="skip the hydro and stripped side workloads")
     args = ap.parse_args()
     if args.total is None:
         args.total = {"stripped": 20000, "hydro": 4e6}.get(args.workload, 5e7)

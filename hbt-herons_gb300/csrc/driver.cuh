@@ -184,17 +184,29 @@ struct IterationDriver
     k_tree_count<<<grid_for(src_total + 1, 256), 256, 0, st>>>(D, src_total);
     launches++;
     check();
-    const int internal = scan_counts(D.cnt, D.X, src_total);
+    // the cell total and the cells per level (k_tree_count's histogram) in one host read
+    scan<int, false>(D.cnt, D.X, src_total + 1, mem.scan_scratch(src_total + 1), st, &launches);
+    check();
+    int counts[1 + kLevels];
+    mem.check(cudaMemcpyAsync(&counts[0], D.X + src_total, sizeof(int), cudaMemcpyDeviceToHost, st));
+    mem.check(cudaMemcpyAsync(&counts[1], D.lvl, sizeof(int) * kLevels, cudaMemcpyDeviceToHost, st));
+    mem.check(cudaStreamSynchronize(st));
+    host_syncs++;
+    const int internal = counts[0];
+    const int *per_level = counts + 1;
     // one padding slot after the last: the walk reads a node's second slot unconditionally
     D.nodes = mem.tree_slots((long long)src_total + 2LL * internal + 1);
     D.cell_list = mem.cell_list(internal);
     tree_nodes += internal;
     k_tree_emit<<<grid_for(src_total, 128), 128, 0, st>>>(D, K, src_total);
     launches++;
-    // cell multipoles (or bounding boxes) bottom-up, one launch per level, deepest first
-    const unsigned mg = std::max(1u, std::min(grid_for(internal, 256), (unsigned)sm_count * 8u));
+    // cell multipoles (or bounding boxes) bottom-up, one launch per non-empty
+    // level, deepest first
     for (int L = 21; L >= 0; L--) // keys have 21 digits: no cell below level 21
     {
+      if (per_level[L] <= 0)
+        continue;
+      const unsigned mg = std::max(1u, std::min(grid_for(per_level[L], 256), (unsigned)sm_count * 8u));
       if (geometric)
         k_tree_bounds<<<mg, 256, 0, st>>>(D, L);
       else

@@ -426,6 +426,136 @@ __global__ void __launch_bounds__(kRadixThreads)
   }
 }
 
+// One-block LSD radix sort of n <= Threads * kRadixItems items: every pass
+// runs in shared memory (the same per-warp ranking and digit scan as
+// k_radix_scatter, with the whole input as one tile), and the sorted items
+// are written back to (keys, vals).  It replaces three launches per pass for
+// the small sorts of the late iterations, where launch latency, not memory
+// traffic, is the cost.  Dynamic shared memory: radix_block_smem<K>(Threads).
+template <typename K>
+__host__ __device__ constexpr size_t radix_block_smem(int threads)
+{
+  return (size_t)threads * kRadixItems * (sizeof(K) + sizeof(uint32_t)) + sizeof(int) * (size_t)(threads / kWarp) * 256 +
+         sizeof(int) * (256 + 8);
+}
+
+template <typename K, int Threads>
+__global__ void __launch_bounds__(Threads)
+  k_radix_sort_block(K *__restrict__ keys, uint32_t *__restrict__ vals, int n, int begin_bit, int end_bit)
+{
+  constexpr int kWarps = Threads / kWarp;
+  constexpr int kN = Threads * kRadixItems;
+  extern __shared__ __align__(16) unsigned char radix_smem[];
+  K *s_key = reinterpret_cast<K *>(radix_smem);
+  uint32_t *s_val = reinterpret_cast<uint32_t *>(s_key + kN);
+  int *s_wcnt = reinterpret_cast<int *>(s_val + kN); // [kWarps][256]
+  int *s_start = s_wcnt + kWarps * 256;               // [256]
+  int *s_dsum = s_start + 256;                        // [8]: digit sums of the eight digit warps
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  const int wbase = warp * (kWarp * kRadixItems);
+  K key[kRadixItems];
+  uint32_t val[kRadixItems], dr[kRadixItems];
+#pragma unroll
+  for (int r = 0; r < kRadixItems; r++)
+  {
+    const int k = wbase + r * kWarp + lane;
+    key[r] = k < n ? keys[k] : K(0);
+    val[r] = k < n ? vals[k] : 0u;
+  }
+  for (int shift = begin_bit; shift < end_bit; shift += 8)
+  {
+    const int bits = (end_bit - shift) < 8 ? (end_bit - shift) : 8;
+    const uint32_t mask = (1u << bits) - 1u;
+    for (int i = tid; i < kWarps * 256; i += Threads)
+      s_wcnt[i] = 0;
+    __syncthreads();
+    // 1. rank within the warp, row by row (rows in item order: stable)
+#pragma unroll
+    for (int r = 0; r < kRadixItems; r++)
+    {
+      const int k = wbase + r * kWarp + lane;
+      const uint32_t d = k < n ? ((uint32_t)(key[r] >> shift) & mask) : 256u;
+      const uint32_t peers = __match_any_sync(0xffffffffu, d);
+      const int before = (d < 256u) ? s_wcnt[warp * 256 + d] : 0;
+      dr[r] = d | ((uint32_t)(before + __popc(peers & lt_mask)) << 9);
+      __syncwarp();
+      if (d < 256u && lane == __ffs(peers) - 1)
+        s_wcnt[warp * 256 + d] = before + __popc(peers);
+      __syncwarp();
+    }
+    __syncthreads();
+    // 2. threads 0..255, one per digit: each warp's offset within the digit,
+    // then the digit's first slot (exclusive scan over digits)
+    int run = 0, incl = 0;
+    if (tid < 256)
+    {
+      for (int w = 0; w < kWarps; w++)
+      {
+        const int c = s_wcnt[w * 256 + tid];
+        s_wcnt[w * 256 + tid] = run;
+        run += c;
+      }
+      incl = run;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1)
+      {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+          incl += y;
+      }
+      if (lane == 31)
+        s_dsum[warp] = incl;
+    }
+    __syncthreads();
+    if (tid < 256)
+    {
+      int woff = 0;
+      for (int w = 0; w < warp; w++)
+        woff += s_dsum[w];
+      s_start[tid] = woff + incl - run;
+    }
+    __syncthreads();
+    // 3. place in digit order, then read back in item order for the next pass
+#pragma unroll
+    for (int r = 0; r < kRadixItems; r++)
+    {
+      const uint32_t d = dr[r] & 511u;
+      if (d < 256u)
+      {
+        const int pos = s_start[d] + s_wcnt[warp * 256 + d] + (int)(dr[r] >> 9);
+        s_key[pos] = key[r];
+        s_val[pos] = val[r];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kRadixItems; r++)
+    {
+      const int k = wbase + r * kWarp + lane;
+      if (k < n)
+      {
+        key[r] = s_key[k];
+        val[r] = s_val[k];
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < kRadixItems; r++)
+  {
+    const int k = wbase + r * kWarp + lane;
+    if (k < n)
+    {
+      keys[k] = key[r];
+      vals[k] = val[r];
+    }
+  }
+}
+
+// Largest sort done by one block (k_radix_sort_block<K, 1024>).
+constexpr int kRadixBlockMax = 1024 * kRadixItems;
+
 inline size_t radix_table_elems(long long n)
 {
   const long long tiles = (n + kRadixTile - 1) / kRadixTile;
@@ -442,6 +572,21 @@ bool radix_sort_pairs(K *keys, uint32_t *vals, K *k_alt, uint32_t *v_alt, long l
 {
   if (n <= 1 || end_bit <= begin_bit)
     return false;
+  if (n <= kRadixTile)
+  { // one block, every pass in shared memory; the result stays in (keys, vals)
+    k_radix_sort_block<K, kRadixThreads><<<1, kRadixThreads, radix_block_smem<K>(kRadixThreads), st>>>(
+      keys, vals, (int)n, begin_bit, end_bit);
+    (*launches)++;
+    return false;
+  }
+  if (n <= kRadixBlockMax)
+  {
+    const size_t smem = radix_block_smem<K>(1024);
+    cudaFuncSetAttribute(k_radix_sort_block<K, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    k_radix_sort_block<K, 1024><<<1, 1024, smem, st>>>(keys, vals, (int)n, begin_bit, end_bit);
+    (*launches)++;
+    return false;
+  }
   const int tiles = (int)((n + kRadixTile - 1) / kRadixTile);
   bool flipped = false;
   for (int shift = begin_bit; shift < end_bit; shift += 8)

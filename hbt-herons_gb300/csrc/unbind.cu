@@ -210,6 +210,7 @@ struct hbtg_handle
   float threshold = 0.5f;
   float exclude_below = 0.f;
   long long min_particles = 0;
+  int first_test = 1;
   // state of the last unbinding call, for hbtg_trace_labels_device
   int last_S = 0;
   long long last_N = 0;
@@ -261,6 +262,7 @@ struct WarmArgs
   const long long *nb_prev = nullptr;
   const float *e_prev = nullptr;
   long long min_n = 0;
+  int first_test = 1;             // 0: uncertain particles join the set untested
   float *features_only = nullptr; // compute the features into this [6N] array and stop
 };
 
@@ -490,6 +492,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
     W.feat = wa->features_only;
     W.prop = wa->proposal;
     W.min_n = wa->min_n;
+    W.first_test = wa->first_test;
     mem.mark(-1);
     if (wa->features_only || !wa->proposal)
     {
@@ -724,6 +727,7 @@ int host_call(void *arg)
   if (c.learned)
   {
     wa.min_n = H->min_particles;
+    wa.first_test = H->first_test;
     if (c.prior && c.prior->nbound_prev)
     {
       wa.nb_prev = reinterpret_cast<const long long *>(upload(P, S_PNB, c.prior->nbound_prev, S, st, h2d));
@@ -1267,6 +1271,7 @@ int model_call(void *arg)
   c.H->threshold = c.m->threshold;
   c.H->exclude_below = c.m->exclude_below;
   c.H->min_particles = c.m->min_particles;
+  c.H->first_test = c.m->first_test;
   return HBTG_OK;
 }
 
@@ -1432,7 +1437,7 @@ int hbtg_unbind_batch_device(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b
 int hbtg_set_model(hbtg_handle *h, const hbtg_model *m)
 {
   if (!h || !m || !m->weights || !(m->threshold == m->threshold) || !(m->exclude_below <= m->threshold) ||
-      m->min_particles < 0)
+      m->min_particles < 0 || (m->first_test != 0 && m->first_test != 1))
     return HBTG_ERR_INVALID;
   ModelCall c{h, m};
   return guarded(model_call, &c);
@@ -1453,6 +1458,7 @@ int hbtg_unbind_batch_learned_device(hbtg_handle *h, const hbtg_params *p, hbtg_
     return HBTG_ERR_INVALID;
   WarmArgs wa;
   wa.min_n = h->min_particles;
+  wa.first_test = h->first_test;
   if (prior && prior->nbound_prev)
   {
     wa.nb_prev = reinterpret_cast<const long long *>(prior->nbound_prev);

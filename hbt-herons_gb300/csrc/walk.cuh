@@ -65,11 +65,23 @@ namespace hbtg
 namespace
 {
 
+// List and stack capacities (per warp) and the resident blocks the launch
+// bounds ask for; the defaults are the measured best on GB300 (overridable at
+// build time for launch-shape sweeps).
+#ifndef HBTG_WALK_FULL
+#define HBTG_WALK_FULL 96
+#endif
+#ifndef HBTG_WALK_STACK
+#define HBTG_WALK_STACK 256
+#endif
+#ifndef HBTG_WALK_MIN_BLOCKS
+#define HBTG_WALK_MIN_BLOCKS 1
+#endif
 constexpr int kWalkWarps = 4;   // warps per block
-constexpr int kWalkFull = 96;   // far-list entries that every target takes, per warp
+constexpr int kWalkFull = HBTG_WALK_FULL; // far-list entries that every target takes, per warp
 constexpr int kWalkFar = 64;    // other far-list entries per warp
 constexpr int kWalkNear = 64;   // near-list entries per warp
-constexpr int kWalkStack = 256; // traversal ranges per warp
+constexpr int kWalkStack = HBTG_WALK_STACK; // traversal ranges per warp
 constexpr int kWalkDrain = kWalkStack - 64; // a deeper stack is drained (a step pushes at most 2 per lane)
 constexpr int kWalkPending = 64; // cells waiting for the targets' own opening tests
 constexpr int kWalkWarp2 = 16;  // target pairs per warp
@@ -697,7 +709,8 @@ __device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, 
 // the tree slots in L1; a warp whose range is used up moves on to the next
 // ranges (each tried once).  Without counters, a grid-stride loop.
 template <bool Count>
-__global__ void __launch_bounds__(32 * kWalkWarps) k_walk(DevState D, KParams K, int total_chunks, int nranges)
+__global__ void __launch_bounds__(32 * kWalkWarps, HBTG_WALK_MIN_BLOCKS)
+  k_walk(DevState D, KParams K, int total_chunks, int nranges)
 {
   __shared__ WalkShared sh;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;

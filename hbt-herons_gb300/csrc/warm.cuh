@@ -72,8 +72,9 @@ struct WarmBufs
   unsigned long long *hist; // [64 S] fixed-point mass per radial bin
   float *tab;               // [kTab S]
   float *feat;              // [6 N]
-  const uint8_t *prop;      // [N] proposal: 1 trusted, 0 to test, 2 left out
+  const uint8_t *prop;      // [N] proposal: 1 trusted, 0 uncertain, 2 left out
   long long min_n;          // subhaloes with fewer particles start cold
+  int first_test;           // 1: the uncertain particles get the first test; 0: they join untested
 };
 
 __device__ __forceinline__ bool has_prior(const WarmBufs &W, int s) { return W.nb_prev && W.nb_prev[s] > 0; }
@@ -425,7 +426,9 @@ __global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
   const int n = D.n_s[s];
   const int npred = D.F[D.off[s + 1]] - D.F[D.off[s]];
   const int ntest = D.X[D.off[s + 1]] - D.X[D.off[s]];
-  const bool warm = warm_eligible(D, W, s) && (float)npred < __fmul_rn((float)n, K.bmp);
+  // without the first test the uncertain particles stay in the set
+  const int nkept = W.first_test ? npred : npred + ntest;
+  const bool warm = warm_eligible(D, W, s) && (float)nkept < __fmul_rn((float)n, K.bmp);
   D.warm[s] = warm ? 1 : 0;
   D.flag_s[s] = warm ? 1 : 0;
   D.nexcl[s] = warm ? n - npred : 0;
@@ -620,6 +623,44 @@ __global__ void k_first_apply(DevState D, KParams K)
     D.warm[s] = 4;
   else
     D.flag_s[s] = 1;
+}
+
+// Without the first test: the uncertain particles (positions [nbound,
+// nbound + ntest) of a warm subhalo, after the trusted ones) join the set.
+// Runs after the trusted particles' frame is computed.
+__global__ void k_untested_bnd(DevState D)
+{
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= D.N)
+    return;
+  const int s = D.seg_of[g];
+  if (D.warm[s] != 1)
+    return;
+  const long long k = g - D.off[s];
+  if (k >= D.nbound[s] && k < (long long)D.nbound[s] + D.ntest[s])
+    D.bnd[D.ord[g]] = 1;
+}
+
+// The set after the proposal without the first test: trusted plus uncertain.
+// As after the test, a subhalo whose first iteration would already have
+// converged is marked for a cold restart (warm = 4).
+__global__ void k_untested_apply(DevState D, KParams K)
+{
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= D.S)
+    return;
+  D.flag_s[s] = 0;
+  if (D.warm[s] != 1)
+    return;
+  const int nb = D.nbound[s] + D.ntest[s];
+  D.nbound[s] = nb;
+  D.nlast[s] = nb;
+  D.corr[s] = 0;
+  D.self_cnt[s] = 0;
+  D.nexcl[s] = D.n_s[s] - nb;
+  D.iter_extra[s] = 1; // the first iteration, done by the proposal
+  if ((float)nb >= __fmul_rn((float)D.n_s[s], K.bmp))
+    D.warm[s] = 4;
 }
 
 // Cold restart of the warm subhaloes marked for it (warm = 4).
@@ -824,8 +865,24 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     R.launches++;
   }
   R.check();
-  C.readmitted += first_test(R, W);
-  C.readmit_rounds++;
+  if (W.first_test)
+  {
+    C.readmitted += first_test(R, W);
+    C.readmit_rounds++;
+  }
+  else
+  { // the first frame from the trusted particles alone (k_warm_setup flagged
+    // the warm subhaloes), then the uncertain ones join the set
+    flagged_frames(R);
+    if (D.N > 0)
+    {
+      k_untested_bnd<<<grid_for(D.N, 256), 256, 0, st>>>(D);
+      R.launches++;
+    }
+    k_untested_apply<<<sb, 256, 0, st>>>(D, R.K);
+    R.launches++;
+    R.check();
+  }
   {
     std::vector<int> nex(S);
     R.mem.check(cudaMemcpyAsync(nex.data(), D.nexcl, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
@@ -834,7 +891,8 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     for (int v : nex)
       C.excluded += v;
   }
-  flagged_frames(R); // the frame of the set the second iteration evaluates
+  if (W.first_test)
+    flagged_frames(R); // the frame of the set the second iteration evaluates
   k_warm_fallback<<<sb, 256, 0, st>>>(D); // subhaloes whose first iteration converges run cold
   R.launches++;
   if (D.N > 0)

@@ -176,7 +176,7 @@ class CPrior(C.Structure):
 class CModel(C.Structure):
     """hbtg_model."""
     _fields_ = [("weights", _P), ("threshold", C.c_float), ("min_particles", C.c_int64),
-                ("exclude_below", C.c_float)]
+                ("exclude_below", C.c_float), ("first_test", C.c_int32)]
 
 
 MLP_PARAMS = 4673

@@ -126,12 +126,12 @@ class Unbinder:
         return s.as_dict()
 
     # -- warm start ---------------------------------------------------------
-    def set_model(self, weights, threshold, min_particles=0, exclude_below=0.0):
+    def set_model(self, weights, threshold, min_particles=0, exclude_below=0.0, first_test=1):
         """Loads the proposer network (hbtg_set_model)."""
         w = np.ascontiguousarray(weights, dtype=np.float32)
         if w.shape != (MLP_PARAMS,):
             raise ValueError("expected %d weights" % MLP_PARAMS)
-        m = CModel(w.ctypes.data, float(threshold), int(min_particles), float(exclude_below))
+        m = CModel(w.ctypes.data, float(threshold), int(min_particles), float(exclude_below), int(first_test))
         rc = self.lib.hbtg_set_model(self.h, C.byref(m))
         if rc != 0:
             raise UnbindError(rc, "hbtg_set_model")

@@ -39,21 +39,23 @@ class Model:
     min_particles: int = 100    # smaller subhaloes start cold
     meta: dict = field(default_factory=dict)
     exclude_below: float = 0.0  # left out without the first test below
+    first_test: int = 1         # 1: uncertain particles get the first test; 0: they join the set untested
 
     def save(self, path):
         np.savez(path, weights=np.asarray(self.weights, np.float32), threshold=np.float32(self.threshold),
                  min_particles=np.int64(self.min_particles), exclude_below=np.float32(self.exclude_below),
-                 meta=np.array(json.dumps(self.meta)))
+                 first_test=np.int32(self.first_test), meta=np.array(json.dumps(self.meta)))
 
     @staticmethod
     def load(path=MODEL_FILE):
         z = np.load(path)
         lo = float(z["exclude_below"]) if "exclude_below" in z else 0.0
+        ft = int(z["first_test"]) if "first_test" in z else 1
         return Model(z["weights"].astype(np.float32), float(z["threshold"]), int(z["min_particles"]),
-                     json.loads(str(z["meta"])), lo)
+                     json.loads(str(z["meta"])), lo, ft)
 
     def install(self, unbinder):
-        unbinder.set_model(self.weights, self.threshold, self.min_particles, self.exclude_below)
+        unbinder.set_model(self.weights, self.threshold, self.min_particles, self.exclude_below, self.first_test)
 
 
 def initial_weights(seed=0):

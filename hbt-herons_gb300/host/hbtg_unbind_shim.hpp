@@ -83,12 +83,14 @@ public:
   Unbinder(const Unbinder &) = delete;
   Unbinder &operator=(const Unbinder &) = delete;
 
-  // Loads the learned warm start's proposer (weights of hbtg_mlp_forward's layout).
-  void set_model(const std::vector<float> &weights, float threshold, float exclude_below, int64_t min_particles)
+  // Loads the learned warm start's proposer (weights of hbtg_mlp_forward's
+  // layout); first_test as in hbtg_model.
+  void set_model(const std::vector<float> &weights, float threshold, float exclude_below, int64_t min_particles,
+                 int first_test = 1)
   {
     if (weights.size() != HBTG_MLP_PARAMS)
       throw std::runtime_error("hbtg_set_model: wrong number of weights");
-    hbtg_model m{weights.data(), threshold, min_particles, exclude_below};
+    hbtg_model m{weights.data(), threshold, min_particles, exclude_below, (int32_t)first_test};
     const int rc = hbtg_set_model(h_, &m);
     if (rc != HBTG_OK)
       throw std::runtime_error(std::string("hbtg_set_model: ") + hbtg_status_string(rc));

@@ -344,14 +344,20 @@ typedef struct hbtg_prior
 
 /* The learned proposer: a particle is trusted when the network's
  * probability is >= threshold, left out without the first test when it is
- * below exclude_below (0 = test every untrusted particle), tested otherwise;
- * subhaloes with fewer than min_particles particles start cold. */
+ * below exclude_below (0 = test every untrusted particle), uncertain
+ * otherwise; subhaloes with fewer than min_particles particles start cold.
+ * first_test = 1: every uncertain particle gets the plain method's first
+ * test (its energy against the tree of every particle) and joins the set if
+ * bound.  first_test = 0: the uncertain particles join the set untested (the
+ * exact iteration removes those that are unbound) and the first frame is
+ * that of the trusted particles alone; this skips the tree of every particle. */
 typedef struct hbtg_model
 {
   const float *weights; /* [HBTG_MLP_PARAMS] host array */
   float threshold;
   int64_t min_particles;
   float exclude_below;  /* <= threshold */
+  int32_t first_test;   /* 1 or 0, see above */
 } hbtg_model;
 
 /* Copies the proposer network to the handle's device. */

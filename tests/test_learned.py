@@ -333,3 +333,44 @@ def test_trained_network_gains_over_the_plain_method(unbinder):
     assert m["mass_rel"] <= 2e-4 and m["membership"] <= 2 * PATH_NOISE, m
     assert st["warm_subhaloes"] > 0
     assert st["interactions"] < 0.85 * work_plain, (st["interactions"], work_plain)
+
+
+@pytest.mark.gpu
+def test_uncertain_particles_join_untested(unbinder):
+    """first_test = 0: the particles between the two thresholds join the set
+    without the first test (no tree of every particle), the first frame is the
+    trusted particles' own, and the exact iteration still ends at the plain
+    fixed point with every kept particle bound."""
+    from hbtg.gpu import DeviceBatch
+    if not os.path.exists(learned.MODEL_FILE):
+        pytest.skip("no trained model shipped")
+    params = _params()
+    inp = synthetic.stripped(n_sub=1500, seed=23, nmax=100_000)
+    db = DeviceBatch(inp)
+    db.reset_inout()
+    unbinder.unbind_device(params, db.c)
+    plain = db.outputs()
+    m = learned.Model.load()
+    got = {}
+    for ft in (1, 0):
+        unbinder.set_model(m.weights, m.threshold, m.min_particles, m.exclude_below, ft)
+        db.reset_inout()
+        unbinder.unbind_learned_device(params, db)
+        got[ft] = (db.outputs(), unbinder.stats())
+    m.install(unbinder)
+    warm, st = got[0]
+    check_invariants(inp, warm)
+    assert st["warm_subhaloes"] > 0 and st["readmitted"] == 0 and st["readmit_rounds"] == 0
+    assert got[1][1]["readmit_rounds"] == 1
+    r = compare(inp, warm, plain)
+    assert r["mass_rel"] <= 2e-4 and r["membership"] <= 2 * PATH_NOISE, r
+    # the tree of every particle is not built: fewer tree cells than with the test
+    assert st["tree_nodes"] < got[1][1]["tree_nodes"], (st["tree_nodes"], got[1][1]["tree_nodes"])
+
+
+def test_model_file_keeps_first_test(tmp_path):
+    m = learned.Model(learned.initial_weights(2), 0.9, 50, {}, 1e-3, 0)
+    p = str(tmp_path / "m.npz")
+    m.save(p)
+    m2 = learned.Model.load(p)
+    assert m2.first_test == 0 and m2.exclude_below == pytest.approx(1e-3)
