@@ -240,6 +240,13 @@ def bench_reference(args):
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": kind, "cpu_model": cpu_model(),
                          "sample": _sample_text(inp, sample, picked)},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "implementation": ("the reference's own Unbind, compiled from its sources (oracle/_ref)" if kind == "reference"
+                           else "the oracle's restatement of the reference's Unbind (oracle/unbind_port.cpp), pinned "
+                                "bit for bit to the reference's own outputs (tests/golden); the reference's own build "
+                                "needs its sources, which this machine does not have"),
+        "same_config": False,
+        "why_sampled": "the whole batch would take hours on the host cores; each step times a particle-weighted "
+                       "stratified sample of the same batch (same size distribution, largest decade included)",
     }
     print(json.dumps(line))
     return 0
@@ -465,7 +472,7 @@ def bench_gpu(args):
                        "softening": 0.005, "bound_mass_precision": 0.995, "max_sample_size": 0,
                        "l2": "inputs larger than L2 (%.1f GB of particle data)" % (inp.n_particles * 44 / 1e9),
                        "proposer": {"threshold": model.threshold, "exclude_below": model.exclude_below,
-                                    "min_particles": model.min_particles,
+                                    "first_test": model.first_test, "min_particles": model.min_particles,
                                     "trained_on": {k: model.meta.get(k) for k in ("n_sub_stripped", "n_batched",
                                                                                   "rows", "steps")}},
                        "global_iterations": {"learned": cw["global_iterations"],

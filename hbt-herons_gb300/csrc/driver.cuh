@@ -76,33 +76,47 @@ struct IterationDriver
     return h;
   }
 
-  struct Count3Load
+  // Up to four count arrays (null = none) read as one I4c item.
+  struct Count4Load
   {
-    const int *a, *b, *c;
-    __device__ I3 operator()(long long i) const { return I3{a[i], b[i], c[i]}; }
-  };
-  struct Count3Store
-  {
-    int *a, *b, *c;
-    __device__ void operator()(long long i, const I3 &v) const
+    const int *a, *b, *c, *d;
+    __device__ I4c operator()(long long i) const
     {
-      a[i] = v.a;
-      b[i] = v.b;
-      c[i] = v.c;
+      return I4c{a ? a[i] : 0, b ? b[i] : 0, c ? c[i] : 0, d ? d[i] : 0};
+    }
+  };
+  struct Count4Store
+  {
+    int *a, *b, *c, *d;
+    __device__ void operator()(long long i, const I4c &v) const
+    {
+      if (a)
+        a[i] = v.a;
+      if (b)
+        b[i] = v.b;
+      if (c)
+        c[i] = v.c;
+      if (d)
+        d[i] = v.d;
     }
   };
 
-  // Exclusive scans of three count arrays (n counts plus a trailing zero
-  // each) in one pass, with one host read of the three totals.
-  void scan_counts3(const int *c0, int *o0, const int *c1, int *o1, const int *c2, int *o2, long long n, int tot[3])
+  // Exclusive scans of up to four count arrays (n counts plus a trailing zero
+  // each; null pairs are skipped) in one pass, with one host read of the totals.
+  void scan_counts4(const int *c0, int *o0, const int *c1, int *o1, const int *c2, int *o2, const int *c3, int *o3,
+                    long long n, int tot[4])
   {
-    // an int scratch for 8 (n + 1) items covers scan_scratch_elems<I3>(n + 1) I3s
-    I3 *scr = reinterpret_cast<I3 *>(mem.scan_scratch(8 * (n + 1)));
-    scan_load_store<I3, false>(Count3Load{c0, c1, c2}, Count3Store{o0, o1, o2}, n + 1, scr, st, &launches);
+    // an int scratch for 8 (n + 1) items covers scan_scratch_elems<I4c>(n + 1) I4cs
+    I4c *scr = reinterpret_cast<I4c *>(mem.scan_scratch(8 * (n + 1)));
+    scan_load_store<I4c, false>(Count4Load{c0, c1, c2, c3}, Count4Store{o0, o1, o2, o3}, n + 1, scr, st, &launches);
     check();
-    mem.check(cudaMemcpyAsync(&tot[0], o0 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
-    mem.check(cudaMemcpyAsync(&tot[1], o1 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
-    mem.check(cudaMemcpyAsync(&tot[2], o2 + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int *outs[4] = {o0, o1, o2, o3};
+    for (int k = 0; k < 4; k++)
+    {
+      tot[k] = 0;
+      if (outs[k])
+        mem.check(cudaMemcpyAsync(&tot[k], outs[k] + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
     mem.check(cudaStreamSynchronize(st));
     host_syncs++;
   }
@@ -221,10 +235,10 @@ struct IterationDriver
     check();
   }
 
-  // Targets of the correction walks in key order (see k_tgt_flags).
-  void correction_targets()
+  // Targets of the correction walks in key order (see k_tgt_flags); `total`
+  // is the sum of sp_cnt, already scanned into sp_off.
+  void correction_targets(int total)
   {
-    const int total = scan_counts(D.sp_cnt, D.sp_off, S);
     if (total == 0)
       return;
     k_tgt_flags<<<grid_for(total + 1, 256), 256, 0, st>>>(D, total);
@@ -271,9 +285,9 @@ struct IterationDriver
       k_plan<<<sb, 256, 0, st>>>(D, K);
       launches++;
       check();
-      int tot[3];
-      scan_counts3(D.src_cnt, D.src_off, D.chunk_cnt, D.chunk_off, D.part_cnt, D.part_off, S, tot);
-      const int src_total = tot[0], chunk_total = tot[1], part_total = tot[2];
+      int tot[4];
+      scan_counts4(D.src_cnt, D.src_off, D.chunk_cnt, D.chunk_off, D.part_cnt, D.part_off, D.sp_cnt, D.sp_off, S, tot);
+      const int src_total = tot[0], chunk_total = tot[1], part_total = tot[2], sp_total = tot[3];
       mem.mark(0);
       if (part_total == 0 && src_total == 0)
         break;
@@ -291,7 +305,7 @@ struct IterationDriver
         k_record_candidates<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
         launches++;
       }
-      correction_targets();
+      correction_targets(sp_total);
       mem.mark(2);
       walk(chunk_total);
       mem.mark(1);
@@ -306,9 +320,12 @@ struct IterationDriver
         k_part_scatter<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
         k_part_copy<<<grid_for(part_total, 256), 256, 0, st>>>(D, part_total);
         k_after_part<<<sb, 256, 0, st>>>(D, K);
-        launches += 4;
+        k_plan_counts<<<sb, 256, 0, st>>>(D, 0); // the bound sets for the frame sums
+        launches += 5;
         check();
-        const int tail_total = scan_counts(D.tail_cnt, D.tail_off, S);
+        int tb[4];
+        scan_counts4(D.tail_cnt, D.tail_off, D.fin_cnt, D.fin_off, nullptr, nullptr, nullptr, nullptr, S, tb);
+        const int tail_total = tb[0], bound_total = tb[1];
         if (tail_total > 0)
         {
           k_energy_keys<<<grid_for(tail_total, 256), 256, 0, st>>>(D, D.tail_off, tail_total, 0);
@@ -319,9 +336,6 @@ struct IterationDriver
           check();
         }
         mem.mark(3);
-        k_plan_counts<<<sb, 256, 0, st>>>(D, 0);
-        launches++;
-        const int bound_total = scan_counts(D.fin_cnt, D.fin_off, S);
         if (bound_total > 0)
         {
           k_com<<<grid_for((bound_total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, K,
@@ -363,8 +377,9 @@ struct IterationDriver
     k_plan_refine<<<sb, 256, 0, st>>>(D, K);
     launches++;
     check();
-    const int src_total = scan_counts(D.src_cnt, D.src_off, S);
-    const int chunk_total = scan_counts(D.chunk_cnt, D.chunk_off, S);
+    int tot[4];
+    scan_counts4(D.src_cnt, D.src_off, D.chunk_cnt, D.chunk_off, nullptr, nullptr, nullptr, nullptr, S, tot);
+    const int src_total = tot[0], chunk_total = tot[1];
     if (src_total == 0)
       return;
     build_tree(src_total);

@@ -46,6 +46,13 @@ struct I3
   __host__ __device__ I3 operator+(const I3 &o) const { return I3{a + o.a, b + o.b, c + o.c}; }
 };
 
+// Four counts scanned together (one pass, one host read of the totals).
+struct I4c
+{
+  int a, b, c, d;
+  __host__ __device__ I4c operator+(const I4c &o) const { return I4c{a + o.a, b + o.b, c + o.c, d + o.d}; }
+};
+
 // Segmented double sum: head marks the first item of a segment, where the
 // running sum restarts.  Associative, not commutative.
 struct SegD
@@ -78,6 +85,8 @@ __device__ __forceinline__ I4 zero_of<I4>() { return I4{0, 0, 0, 0}; }
 template <>
 __device__ __forceinline__ I3 zero_of<I3>() { return I3{0, 0, 0}; }
 template <>
+__device__ __forceinline__ I4c zero_of<I4c>() { return I4c{0, 0, 0, 0}; }
+template <>
 __device__ __forceinline__ SegD zero_of<SegD>() { return SegD{0., 0}; }
 
 template <typename T>
@@ -90,6 +99,12 @@ __device__ __forceinline__ I3 shfl_up<I3>(I3 v, int d)
 {
   return I3{__shfl_up_sync(0xffffffffu, v.a, d), __shfl_up_sync(0xffffffffu, v.b, d),
             __shfl_up_sync(0xffffffffu, v.c, d)};
+}
+template <>
+__device__ __forceinline__ I4c shfl_up<I4c>(I4c v, int d)
+{
+  return I4c{__shfl_up_sync(0xffffffffu, v.a, d), __shfl_up_sync(0xffffffffu, v.b, d),
+             __shfl_up_sync(0xffffffffu, v.c, d), __shfl_up_sync(0xffffffffu, v.d, d)};
 }
 template <>
 __device__ __forceinline__ I4 shfl_up<I4>(I4 v, int d)
@@ -114,6 +129,12 @@ __device__ __forceinline__ I3 shfl_idx<I3>(I3 v, int src)
 {
   return I3{__shfl_sync(0xffffffffu, v.a, src), __shfl_sync(0xffffffffu, v.b, src),
             __shfl_sync(0xffffffffu, v.c, src)};
+}
+template <>
+__device__ __forceinline__ I4c shfl_idx<I4c>(I4c v, int src)
+{
+  return I4c{__shfl_sync(0xffffffffu, v.a, src), __shfl_sync(0xffffffffu, v.b, src),
+             __shfl_sync(0xffffffffu, v.c, src), __shfl_sync(0xffffffffu, v.d, src)};
 }
 template <>
 __device__ __forceinline__ I4 shfl_idx<I4>(I4 v, int src)

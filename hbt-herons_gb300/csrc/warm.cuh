@@ -794,10 +794,10 @@ long long first_test(IterationDriver<Mem> &R, const WarmBufs &W)
   k_plan_first<<<grid_for(S + 1, 256), 256, 0, st>>>(D);
   R.launches++;
   R.check();
-  const int src_total = R.scan_counts(D.src_cnt, D.src_off, S);
-  const int chunk_total = R.scan_counts(D.chunk_cnt, D.chunk_off, S);
-  const int part_total = R.scan_counts(D.part_cnt, D.part_off, S);
-  const int tail_total = R.scan_counts(D.tail_cnt, D.tail_off, S);
+  int tot[4];
+  R.scan_counts4(D.src_cnt, D.src_off, D.chunk_cnt, D.chunk_off, D.part_cnt, D.part_off, D.tail_cnt, D.tail_off, S,
+                 tot);
+  const int src_total = tot[0], chunk_total = tot[1], part_total = tot[2], tail_total = tot[3];
   R.mem.mark(6);
   if (src_total > 0)
   {
@@ -873,6 +873,7 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
   else
   { // the first frame from the trusted particles alone (k_warm_setup flagged
     // the warm subhaloes), then the uncertain ones join the set
+    R.mem.mark(6); // the proposal ends here
     flagged_frames(R);
     if (D.N > 0)
     {
