@@ -373,6 +373,7 @@ def bench_gpu(args):
         assert rc in (0, 4), rc
 
     e2e_call()  # warm the host path once
+    link = host_link_rates("cuda:%d" % local, u.stats()["h2d_bytes"], u.stats()["d2h_bytes"], args.steps)
     e2e_times, e2e_device, e2e_h2d, e2e_d2h, h2d, d2h = [], [], [], [], 0, 0
     for _ in range(args.steps):
         _reset_frames(buf, hin)
@@ -497,7 +498,11 @@ def bench_gpu(args):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "call": "hbtg_unbind_batch_learned (host pointers, pinned)",
                     "ms_per_call": 1e3 * float(np.mean(e2e_times)),
-                    "ms_device_part": float(np.mean(e2e_device)), "ms_uploads": h2d_ms, "ms_downloads": d2h_ms},
+                    "ms_device_part": float(np.mean(e2e_device)), "ms_uploads": h2d_ms, "ms_downloads": d2h_ms,
+                    "ms_uploads_each": [round(x, 2) for x in e2e_h2d],
+                    "ms_downloads_each": [round(x, 2) for x in e2e_d2h],
+                    "value_best_call": (warm["bound_all"] / args.steps) / float(np.min(e2e_times)),
+                    "host_link": link},
             "gpu_launches": warm["kernel_launches"] // args.steps,
             "host_syncs_per_step": warm["last"].get("host_syncs"),
             "roofline": {"kernel": "k_walk", "bound": "fp32", "achieved": achieved, "peak": peak,
@@ -574,6 +579,33 @@ def side_workload(kind, u, args, local, stream):
         res["cpu"] = {"value": float(out.nbound.sum() / dt), "cores": os.cpu_count() or 1, "kind": kind_cpu,
                       "sample": _sample_text(inp, sample, picked)}
     return res
+
+
+def host_link_rates(device, up_bytes, down_bytes, reps):
+    """Plain pinned copies of the e2e call's byte counts (one cudaMemcpyAsync
+    each way, CUDA events), repeated: the host link's own rate at the time of
+    the e2e calls, which shares the link with the machine's other GPUs."""
+    import torch
+    up = torch.empty(int(up_bytes), dtype=torch.uint8, pin_memory=True)
+    down = torch.empty(int(down_bytes), dtype=torch.uint8, pin_memory=True)
+    dev = torch.empty(int(max(up_bytes, down_bytes)), dtype=torch.uint8, device=device)
+    up.fill_(1)
+    ups, downs = [], []
+    for _ in range(max(3, reps)):
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record()
+        dev[:up.numel()].copy_(up, non_blocking=True)
+        e[1].record()
+        down.copy_(dev[:down.numel()], non_blocking=True)
+        e[2].record()
+        torch.cuda.synchronize()
+        ups.append(e[0].elapsed_time(e[1]))
+        downs.append(e[1].elapsed_time(e[2]))
+    del up, down, dev
+    return {"h2d_GBs_each": [round(up_bytes / (t * 1e-3) / 1e9, 1) for t in ups],
+            "d2h_GBs_each": [round(down_bytes / (t * 1e-3) / 1e9, 1) for t in downs],
+            "note": "plain pinned copies of the same byte counts just before the e2e calls"}
 
 
 def _membership(inp, got, ref):

@@ -65,17 +65,16 @@ namespace hbtg
 namespace
 {
 
-// List and stack capacities (per warp) and the resident blocks the launch
-// bounds ask for; the defaults are the measured best on GB300 (overridable at
-// build time for launch-shape sweeps).
+// List and stack capacities (per warp); the defaults are the measured best on
+// GB300 (overridable at build time for sweeps).  HBTG_WALK_MIN_BLOCKS, when
+// defined, adds a minimum of resident blocks to the launch bounds (a register
+// cap); by default the compiler's own allocation (72 registers, 7 blocks of 4
+// warps per SM, limited equally by registers and shared memory) is kept.
 #ifndef HBTG_WALK_FULL
 #define HBTG_WALK_FULL 96
 #endif
 #ifndef HBTG_WALK_STACK
 #define HBTG_WALK_STACK 256
-#endif
-#ifndef HBTG_WALK_MIN_BLOCKS
-#define HBTG_WALK_MIN_BLOCKS 1
 #endif
 constexpr int kWalkWarps = 4;   // warps per block
 constexpr int kWalkFull = HBTG_WALK_FULL; // far-list entries that every target takes, per warp
@@ -709,7 +708,11 @@ __device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, 
 // the tree slots in L1; a warp whose range is used up moves on to the next
 // ranges (each tried once).  Without counters, a grid-stride loop.
 template <bool Count>
+#ifdef HBTG_WALK_MIN_BLOCKS
 __global__ void __launch_bounds__(32 * kWalkWarps, HBTG_WALK_MIN_BLOCKS)
+#else
+__global__ void __launch_bounds__(32 * kWalkWarps)
+#endif
   k_walk(DevState D, KParams K, int total_chunks, int nranges)
 {
   __shared__ WalkShared sh;
