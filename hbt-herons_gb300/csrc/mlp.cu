@@ -3,11 +3,13 @@
 //
 // Weights are one flat FP32 array (HBTG_MLP_PARAMS floats):
 //   W1[6][64] (in x out), b1[64], W2[64][64] (in x out), b2[64], w3[64], b3
-// Kernels stage them in shared memory as BF16; every layer is a chain of
-// mma.sync.m16n8k16 (BF16 operands, FP32 accumulation) over tiles of 16 rows,
-// one tile per warp.  The accumulator fragment of one layer is re-packed in
-// registers as the A fragment of the next (the m16n8 C layout of two adjacent
-// n-tiles is the m16k16 A layout).
+// Inference (hbtg_mlp_forward) runs on the tcgen05 tensor cores with TMEM
+// accumulators (k_mlp_forward_tc, below).  Training (hbtg_mlp_backward)
+// stages the weights in shared memory as BF16 and chains mma.sync.m16n8k16
+// (BF16 operands, FP32 accumulation) over tiles of 16 rows, one tile per warp:
+// the accumulator fragment of one layer is re-packed in registers as the A
+// fragment of the next (the m16n8 C layout of two adjacent n-tiles is the
+// m16k16 A layout), and the backward pass needs those per-warp fragments.
 #include <algorithm>
 #include <cstdint>
 #include <cuda_bf16.h>
@@ -170,25 +172,272 @@ __device__ __forceinline__ void forward_tile(const SmemWeights &S, const float *
   T.logit_g8 = __shfl_sync(0xffffffffu, d[2], lane & ~3) + S.b3;
 }
 
-__global__ void __launch_bounds__(256) k_mlp_forward(const float *__restrict__ w, const float *__restrict__ x,
-                                                     float *__restrict__ prob, long long n)
+// ---------------------------------------------------------------------------
+// Inference on the Blackwell tensor cores (tcgen05).  A CTA of four warps
+// takes tiles of 128 rows.  Layer 1 (K = 16: the six features and ten zeros)
+// and layer 2 (K = 64) are tcgen05.mma.kind::f16 issued by one thread: BF16
+// operands in shared memory, FP32 accumulators in tensor memory (TMEM, 128
+// lanes = rows; columns 0-63 layer 1, 64-127 layer 2), completion signalled
+// to an mbarrier by tcgen05.commit.  The epilogues run on the CUDA cores from
+// tcgen05.ld (thread t reads TMEM lane t, i.e. row t of the tile): bias,
+// ReLU and BF16 rounding into layer 2's A operand; then bias, ReLU, BF16
+// rounding and the output neuron's 64-term dot product with the BF16 w3 in
+// FP32, and the sigmoid -- the rounding points of the mma.sync training
+// kernels and of the numpy oracle.
+//
+// Operand layout (no swizzle, K-major): core matrices of 8 rows x 16 bytes
+// (8 BF16 along K), stored row by row; the core matrices of one 8-row group
+// follow each other along K (leading byte offset 128), and the 8-row groups
+// are K * 16 bytes apart (stride byte offset).
+//
+// Every wait on the mbarrier is bounded (about one second of clock); a CTA
+// that gives up writes NaN for the rows it has not finished (a NaN
+// probability is neither trusted nor left out, so the exact iteration decides
+// those particles), frees its tensor memory and returns.
+// ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr uint32_t kTmemCols = 128;
+constexpr size_t kTcSmemBytes = 52 * 1024; // at most 4 CTAs per SM: 4 x 128 TMEM columns = 512
+constexpr long long kTcWaitCycles = 2000000000LL;
+
+struct TcSmem
 {
-  __shared__ SmemWeights S;
-  load_weights(S, w, false);
-  const int lane = threadIdx.x & 31, g = lane >> 2, c = lane & 3;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long row0 = warp * 16; row0 < n; row0 += nwarps * 16)
+  __nv_bfloat16 a1[kTcRows * 16]; // A of layer 1: the features (BF16), K = 16
+  __nv_bfloat16 a2[kTcRows * kHid]; // A of layer 2: relu(layer 1) in BF16, K = 64
+  __nv_bfloat16 b1[kHid * 16];    // B of layer 1: W1^T (N = 64 x K = 16)
+  __nv_bfloat16 b2[kHid * kHid];  // B of layer 2: W2^T (N = 64 x K = 64)
+  float bias1[kHid], bias2[kHid], w3[kHid], b3;
+  unsigned long long mbar;
+  uint32_t tmem_base;
+};
+static_assert(sizeof(TcSmem) <= kTcSmemBytes, "tcgen05 forward shared memory");
+
+// Byte offset of element (row, k) of a K-major operand with K columns.
+__device__ __forceinline__ uint32_t kmajor_off(int row, int k, int K)
+{
+  return (uint32_t)((row >> 3) * (K * 16) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: start address, leading and stride byte
+// offsets (each encoded >> 4), descriptor version 1, no swizzling.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N = 64, M = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kHid >> 3) << 17) |
+                              ((uint32_t)(kTcRows >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate)
+{
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+               "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+               "l"(a), "l"(b), "r"(kTcIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t mbar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+               : "memory");
+}
+
+// Bounded wait for the mbarrier phase with the given parity; false on timeout.
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity)
+{
+  const long long t0 = clock64();
+  for (;;)
   {
-    Tile T;
-    forward_tile(S, x, row0, n, T);
-    if (c == 0)
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}\n"
+                 : "=r"(done)
+                 : "r"(mbar), "r"(parity)
+                 : "memory");
+    if (done)
+      return true;
+    if (clock64() - t0 > kTcWaitCycles)
+      return false;
+  }
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
+{
+  uint32_t r[16];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+               "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                 "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                 "=r"(r[15])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 16; j++)
+    v[j] = __uint_as_float(r[j]);
+}
+
+__global__ void __launch_bounds__(kTcThreads) k_mlp_forward_tc(const float *__restrict__ w,
+                                                               const float *__restrict__ x,
+                                                               float *__restrict__ prob, long long n)
+{
+  extern __shared__ __align__(1024) unsigned char tc_raw[];
+  TcSmem &S = *reinterpret_cast<TcSmem *>(tc_raw);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *a1 = reinterpret_cast<unsigned char *>(S.a1), *a2 = reinterpret_cast<unsigned char *>(S.a2);
+  unsigned char *b1 = reinterpret_cast<unsigned char *>(S.b1), *b2 = reinterpret_cast<unsigned char *>(S.b2);
+  for (int i = tid; i < kHid * 16; i += kTcThreads)
+  {
+    const int nn = i >> 4, k = i & 15;
+    *reinterpret_cast<__nv_bfloat16 *>(b1 + kmajor_off(nn, k, 16)) =
+      __float2bfloat16_rn(k < kIn ? w[kW1 + k * kHid + nn] : 0.f);
+  }
+  for (int i = tid; i < kHid * kHid; i += kTcThreads)
+  {
+    const int nn = i >> 6, k = i & 63;
+    *reinterpret_cast<__nv_bfloat16 *>(b2 + kmajor_off(nn, k, kHid)) = __float2bfloat16_rn(w[kW2 + k * kHid + nn]);
+  }
+  for (int i = tid; i < kHid; i += kTcThreads)
+  {
+    S.bias1[i] = w[kB1 + i];
+    S.bias2[i] = w[kB2 + i];
+    S.w3[i] = __bfloat162float(__float2bfloat16_rn(w[kW3 + i]));
+  }
+  if (tid == 0)
+    S.b3 = w[kB3];
+  // features 8..15 of layer 1's A are zero padding for every tile
+  *reinterpret_cast<uint4 *>(a1 + kmajor_off(tid, 8, 16)) = make_uint4(0u, 0u, 0u, 0u);
+  const uint32_t mbar = smem_u32(&S.mbar);
+  if (tid == 0)
+  {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0)
+  {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_base)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem_base;
+  const uint32_t my_lane = tmem + ((uint32_t)(warp * 32) << 16); // this warp's 32 TMEM lanes
+  const uint64_t da1 = smem_desc(smem_u32(a1), 128, 16 * 16), db1 = smem_desc(smem_u32(b1), 128, 16 * 16);
+  const uint32_t sa2 = smem_u32(a2), sb2 = smem_u32(b2);
+  const long long tiles = (n + kTcRows - 1) / kTcRows;
+  uint32_t parity = 0;
+  bool ok = true;
+  long long t = blockIdx.x;
+  // this thread's row of a tile (zero past the end)
+  auto load_row = [&](long long tile, float (&f)[kIn]) {
+    const long long row = tile * kTcRows + tid;
+#pragma unroll
+    for (int q = 0; q < kIn; q++)
+      f[q] = (tile < tiles && row < n) ? __ldg(x + row * kIn + q) : 0.f;
+  };
+  float f[kIn];
+  load_row(t, f);
+  for (; t < tiles; t += gridDim.x)
+  {
+    const long long row = t * kTcRows + tid;
+    *reinterpret_cast<uint4 *>(a1 + kmajor_off(tid, 0, 16)) =
+      make_uint4(pack_bf16(f[0], f[1]), pack_bf16(f[2], f[3]), pack_bf16(f[4], f[5]), 0u);
+    fence_async_smem();
+    __syncthreads();
+    if (tid == 0)
     {
-      if (row0 + g < n)
-        prob[row0 + g] = 1.f / (1.f + __expf(-T.logit_g));
-      if (row0 + g + 8 < n)
-        prob[row0 + g + 8] = 1.f / (1.f + __expf(-T.logit_g8));
+      tc_fence_after();
+      tc_mma(tmem, da1, db1, 0u);
+      tc_commit(mbar);
     }
+    load_row(t + gridDim.x, f); // the next tile's features load while the tensor core works
+    ok = tc_wait(mbar, parity);
+    parity ^= 1u;
+    if (!ok)
+      break;
+    tc_fence_after();
+    // layer 1 epilogue: bias, ReLU, BF16 -> layer 2's A (row tid, 8 columns per 16-byte store)
+#pragma unroll
+    for (int c0 = 0; c0 < kHid; c0 += 16)
+    {
+      float v[16];
+      tc_ld16(my_lane + (uint32_t)c0, v);
+      uint32_t pk[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        pk[j] = pack_bf16(fmaxf(v[2 * j] + S.bias1[c0 + 2 * j], 0.f), fmaxf(v[2 * j + 1] + S.bias1[c0 + 2 * j + 1], 0.f));
+      *reinterpret_cast<uint4 *>(a2 + kmajor_off(tid, c0, kHid)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      *reinterpret_cast<uint4 *>(a2 + kmajor_off(tid, c0 + 8, kHid)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0)
+    {
+      tc_fence_after();
+#pragma unroll
+      for (int kb = 0; kb < kHid / 16; kb++) // K steps of 16: two core matrices, 256 bytes
+        tc_mma(tmem + (uint32_t)kHid, smem_desc(sa2 + 256u * kb, 128, kHid * 16),
+               smem_desc(sb2 + 256u * kb, 128, kHid * 16), kb > 0 ? 1u : 0u);
+      tc_commit(mbar);
+    }
+    ok = tc_wait(mbar, parity);
+    parity ^= 1u;
+    if (!ok)
+      break;
+    tc_fence_after();
+    // layer 2 epilogue and the output neuron
+    float logit = 0.f;
+#pragma unroll
+    for (int c0 = 0; c0 < kHid; c0 += 16)
+    {
+      float v[16];
+      tc_ld16(my_lane + (uint32_t)(kHid + c0), v);
+#pragma unroll
+      for (int j = 0; j < 16; j++)
+      {
+        const float h = __bfloat162float(__float2bfloat16_rn(fmaxf(v[j] + S.bias2[c0 + j], 0.f)));
+        logit = fmaf(h, S.w3[c0 + j], logit);
+      }
+    }
+    if (row < n)
+      prob[row] = 1.f / (1.f + __expf(-(logit + S.b3)));
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (!ok)
+  { // gave up on a tile: NaN for it and the CTA's remaining tiles; let the
+    // tensor core finish (bounded) before the memory is freed
+    for (long long u = t; u < tiles; u += gridDim.x)
+    {
+      const long long row = u * kTcRows + tid;
+      if (row < n)
+        prob[row] = __int_as_float(0x7fc00000);
+    }
+    tc_wait(mbar, parity ^ 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0)
+  {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
   }
 }
 
@@ -429,7 +678,16 @@ extern "C" int hbtg_mlp_forward(const float *weights, const float *features, flo
     return HBTG_ERR_INVALID;
   if (n == 0)
     return HBTG_OK;
-  k_mlp_forward<<<grid_for_rows(n, 128), 256, 0, static_cast<cudaStream_t>(stream)>>>(weights, features, prob, n);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return HBTG_ERR_CUDA;
+  if (cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemBytes) !=
+      cudaSuccess)
+    return HBTG_ERR_CUDA;
+  const long long tiles = (n + kTcRows - 1) / kTcRows;
+  const int grid = (int)std::min<long long>(tiles, 4LL * sms); // persistent: 4 CTAs per SM (TMEM: 4 x 128 columns)
+  k_mlp_forward_tc<<<grid, kTcThreads, kTcSmemBytes, static_cast<cudaStream_t>(stream)>>>(weights, features, prob,
+                                                                                        n);
   return cudaGetLastError() == cudaSuccess ? HBTG_OK : HBTG_ERR_CUDA;
 }
 

@@ -394,11 +394,13 @@ int hbtg_features_device(hbtg_handle *handle, const hbtg_params *params, const h
  * iteration). */
 int hbtg_trace_labels_device(hbtg_handle *handle, uint8_t *labels, int which, void *cuda_stream);
 
-/* The proposer network on the tensor cores (BF16 operands, FP32
- * accumulation).  Weights (FP32, device): W1[6][64], b1[64], W2[64][64],
- * b2[64], w3[64], b3 (matrices in x out);
+/* The proposer network on the tensor cores (tcgen05.mma, BF16 operands,
+ * FP32 accumulators in tensor memory).  Weights (FP32, device): W1[6][64],
+ * b1[64], W2[64][64], b2[64], w3[64], b3 (matrices in x out);
  * p = sigmoid(w3 . relu(W2^T relu(W1^T x + b1) + b2) + b3).
- * prob[i] for features[6i..6i+5]; all device arrays. */
+ * prob[i] for features[6i..6i+5]; all device arrays.  Should the tensor core
+ * not signal completion within about a second, the rows it had not finished
+ * get NaN (neither trusted nor left out by the learned call). */
 int hbtg_mlp_forward(const float *weights, const float *features, float *prob, int64_t n, void *cuda_stream);
 
 /* Gradient of sum_i w_i BCE(p_i, y_i) over n rows (sample_weights may be
