@@ -255,15 +255,16 @@ struct IterationDriver
     if (chunk_total <= 0)
       return;
     unsigned grid = grid_for(chunk_total, kWalkWarps);
+    const int nranges = std::max(1, std::min(sm_count, chunk_total)); // every range holds a chunk
     if (D.walk_ctr)
     { // one resident wave over per-SM chunk ranges
-      mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)sm_count, st));
+      mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)nranges, st));
       grid = std::min<unsigned>(grid, (unsigned)sm_count * (unsigned)walk_blocks_per_sm);
     }
     if (K.count_interactions)
-      k_walk<true><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, sm_count);
+      k_walk<true><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, nranges);
     else
-      k_walk<false><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, sm_count);
+      k_walk<false><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, nranges);
     launches++;
     walk_launches++;
     check();
