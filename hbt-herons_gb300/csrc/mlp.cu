@@ -289,9 +289,13 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
     v[j] = __uint_as_float(r[j]);
 }
 
-__global__ void __launch_bounds__(kTcThreads) k_mlp_forward_tc(const float *__restrict__ w,
-                                                               const float *__restrict__ x,
-                                                               float *__restrict__ prob, long long n)
+// Propose = false: prob[row] = p.  Propose = true (the learned call): the
+// proposal byte instead, prop[row] = 1 (trusted, p >= trust), 2 (left out,
+// p < leave_out) or 0 (uncertain; also for NaN).
+template <bool Propose>
+__global__ void __launch_bounds__(kTcThreads)
+  k_mlp_forward_tc(const float *__restrict__ w, const float *__restrict__ x, float *__restrict__ prob,
+                   uint8_t *__restrict__ prop, float trust, float leave_out, long long n)
 {
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   TcSmem &S = *reinterpret_cast<TcSmem *>(tc_raw);
@@ -417,7 +421,13 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_forward_tc(const float *__re
       }
     }
     if (row < n)
-      prob[row] = 1.f / (1.f + __expf(-(logit + S.b3)));
+    {
+      const float p = 1.f / (1.f + __expf(-(logit + S.b3)));
+      if (Propose)
+        prop[row] = p >= trust ? 1 : (p < leave_out ? 2 : 0);
+      else
+        prob[row] = p;
+    }
     tc_fence_before();
     __syncthreads();
   }
@@ -428,7 +438,12 @@ __global__ void __launch_bounds__(kTcThreads) k_mlp_forward_tc(const float *__re
     {
       const long long row = u * kTcRows + tid;
       if (row < n)
-        prob[row] = __int_as_float(0x7fc00000);
+      {
+        if (Propose)
+          prop[row] = 0;
+        else
+          prob[row] = __int_as_float(0x7fc00000);
+      }
     }
     tc_wait(mbar, parity ^ 1u);
   }
@@ -670,7 +685,34 @@ inline int grid_for_rows(long long n, int rows_per_block)
   return (int)(b < 1 ? 1 : (b > 4096 ? 4096 : b));
 }
 
+template <bool Propose>
+int launch_forward_tc(const float *w, const float *x, float *prob, uint8_t *prop, float trust, float leave_out,
+                      long long n, cudaStream_t st)
+{
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return HBTG_ERR_CUDA;
+  if (cudaFuncSetAttribute(k_mlp_forward_tc<Propose>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)kTcSmemBytes) != cudaSuccess)
+    return HBTG_ERR_CUDA;
+  const long long tiles = (n + kTcRows - 1) / kTcRows;
+  const int grid = (int)std::min<long long>(tiles, 4LL * sms); // persistent: 4 CTAs per SM (TMEM: 4 x 128 columns)
+  k_mlp_forward_tc<Propose><<<grid, kTcThreads, kTcSmemBytes, st>>>(w, x, prob, prop, trust, leave_out, n);
+  return cudaGetLastError() == cudaSuccess ? HBTG_OK : HBTG_ERR_CUDA;
+}
+
 } // namespace
+
+// The learned call's proposal straight from the network (not exported: the
+// library's own units call it).
+__attribute__((visibility("hidden"))) int hbtg_mlp_propose(const float *weights, const float *features,
+                                                            uint8_t *prop, float trust, float leave_out, int64_t n,
+                                                            cudaStream_t stream)
+{
+  if (n <= 0)
+    return HBTG_OK;
+  return launch_forward_tc<true>(weights, features, nullptr, prop, trust, leave_out, n, stream);
+}
 
 extern "C" int hbtg_mlp_forward(const float *weights, const float *features, float *prob, int64_t n, void *stream)
 {
@@ -678,17 +720,7 @@ extern "C" int hbtg_mlp_forward(const float *weights, const float *features, flo
     return HBTG_ERR_INVALID;
   if (n == 0)
     return HBTG_OK;
-  int dev = 0, sms = 152;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return HBTG_ERR_CUDA;
-  if (cudaFuncSetAttribute(k_mlp_forward_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemBytes) !=
-      cudaSuccess)
-    return HBTG_ERR_CUDA;
-  const long long tiles = (n + kTcRows - 1) / kTcRows;
-  const int grid = (int)std::min<long long>(tiles, 4LL * sms); // persistent: 4 CTAs per SM (TMEM: 4 x 128 columns)
-  k_mlp_forward_tc<<<grid, kTcThreads, kTcSmemBytes, static_cast<cudaStream_t>(stream)>>>(weights, features, prob,
-                                                                                        n);
-  return cudaGetLastError() == cudaSuccess ? HBTG_OK : HBTG_ERR_CUDA;
+  return launch_forward_tc<false>(weights, features, prob, nullptr, 0.f, 0.f, n, static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int hbtg_mlp_backward(const float *weights, const float *features, const float *labels,

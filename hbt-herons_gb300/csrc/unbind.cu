@@ -15,6 +15,10 @@
 #include <vector>
 
 #include "../../include/hbt_unbind_gpu.h"
+
+// csrc/mlp.cu: the proposer's inference writing the proposal byte directly
+int hbtg_mlp_propose(const float *weights, const float *features, uint8_t *prop, float trust, float leave_out,
+                     int64_t n, cudaStream_t stream);
 #include "common.cuh"
 #include "driver.cuh"
 #include "props.cuh"
@@ -135,7 +139,7 @@ enum Slot
   S_SUBI, S_SUBF, S_BB, S_ROOT, S_KEYP, S_COM,
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F,
   S_NODES, S_TABLE, S_SCRATCH, S_CELLS, S_LVL, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
-  S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROB, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
+  S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
   S_POTI, S_WCTR, S_FRAMEW,
   S_PR_OFF, S_PR_CNT, S_PR_FIN, S_PR_RR, S_PR_MM, S_PR_K, S_PR_V, S_PR_KA, S_PR_VA, S_PR_MC, S_PR_VK, S_PR_SO,
   S_PR_SH, S_PR_SCR, S_PR_POS, S_PR_MASS, S_PR_ORD, S_PR_NB, S_PR_MBND, S_PR_MBP, S_PR_OUTF, S_PR_OUTI, S_PR_OUTL,
@@ -507,15 +511,14 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
         H->stats.kernel_launches = R.launches;
         return HBTG_OK;
       }
-      float *prob = P.get<float>(S_PROB, n1);
       uint8_t *prop = P.get<uint8_t>(S_PROP, n1);
       if (N > 0)
-      {
-        const int mrc = hbtg_mlp_forward(P.get<float>(S_MODEL, HBTG_MLP_PARAMS), W.feat, prob, N, st);
+      { // the network's proposal (trusted / uncertain / left out) per particle
+        const int mrc = hbtg_mlp_propose(P.get<float>(S_MODEL, HBTG_MLP_PARAMS), W.feat, prop, H->threshold,
+                                         H->exclude_below, N, st);
         if (mrc != HBTG_OK)
           return mrc;
-        k_propose<<<blocks_for(N, 256), 256, 0, st>>>(prob, H->threshold, H->exclude_below, prop, N);
-        R.launches += 2;
+        R.launches++;
         R.check();
       }
       W.prop = prop;

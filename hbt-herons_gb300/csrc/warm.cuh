@@ -370,18 +370,6 @@ __global__ void k_features(DevState D, KParams K, WarmBufs W)
   }
 }
 
-// Proposal from the network's probabilities: trusted at or above `trust`,
-// left out below `leave_out`, tested in between.
-__global__ void k_propose(const float *__restrict__ prob, float trust, float leave_out, uint8_t *__restrict__ prop,
-                          long long n)
-{
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-  {
-    const float p = prob[i];
-    prop[i] = p >= trust ? 1 : (p < leave_out ? 2 : 0);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // Warm start from a proposal
 // ---------------------------------------------------------------------------
@@ -447,7 +435,10 @@ __global__ void k_warm_setup(DevState D, KParams K, WarmBufs W)
   D.wrap[s] = K.periodic && (len > (double)K.half);
 }
 
-__global__ void k_warm_scatter(DevState D)
+// join_uncertain (no first test): the uncertain particles are set members from
+// the start (bnd), though they are left out of the first frame (positions
+// past nbound); the frame kernels read positions, not bnd.
+__global__ void k_warm_scatter(DevState D, int join_uncertain)
 {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= D.N)
@@ -460,7 +451,7 @@ __global__ void k_warm_scatter(DevState D)
   const int nt = D.nbound[s], nu = D.ntest[s];
   const int pos = D.flags[i] ? rt : (D.cnt[i] ? nt + ru : nt + nu + (int)(i - off) - rt - ru);
   D.ord[off + pos] = (int)i;
-  D.bnd[i] = (uint8_t)D.flags[i];
+  D.bnd[i] = (uint8_t)(D.flags[i] | (join_uncertain ? D.cnt[i] : 0));
 }
 
 // Frame and mass of the flagged subhaloes from the k_com sums (no convergence
@@ -623,22 +614,6 @@ __global__ void k_first_apply(DevState D, KParams K)
     D.warm[s] = 4;
   else
     D.flag_s[s] = 1;
-}
-
-// Without the first test: the uncertain particles (positions [nbound,
-// nbound + ntest) of a warm subhalo, after the trusted ones) join the set.
-// Runs after the trusted particles' frame is computed.
-__global__ void k_untested_bnd(DevState D)
-{
-  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= D.N)
-    return;
-  const int s = D.seg_of[g];
-  if (D.warm[s] != 1)
-    return;
-  const long long k = g - D.off[s];
-  if (k >= D.nbound[s] && k < (long long)D.nbound[s] + D.ntest[s])
-    D.bnd[D.ord[g]] = 1;
 }
 
 // The set after the proposal without the first test: trusted plus uncertain.
@@ -861,7 +836,7 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
   R.launches++;
   if (D.N > 0)
   {
-    k_warm_scatter<<<grid_for(D.N, 256), 256, 0, st>>>(D);
+    k_warm_scatter<<<grid_for(D.N, 256), 256, 0, st>>>(D, W.first_test ? 0 : 1);
     R.launches++;
   }
   R.check();
@@ -875,28 +850,27 @@ void warm_run(IterationDriver<Mem> &R, const WarmBufs &W, WarmCounters &C, bool 
     // the warm subhaloes), then the uncertain ones join the set
     R.mem.mark(6); // the proposal ends here
     flagged_frames(R);
-    if (D.N > 0)
-    {
-      k_untested_bnd<<<grid_for(D.N, 256), 256, 0, st>>>(D);
-      R.launches++;
-    }
     k_untested_apply<<<sb, 256, 0, st>>>(D, R.K);
     R.launches++;
     R.check();
   }
-  {
-    std::vector<int> nex(S);
+  long long restarts = 0;
+  { // left-out counts and the subhaloes marked for a cold restart, in one host read
+    std::vector<int> nex(S), wm(S);
     R.mem.check(cudaMemcpyAsync(nex.data(), D.nexcl, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
+    R.mem.check(cudaMemcpyAsync(wm.data(), D.warm, sizeof(int) * S, cudaMemcpyDeviceToHost, st));
     R.mem.check(cudaStreamSynchronize(st));
     R.host_syncs++;
     for (int v : nex)
       C.excluded += v;
+    for (int v : wm)
+      restarts += (v == 4);
   }
   if (W.first_test)
     flagged_frames(R); // the frame of the set the second iteration evaluates
   k_warm_fallback<<<sb, 256, 0, st>>>(D); // subhaloes whose first iteration converges run cold
   R.launches++;
-  if (D.N > 0)
+  if (D.N > 0 && restarts > 0)
   {
     k_warm_fallback_particles<<<grid_for(D.N, 256), 256, 0, st>>>(D);
     R.launches++;
