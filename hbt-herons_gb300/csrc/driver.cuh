@@ -339,8 +339,8 @@ struct IterationDriver
         mem.mark(3);
         if (bound_total > 0)
         {
-          k_com<<<grid_for((bound_total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, K,
-                                                                                                     bound_total);
+          D.com_ipt = com_items_per_thread(bound_total); // k_control reads the partials with the same blocking
+          k_com<<<grid_for((bound_total + D.com_ipt - 1) / D.com_ipt, 256), 256, 0, st>>>(D, K, bound_total);
           launches++;
         }
         k_control<<<sb, 256, 0, st>>>(D, K);

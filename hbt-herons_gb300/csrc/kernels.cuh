@@ -98,6 +98,7 @@ struct DevState
   int *fb_list, *fb_count; // packed items whose key needs the exact double descent
   double *com;             // [7S] M, sum m dx, sum m v (epilogue: kinematics sums)
   double *com_part;        // [7 x blocks] per-block frame sums of single-subhalo k_com blocks
+  int com_ipt = 16;        // items per thread of the k_com launch whose sums k_control / k_frame_flagged read
   // packed arrays
   unsigned long long *key, *key_alt;
   uint32_t *val, *val_alt, *k32, *k32_alt, *perm, *perm_alt;
@@ -1350,6 +1351,18 @@ __device__ __forceinline__ void segmented_flush(double (&acc)[Q], int seg, doubl
 
 constexpr int kItemsPerThread = 16;
 
+// k_com takes kItemsPerThread consecutive items per thread over large bound
+// sets (bandwidth) and one item per thread over small ones (the late
+// iterations: a thread's items are a chain of dependent loads, so fewer per
+// thread means a shorter launch).
+constexpr long long kComSmall = 65536;
+__host__ __device__ inline int com_items_per_thread(long long total) { return total <= kComSmall ? 1 : kItemsPerThread; }
+// Per-block partials that k_com can write over n bound particles.
+__host__ __device__ inline long long com_part_blocks(long long n)
+{
+  return n / (256LL * kItemsPerThread) + kComSmall / 256 + 2;
+}
+
 // Kahan-compensated float accumulator.
 struct KahanF
 {
@@ -1371,7 +1384,8 @@ struct KahanF
 // double as the reference does.
 __global__ void k_com(DevState D, KParams K, int total)
 {
-  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * kItemsPerThread;
+  const int ipt = D.com_ipt;
+  const long long first = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * ipt;
   KahanF acc[7];
   double out[7] = {0., 0., 0., 0., 0., 0., 0.};
   int s = -1;
@@ -1389,7 +1403,7 @@ __global__ void k_com(DevState D, KParams K, int total)
   if (first < total)
   {
     s = s_first;
-    const int last = (int)min((long long)total, first + kItemsPerThread);
+    const int last = (int)min((long long)total, first + ipt);
     float4 o = D.pm[D.ord[D.off[s]]];
     for (int j = (int)first; j < last; j++)
     {
@@ -1429,8 +1443,8 @@ __global__ void k_com(DevState D, KParams K, int total)
   // partial instead of contending atomics; k_control adds those partials.
   __shared__ int s_seg_lo, s_seg_hi;
   __shared__ double s_part[7][8];
-  const long long b0 = (long long)blockIdx.x * blockDim.x * kItemsPerThread;
-  const long long b1 = min((long long)total, b0 + (long long)blockDim.x * kItemsPerThread);
+  const long long b0 = (long long)blockIdx.x * blockDim.x * ipt;
+  const long long b1 = min((long long)total, b0 + (long long)blockDim.x * ipt);
   if (threadIdx.x == 0)
   {
     s_seg_lo = find_segment<int>(D.fin_off, D.S, (int)b0);
@@ -1471,7 +1485,7 @@ __device__ void frame_from_sums(DevState &D, const KParams &K, int s)
     c[q] = D.com[7 * s + q];
   // add the partials of the k_com blocks lying entirely inside this subhalo
   // (same test as k_com: the block's item range [b0, b1) lies in [lo, hi))
-  const long long per_block = 256LL * kItemsPerThread;
+  const long long per_block = 256LL * D.com_ipt;
   const long long lo = D.fin_off[s], hi = D.fin_off[s + 1], total = D.fin_off[D.S];
   for (long long b = (lo + per_block - 1) / per_block; b * per_block < hi; b++)
   {

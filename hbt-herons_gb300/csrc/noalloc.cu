@@ -74,7 +74,7 @@ constexpr size_t kScratchBytes =
   al(sizeof(double) * 4 * kS1) +             // root cubes
   al(sizeof(float) * 12 * kS1) +             // fast key-descent constants
   al(sizeof(double) * 7 * kS1) +             // frame sums
-  al(sizeof(double) * 7 * (kN1 / 4096 + 2)) + // per-block frame sums
+  al(sizeof(double) * 7 * (kN1 / 4096 + kComSmall / 256 + 2)) + // per-block frame sums (com_part_blocks)
   2 * al(sizeof(unsigned long long) * kN1) + // key, key_alt
   6 * al(sizeof(uint32_t) * kN1) +           // val, val_alt, k32, k32_alt, perm, perm_alt
   al(sizeof(int) * kN1) + al(sizeof(int)) +  // key fallback list and its count
@@ -292,7 +292,7 @@ int noalloc_call(const hbtg_params *p, hbtg_batch *b, cudaStream_t st)
   D.root = c.take<double>(4 * kS1);
   D.keyp = c.take<float>(12 * kS1);
   D.com = c.take<double>(7 * kS1);
-  D.com_part = c.take<double>(7 * (kN1 / (256 * kItemsPerThread) + 2));
+  D.com_part = c.take<double>(7 * (size_t)com_part_blocks((long long)kN1));
   D.key = c.take<unsigned long long>(kN1);
   D.key_alt = c.take<unsigned long long>(kN1);
   D.val = c.take<uint32_t>(kN1);

@@ -444,7 +444,7 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   D.root = P.get<double>(S_ROOT, (size_t)S * 4);
   D.keyp = P.get<float>(S_KEYP, (size_t)S * 12);
   D.com = P.get<double>(S_COM, (size_t)S * 7);
-  D.com_part = P.get<double>(S_COMP, 7 * ((size_t)N / (256 * kItemsPerThread) + 2));
+  D.com_part = P.get<double>(S_COMP, 7 * (size_t)com_part_blocks(N));
   D.key = P.get<unsigned long long>(S_KEY, n1);
   D.key_alt = P.get<unsigned long long>(S_KEYA, n1);
   D.val = P.get<uint32_t>(S_VAL, n1);

@@ -750,7 +750,8 @@ void flagged_frames(IterationDriver<Mem> &R)
   const int total = R.scan_counts(D.fin_cnt, D.fin_off, D.S);
   if (total > 0)
   {
-    k_com<<<grid_for((total + kItemsPerThread - 1) / kItemsPerThread, 256), 256, 0, st>>>(D, R.K, total);
+    D.com_ipt = com_items_per_thread(total); // k_frame_flagged reads the partials with the same blocking
+    k_com<<<grid_for((total + D.com_ipt - 1) / D.com_ipt, 256), 256, 0, st>>>(D, R.K, total);
     R.launches++;
   }
   k_frame_flagged<<<grid_for(D.S, 256), 256, 0, st>>>(D, R.K, 1);
