@@ -643,18 +643,26 @@ def _reset_frames(buf, hin):
     buf.out.most_bound_id[...] = hin.most_bound_id
 
 
+def _reduce_device():
+    """The device the process group reduces on: the GPU for NCCL, the host for gloo."""
+    import torch.distributed as dist
+    return "cuda" if dist.get_backend() == "nccl" else "cpu"
+
+
 def _sum_over_ranks(x):
+    """Sum of x over the ranks (weak scaling: every rank's bound particles)."""
     import torch
     import torch.distributed as dist
-    t = torch.tensor([float(x)], device="cuda", dtype=torch.float64)
+    t = torch.tensor([float(x)], device=_reduce_device(), dtype=torch.float64)
     dist.all_reduce(t)
     return float(t.item())
 
 
 def _max_over_ranks(x):
+    """Max of x over the ranks (the slowest rank's time)."""
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda")
+    t = torch.tensor([float(x)], device=_reduce_device(), dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 

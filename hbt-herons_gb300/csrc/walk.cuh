@@ -728,14 +728,14 @@ __global__ void __launch_bounds__(32 * kWalkWarps)
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
     auto range_lo = [&](int q) { return (int)((long long)q * total_chunks / nranges); };
     int r = (int)(smid % (unsigned)nranges);
+    int lo = range_lo(r), size = range_lo(r + 1) - lo; // recomputed only when the warp changes range
     for (;;)
     {
       int got = 0;
       if (lane == 0)
         got = (int)atomicAdd(&D.walk_ctr[r], 1u);
       got = __shfl_sync(0xffffffffu, got, 0);
-      const int lo = range_lo(r), hi = range_lo(r + 1);
-      if (got < hi - lo)
+      if (got < size)
       {
         walk_chunk<Count>(D, K, lo + got, lane, sh, w, cnt);
         continue;
@@ -752,6 +752,8 @@ __global__ void __launch_bounds__(32 * kWalkWarps)
       if (next < 0)
         break;
       r = next;
+      lo = range_lo(r);
+      size = range_lo(r + 1) - lo;
     }
   }
   else
