@@ -255,7 +255,10 @@ struct IterationDriver
     if (chunk_total <= 0)
       return;
     unsigned grid = grid_for(chunk_total, kWalkWarps);
-    const int nranges = std::max(1, std::min(sm_count, chunk_total)); // every range holds a chunk
+    // ranges of `per` chunks, at most one per SM, none empty (a warp whose range is
+    // done tries the following ranges one atomic each, so empty ranges cost time)
+    const int per = (chunk_total + std::min(sm_count, chunk_total) - 1) / std::min(sm_count, chunk_total);
+    const int nranges = (chunk_total + per - 1) / per;
     if (D.walk_ctr)
     { // one resident wave over per-SM chunk ranges
       mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)nranges, st));

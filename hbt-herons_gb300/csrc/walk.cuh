@@ -703,14 +703,11 @@ __device__ __forceinline__ void walk_chunk(const DevState &D, const KParams &K, 
 }
 
 // With walk counters, the chunks (key order) are split into `nranges`
-// contiguous ranges of balanced size (every range holds at least one chunk:
-// the host passes nranges <= total_chunks), one per SM: the warps resident on
-// an SM take the chunks of their own range in order, so they walk
-// neighbouring targets and share the tree slots in L1.  A warp whose range is
-// used up reads every range's counter at once (32 per load round, from L2)
-// and moves to the first range after its own that still has chunks; it stops
-// when none has.  A counter only grows, so every failed claim retires a
-// range for good and the search ends.  Without counters, a grid-stride loop.
+// contiguous ranges of `per` chunks, one per SM (the host picks nranges so
+// that every range holds a chunk): the warps resident on an SM take the
+// chunks of their own range in order, so they walk neighbouring targets and
+// share the tree slots in L1; a warp whose range is used up moves on to the
+// next ranges (each tried once).  Without counters, a grid-stride loop.
 template <bool Count>
 #ifdef HBTG_WALK_MIN_BLOCKS
 __global__ void __launch_bounds__(32 * kWalkWarps, HBTG_WALK_MIN_BLOCKS)
@@ -726,34 +723,22 @@ __global__ void __launch_bounds__(32 * kWalkWarps)
   {
     unsigned smid;
     asm volatile("mov.u32 %0, %%smid;" : "=r"(smid));
-    auto range_lo = [&](int q) { return (int)((long long)q * total_chunks / nranges); };
+    const int per = (total_chunks + nranges - 1) / nranges;
     int r = (int)(smid % (unsigned)nranges);
-    int lo = range_lo(r), size = range_lo(r + 1) - lo; // recomputed only when the warp changes range
-    for (;;)
+    for (int tries = 0; tries < nranges;)
     {
       int got = 0;
       if (lane == 0)
         got = (int)atomicAdd(&D.walk_ctr[r], 1u);
       got = __shfl_sync(0xffffffffu, got, 0);
-      if (got < size)
+      const long long c = (long long)r * per + got;
+      if (got >= per || c >= total_chunks)
       {
-        walk_chunk<Count>(D, K, lo + got, lane, sh, w, cnt);
+        r = (r + 1 == nranges) ? 0 : r + 1;
+        tries++;
         continue;
       }
-      int next = -1;
-      for (int base = 1; base <= nranges && next < 0; base += kWarp)
-      {
-        const int q = (r + base + lane) % nranges;
-        const bool left = base + lane <= nranges && (int)__ldcg(&D.walk_ctr[q]) < range_lo(q + 1) - range_lo(q);
-        const unsigned b = __ballot_sync(0xffffffffu, left);
-        if (b)
-          next = (r + base + __ffs(b) - 1) % nranges;
-      }
-      if (next < 0)
-        break;
-      r = next;
-      lo = range_lo(r);
-      size = range_lo(r + 1) - lo;
+      walk_chunk<Count>(D, K, (int)c, lane, sh, w, cnt);
     }
   }
   else
