@@ -190,10 +190,12 @@ __device__ __forceinline__ void forward_tile(const SmemWeights &S, const float *
 // follow each other along K (leading byte offset 128), and the 8-row groups
 // are K * 16 bytes apart (stride byte offset).
 //
-// Every wait on the mbarrier is bounded (about one second of clock); a CTA
-// that gives up writes NaN for the rows it has not finished (a NaN
-// probability is neither trusted nor left out, so the exact iteration decides
-// those particles), frees its tensor memory and returns.
+// Every wait on the mbarrier is bounded (about one second of clock), and the
+// CTA decides together (a block-wide AND) whether to go on; a CTA that gives
+// up writes NaN for the rows it has not finished (a NaN probability is neither
+// trusted nor left out, so the exact iteration decides those particles),
+// waits once more (bounded) for the tensor core, frees its tensor memory and
+// returns.
 // ---------------------------------------------------------------------------
 constexpr int kTcRows = 128;
 constexpr int kTcThreads = 128;
@@ -371,7 +373,7 @@ __global__ void __launch_bounds__(kTcThreads)
       tc_commit(mbar);
     }
     load_row(t + gridDim.x, f); // the next tile's features load while the tensor core works
-    ok = tc_wait(mbar, parity);
+    ok = __syncthreads_and(tc_wait(mbar, parity)) != 0; // the whole block gives up together
     parity ^= 1u;
     if (!ok)
       break;
@@ -401,7 +403,7 @@ __global__ void __launch_bounds__(kTcThreads)
                smem_desc(sb2 + 256u * kb, 128, kHid * 16), kb > 0 ? 1u : 0u);
       tc_commit(mbar);
     }
-    ok = tc_wait(mbar, parity);
+    ok = __syncthreads_and(tc_wait(mbar, parity)) != 0; // the whole block gives up together
     parity ^= 1u;
     if (!ok)
       break;
