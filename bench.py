@@ -440,6 +440,7 @@ def bench_gpu(args):
     flops_per_launch = cw["interactions"] * FLOPS_PER_INTERACTION / max(1, cw["walk_launches"])
     achieved = flops_per_launch / (walk_ms_per_launch * 1e-3) / 1e12
     traffic = _walk_traffic(cw)
+    issue = _walk_issue()
 
     cpu = parity = None
     if rank == 0 and not args.skip_cpu:
@@ -510,6 +511,9 @@ def bench_gpu(args):
                          "peak_source": "FP32 FMA throughput measured in-process (hbtg_measure_fp32_peak)",
                          "flops_per_launch": flops_per_launch, "ms_per_launch": walk_ms_per_launch,
                          "blocks_per_sm": warm["last"].get("walk_blocks_per_sm"),
+                         "issue_active_ncu": issue,
+                         "bound_note": "the walk is issue-bound (instruction issue slots, not the FP32 pipe): "
+                                       "issue_active_ncu is its ncu issue-slot utilisation",
                          "walk_share_of_step": warm["ms_walk"] / max(warm["ms"], 1e-9)},
             "cpu_baseline": cpu,
             "parity": parity,
@@ -665,6 +669,15 @@ def _max_over_ranks(x):
     t = torch.tensor([float(x)], device=_reduce_device(), dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _walk_issue():
+    """The walk's issue-slot utilisation (%) from the committed ncu summary, or None."""
+    path = os.path.join(HERE, "profiles", "k_walk_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f).get("issue_active_pct")
 
 
 def _walk_traffic(counted):
