@@ -374,3 +374,34 @@ def test_model_file_keeps_first_test(tmp_path):
     m.save(p)
     m2 = learned.Model.load(p)
     assert m2.first_test == 0 and m2.exclude_below == pytest.approx(1e-3)
+
+
+@pytest.mark.gpu
+def test_learned_proposal_matches_network_thresholds(unbinder):
+    """The learned call takes its proposal straight from the tensor-core
+    inference (proposal bytes, no probability array): the particles it leaves
+    out are exactly those to which hbtg_mlp_forward gives a probability below
+    exclude_below, in exactly the subhaloes that start warm (large enough, and
+    their kept set below BoundMassPrecision of their particles)."""
+    import torch
+    from hbtg.gpu import DeviceBatch
+    if not os.path.exists(learned.MODEL_FILE):
+        pytest.skip("no trained model shipped")
+    params = _params()
+    inp = synthetic.stripped(n_sub=400, seed=31, nmax=50_000)
+    m = learned.Model.load()
+    assert m.first_test == 0
+    db = DeviceBatch(inp)
+    db.reset_inout()
+    feats = unbinder.features_device(params, db)  # the learned call's own features, in the input frame
+    prob = learned.mlp_forward(torch.from_numpy(m.weights).cuda(), feats).cpu().numpy()
+    m.install(unbinder)
+    db.reset_inout()
+    unbinder.unbind_learned_device(params, db)
+    st = unbinder.stats()
+    sizes = np.diff(inp.offsets)
+    seg = np.repeat(np.arange(inp.n_sub), sizes)
+    kept = np.bincount(seg, weights=~(prob < np.float32(m.exclude_below)), minlength=inp.n_sub).astype(np.int64)
+    warm = (sizes >= m.min_particles) & (kept.astype(np.float32) < sizes.astype(np.float32) * np.float32(0.995))
+    assert st["warm_subhaloes"] == int(warm.sum()) > 0
+    assert st["excluded"] == int(np.sum((sizes - kept)[warm]))
