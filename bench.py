@@ -709,6 +709,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-literal", action="store_true", help="skip the literal 20,000-subhalo timing")
     ap.add_argument("--skip-side", action="store_true", help="skip the hydro and stripped side workloads")
+    ap.add_argument("--autotune", action="store_true",
+                    help="only run the launch-settings autotuner (hbtg_autotune) on the workload and print its table")
     args = ap.parse_args()
     if args.total is None:
         args.total = {"stripped": 20000, "hydro": 4e6}.get(args.workload, 5e7)
@@ -717,7 +719,25 @@ def main():
     args.ref_sample = int(args.ref_sample)
     if args.impl == "reference":
         return bench_reference(args)
+    if args.autotune:
+        return autotune_table(args)
     return bench_gpu(args)
+
+
+def autotune_table(args):
+    """hbtg_autotune on the workload (plain path, device-resident inputs): one
+    JSON line with every candidate's time and the setting it keeps."""
+    import torch
+    from hbtg.gpu import DeviceBatch, Unbinder
+    inp, prm = workload(args.total, args.seed, args.workload)
+    u = Unbinder(0)
+    db = DeviceBatch(inp, device="cuda:0")
+    db.reset_inout()
+    report = u.autotune(prm, db.c, torch.cuda.current_stream().cuda_stream)
+    print(json.dumps({"workload": WORKLOADS[args.workload] % args.total, "particles": int(inp.n_particles),
+                      "candidates": report, "kept": u.tuning()}))
+    u.close()
+    return 0
 
 
 if __name__ == "__main__":

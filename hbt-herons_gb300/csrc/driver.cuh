@@ -47,6 +47,10 @@ struct IterationDriver
   int seg_bits = 0;
   int sm_count = 152;
   int walk_blocks_per_sm = 1; // resident k_walk blocks per SM (occupancy)
+  // launch settings that leave every result unchanged (hbtg_tuning, hbtg_autotune)
+  int block_sort_max = kRadixBlockMax; // largest sort done by one block
+  int walk_ranged_min = 0;             // walks of fewer chunks use a grid-stride loop instead of per-SM ranges
+  int moments_blocks_per_sm = 8;       // grid cap of the per-level multipole passes
   int64_t launches = 0;
   int64_t walk_launches = 0;
   int64_t tree_nodes = 0;
@@ -135,7 +139,8 @@ struct IterationDriver
   {
     int *table = mem.radix_table(total), *scr = mem.radix_scan_scratch(total);
     const bool flip =
-      radix_sort_pairs<uint32_t>(D.k32, D.val, D.k32_alt, D.val_alt, total, 0, 32, table, scr, st, &launches);
+      radix_sort_pairs<uint32_t>(D.k32, D.val, D.k32_alt, D.val_alt, total, 0, 32, table, scr, st, &launches,
+                                 block_sort_max);
     uint32_t *v = flip ? D.val_alt : D.val;
     uint32_t *v_other = flip ? D.val : D.val_alt;
     if (S > 1 && seg_bits > 0)
@@ -143,7 +148,8 @@ struct IterationDriver
       k_segkeys<<<grid_for(total, 256), 256, 0, st>>>(v, D.seg_of, D.k32, total);
       launches++;
       const bool f2 =
-        radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scr, st, &launches);
+        radix_sort_pairs<uint32_t>(D.k32, v, D.k32_alt, v_other, total, 0, seg_bits, table, scr, st, &launches,
+                                   block_sort_max);
       v = f2 ? v_other : v;
     }
     check();
@@ -157,7 +163,7 @@ struct IterationDriver
     int *table = mem.radix_table(total), *scr = mem.radix_scan_scratch(total);
     const bool flip =
       radix_sort_pairs<unsigned long long>(D.key, D.val, D.key_alt, D.val_alt, total, 0, 63, table, scr, st,
-                                           &launches);
+                                           &launches, block_sort_max);
     if (flip)
     {
       std::swap(D.key, D.key_alt);
@@ -168,7 +174,7 @@ struct IterationDriver
       k_segkeys_iota<<<grid_for(total, 256), 256, 0, st>>>(D.val, D.seg_of, D.k32, D.perm, total);
       launches++;
       const bool f2 = radix_sort_pairs<uint32_t>(D.k32, D.perm, D.k32_alt, D.perm_alt, total, 0, seg_bits, table,
-                                                 scr, st, &launches);
+                                                 scr, st, &launches, block_sort_max);
       const uint32_t *perm = f2 ? D.perm_alt : D.perm;
       k_gather_keys<<<grid_for(total, 256), 256, 0, st>>>(D.key, D.val, perm, D.key_alt, D.val_alt, total);
       launches++;
@@ -220,7 +226,8 @@ struct IterationDriver
     {
       if (per_level[L] <= 0)
         continue;
-      const unsigned mg = std::max(1u, std::min(grid_for(per_level[L], 256), (unsigned)sm_count * 8u));
+      const unsigned mg =
+        std::max(1u, std::min(grid_for(per_level[L], 256), (unsigned)sm_count * (unsigned)moments_blocks_per_sm));
       if (geometric)
         k_tree_bounds<<<mg, 256, 0, st>>>(D, L);
       else
@@ -259,15 +266,18 @@ struct IterationDriver
     // done tries the following ranges one atomic each, so empty ranges cost time)
     const int per = (chunk_total + std::min(sm_count, chunk_total) - 1) / std::min(sm_count, chunk_total);
     const int nranges = (chunk_total + per - 1) / per;
-    if (D.walk_ctr)
+    DevState Dw = D;
+    if (chunk_total < walk_ranged_min)
+      Dw.walk_ctr = nullptr; // a grid-stride loop, one warp per chunk
+    if (Dw.walk_ctr)
     { // one resident wave over per-SM chunk ranges
-      mem.check(cudaMemsetAsync(D.walk_ctr, 0, sizeof(unsigned) * (size_t)nranges, st));
+      mem.check(cudaMemsetAsync(Dw.walk_ctr, 0, sizeof(unsigned) * (size_t)nranges, st));
       grid = std::min<unsigned>(grid, (unsigned)sm_count * (unsigned)walk_blocks_per_sm);
     }
     if (K.count_interactions)
-      k_walk<true><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, nranges);
+      k_walk<true><<<grid, 32 * kWalkWarps, 0, st>>>(Dw, K, chunk_total, nranges);
     else
-      k_walk<false><<<grid, 32 * kWalkWarps, 0, st>>>(D, K, chunk_total, nranges);
+      k_walk<false><<<grid, 32 * kWalkWarps, 0, st>>>(Dw, K, chunk_total, nranges);
     launches++;
     walk_launches++;
     check();

@@ -586,21 +586,25 @@ inline size_t radix_table_elems(long long n)
 // Sorts (keys, vals) on bits [begin_bit, end_bit).  Ping-pongs between the
 // two buffer pairs; returns true when the result lies in (k_alt, v_alt).
 // `table` holds radix_table_elems(n) ints, `scan_scratch`
-// scan_scratch_elems<int>(radix_table_elems(n)) ints.
+// scan_scratch_elems<int>(radix_table_elems(n)) ints.  Sorts of at most
+// `block_max` items (<= kRadixBlockMax) run in one block; the result is the
+// same either way (a stable sort).
 template <typename K>
 bool radix_sort_pairs(K *keys, uint32_t *vals, K *k_alt, uint32_t *v_alt, long long n, int begin_bit, int end_bit,
-                      int *table, int *scan_scratch, cudaStream_t st, int64_t *launches)
+                      int *table, int *scan_scratch, cudaStream_t st, int64_t *launches,
+                      int block_max = kRadixBlockMax)
 {
   if (n <= 1 || end_bit <= begin_bit)
     return false;
-  if (n <= kRadixTile)
+  block_max = block_max < kRadixBlockMax ? block_max : kRadixBlockMax;
+  if (n <= kRadixTile && n <= block_max)
   { // one block, every pass in shared memory; the result stays in (keys, vals)
     k_radix_sort_block<K, kRadixThreads><<<1, kRadixThreads, radix_block_smem<K>(kRadixThreads), st>>>(
       keys, vals, (int)n, begin_bit, end_bit);
     (*launches)++;
     return false;
   }
-  if (n <= kRadixBlockMax)
+  if (n <= block_max)
   {
     const size_t smem = radix_block_smem<K>(1024);
     cudaFuncSetAttribute(k_radix_sort_block<K, 1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

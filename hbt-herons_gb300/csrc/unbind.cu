@@ -140,7 +140,7 @@ enum Slot
   S_KEY, S_KEYA, S_VAL, S_VALA, S_K32, S_K32A, S_CNT, S_X, S_FLAGS, S_F,
   S_NODES, S_TABLE, S_SCRATCH, S_CELLS, S_LVL, S_COUNTER, S_PERM, S_PERMA, S_FBL, S_FBC, S_TMASS, S_COMP, S_SP, S_TGT, S_BND, S_FACTOR,
   S_WARMI, S_REF0, S_RMAX, S_MMAX, S_WBB, S_HIST, S_TAB, S_FEAT, S_PROP, S_PNB, S_PEN, S_MODEL, S_NB1,
-  S_POTI, S_WCTR, S_FRAMEW,
+  S_POTI, S_WCTR, S_FRAMEW, S_TUNE,
   S_PR_OFF, S_PR_CNT, S_PR_FIN, S_PR_RR, S_PR_MM, S_PR_K, S_PR_V, S_PR_KA, S_PR_VA, S_PR_MC, S_PR_VK, S_PR_SO,
   S_PR_SH, S_PR_SCR, S_PR_POS, S_PR_MASS, S_PR_ORD, S_PR_NB, S_PR_MBND, S_PR_MBP, S_PR_OUTF, S_PR_OUTI, S_PR_OUTL,
   S_RE_OFF, S_RE_SG, S_RE_GP, S_RE_FL, S_RE_RK, S_RE_TG, S_RE_TS, S_RE_GO, S_RE_POS, S_RE_TY, S_RE_DEST,
@@ -215,6 +215,8 @@ struct hbtg_handle
   float exclude_below = 0.f;
   long long min_particles = 0;
   int first_test = 1;
+  // launch settings (hbtg_set_tuning, hbtg_autotune)
+  hbtg_tuning tune{kRadixBlockMax, 0, 8, 0.0};
   // state of the last unbinding call, for hbtg_trace_labels_device
   int last_S = 0;
   long long last_N = 0;
@@ -385,6 +387,9 @@ int run_device(hbtg_handle *H, const hbtg_params *p, const hbtg_batch *b, cudaSt
   R.K = make_kparams(p, H->count_interactions);
   R.S = S;
   R.sm_count = H->sm_count;
+  R.block_sort_max = H->tune.block_sort_max;
+  R.walk_ranged_min = H->tune.walk_ranged_min;
+  R.moments_blocks_per_sm = H->tune.moments_blocks_per_sm;
   int bits = 0;
   while ((1LL << bits) < S)
     bits++;
@@ -889,6 +894,95 @@ int dev_call(void *arg)
   const int rc = run_device(c.H, c.p, c.b, c.st, c.wa);
   HBTG_CUDA(cudaStreamSynchronize(c.st));
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner of the launch settings (hbtg_autotune)
+// ---------------------------------------------------------------------------
+struct TuneCall
+{
+  hbtg_handle *H;
+  const hbtg_params *p;
+  hbtg_batch *b;
+  cudaStream_t st;
+  hbtg_tuning *report;
+  int max_report;
+  int *n_report;
+};
+
+int tune_call(void *arg)
+{
+  TuneCall &c = *static_cast<TuneCall *>(arg);
+  hbtg_handle *H = c.H;
+  hbtg_batch *b = c.b;
+  long long N = 0;
+  int rc = validate(c.p, b, N);
+  if (rc != HBTG_OK)
+    return rc;
+  HBTG_CUDA(cudaSetDevice(H->device));
+  cudaStream_t st = c.st;
+  const size_t S = (size_t)b->n_sub;
+  // the in/out frames, saved once and restored before every trial
+  float *const fr[4] = {b->ref_pos, b->ref_vel, b->mostbound_pos, b->mostbound_vel};
+  const size_t fbytes = sizeof(float) * 3 * S, ibytes = sizeof(int64_t) * S;
+  unsigned char *save = H->pool.get<unsigned char>(S_TUNE, 4 * fbytes + ibytes);
+  for (int k = 0; k < 4; k++)
+    if (fr[k] && S)
+      HBTG_CUDA(cudaMemcpyAsync(save + k * fbytes, fr[k], fbytes, cudaMemcpyDeviceToDevice, st));
+  if (b->most_bound_id && S)
+    HBTG_CUDA(cudaMemcpyAsync(save + 4 * fbytes, b->most_bound_id, ibytes, cudaMemcpyDeviceToDevice, st));
+  auto restore = [&]() {
+    for (int k = 0; k < 4; k++)
+      if (fr[k] && S)
+        HBTG_CUDA(cudaMemcpyAsync(fr[k], save + k * fbytes, fbytes, cudaMemcpyDeviceToDevice, st));
+    if (b->most_bound_id && S)
+      HBTG_CUDA(cudaMemcpyAsync(b->most_bound_id, save + 4 * fbytes, ibytes, cudaMemcpyDeviceToDevice, st));
+  };
+  const hbtg_tuning before = H->tune;
+  cudaEvent_t e0, e1;
+  HBTG_CUDA(cudaEventCreate(&e0));
+  HBTG_CUDA(cudaEventCreate(&e1));
+  std::vector<hbtg_tuning> tried;
+  for (int bs : {0, 2048, kRadixBlockMax})
+    for (int wr : {0, 1024})
+      for (int mb : {4, 8})
+      {
+        H->tune = hbtg_tuning{bs, wr, mb, 0.0};
+        float ms = 0.f;
+        for (int rep = 0; rep < 2 && rc == HBTG_OK; rep++)
+        {
+          restore();
+          HBTG_CUDA(cudaEventRecord(e0, st));
+          rc = run_device(H, c.p, b, st);
+          HBTG_CUDA(cudaEventRecord(e1, st));
+          HBTG_CUDA(cudaStreamSynchronize(st));
+          if (rc == HBTG_ERR_MAX_ITER)
+            rc = HBTG_OK; // the same for every candidate; only the time matters here
+          HBTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        }
+        if (rc != HBTG_OK)
+          break;
+        tried.push_back(hbtg_tuning{bs, wr, mb, (double)ms});
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  restore();
+  HBTG_CUDA(cudaStreamSynchronize(st));
+  if (rc != HBTG_OK || tried.empty())
+  {
+    H->tune = before;
+    return rc != HBTG_OK ? rc : HBTG_ERR_INVALID;
+  }
+  size_t best = 0;
+  for (size_t i = 1; i < tried.size(); i++)
+    if (tried[i].ms < tried[best].ms)
+      best = i;
+  H->tune = tried[best];
+  for (size_t i = 0; i < tried.size() && (int)i < c.max_report; i++)
+    c.report[i] = tried[i];
+  if (c.n_report)
+    *c.n_report = (int)tried.size();
+  return HBTG_OK;
 }
 
 // ---------------------------------------------------------------------------
@@ -1572,6 +1666,33 @@ int hbtg_set_count_interactions(hbtg_handle *h, int enable)
     return HBTG_ERR_INVALID;
   h->count_interactions = enable != 0;
   return HBTG_OK;
+}
+
+int hbtg_get_tuning(const hbtg_handle *h, hbtg_tuning *t)
+{
+  if (!h || !t)
+    return HBTG_ERR_INVALID;
+  *t = h->tune;
+  return HBTG_OK;
+}
+
+int hbtg_set_tuning(hbtg_handle *h, const hbtg_tuning *t)
+{
+  if (!h || !t || t->block_sort_max < 0 || t->walk_ranged_min < 0 || t->moments_blocks_per_sm < 1 ||
+      t->moments_blocks_per_sm > 32)
+    return HBTG_ERR_INVALID;
+  h->tune = *t;
+  h->tune.block_sort_max = std::min(t->block_sort_max, kRadixBlockMax);
+  return HBTG_OK;
+}
+
+int hbtg_autotune(hbtg_handle *h, const hbtg_params *p, hbtg_batch *b, void *cuda_stream, hbtg_tuning *report,
+                  int max_report, int *n_report)
+{
+  if (!h || max_report < 0 || (max_report > 0 && !report))
+    return HBTG_ERR_INVALID;
+  TuneCall c{h, p, b, static_cast<cudaStream_t>(cuda_stream), report, max_report, n_report};
+  return guarded(tune_call, &c);
 }
 
 const char *hbtg_status_string(int status)

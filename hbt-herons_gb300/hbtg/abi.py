@@ -173,6 +173,15 @@ class CPrior(C.Structure):
     _fields_ = [("nbound_prev", _P), ("energy_prev", _P)]
 
 
+class CTuning(C.Structure):
+    """hbtg_tuning: launch settings that leave every result unchanged."""
+    _fields_ = [("block_sort_max", C.c_int32), ("walk_ranged_min", C.c_int32), ("moments_blocks_per_sm", C.c_int32),
+                ("ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class CModel(C.Structure):
     """hbtg_model."""
     _fields_ = [("weights", _P), ("threshold", C.c_float), ("min_particles", C.c_int64),

@@ -55,11 +55,13 @@ def library(path=LIB):
         lib.hbtg_mlp_backward.argtypes = [P, P, P, P, C.c_int64, P, P, P]
         lib.hbtg_adam_step.argtypes = [P, P, P, P, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
                                        C.c_int, P]
+        lib.hbtg_get_tuning.argtypes = [P, P]
+        lib.hbtg_set_tuning.argtypes = [P, P]
         for fn in ("hbtg_create", "hbtg_destroy", "hbtg_unbind_batch", "hbtg_unbind_batch_device", "hbtg_get_stats",
                    "hbtg_set_count_interactions", "hbtg_set_model", "hbtg_unbind_batch_learned",
                    "hbtg_unbind_batch_learned_device", "hbtg_unbind_batch_warm_device", "hbtg_features_device",
                    "hbtg_trace_labels_device", "hbtg_mlp_forward", "hbtg_mlp_backward", "hbtg_adam_step",
-                   "hbtg_tree_potential_device"):
+                   "hbtg_tree_potential_device", "hbtg_get_tuning", "hbtg_set_tuning"):
             getattr(lib, fn).restype = C.c_int
         _lib = lib
     return _lib
@@ -97,6 +99,37 @@ class Unbinder:
 
     def count_interactions(self, enable=True):
         self.lib.hbtg_set_count_interactions(self.h, int(enable))
+
+    # -- launch settings ------------------------------------------------------
+    def tuning(self):
+        """The handle's launch settings (hbtg_get_tuning), as a dict."""
+        from .abi import CTuning
+        t = CTuning()
+        rc = self.lib.hbtg_get_tuning(self.h, C.byref(t))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_get_tuning")
+        return t.as_dict()
+
+    def set_tuning(self, block_sort_max, walk_ranged_min, moments_blocks_per_sm):
+        from .abi import CTuning
+        t = CTuning(int(block_sort_max), int(walk_ranged_min), int(moments_blocks_per_sm), 0.0)
+        rc = self.lib.hbtg_set_tuning(self.h, C.byref(t))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_set_tuning")
+
+    def autotune(self, params: Params, cbatch: CBatch, stream_ptr=0):
+        """hbtg_autotune on a device batch: the candidates with their times;
+        the fastest becomes the handle's setting."""
+        from .abi import CTuning
+        rep = (CTuning * 64)()
+        n = C.c_int(0)
+        fn = self.lib.hbtg_autotune
+        fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+        fn.restype = C.c_int
+        rc = fn(self.h, C.byref(params), C.byref(cbatch), C.c_void_p(stream_ptr), rep, 64, C.byref(n))
+        if rc != 0:
+            raise UnbindError(rc, "hbtg_autotune")
+        return [rep[i].as_dict() for i in range(min(n.value, 64))]
 
     def unbind(self, inp: Inputs, params: Params, want_energy=True, want_potential=False, allow_max_iter=False):
         """Host-pointer call (hbtg_unbind_batch)."""

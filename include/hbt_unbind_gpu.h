@@ -209,6 +209,36 @@ int hbtg_get_stats(const hbtg_handle *handle, hbtg_stats *stats);
  * (slower; used to compute the roofline's algorithmic flops). */
 int hbtg_set_count_interactions(hbtg_handle *handle, int enable);
 
+/* Launch settings of the unbinding that leave every result unchanged: a
+ * stable radix sort gives the same order whether one block or a chain of
+ * passes runs it, the walk computes a 32-target chunk the same way whichever
+ * warp takes it, and each tree cell is summed by one thread whatever the
+ * grid.  No counterpart in the reference (they are choices of the GPU
+ * schedule, not of the method). */
+typedef struct hbtg_tuning
+{
+  int32_t block_sort_max;        /* sorts of at most this many items run in one block (0 = never; at most 8192) */
+  int32_t walk_ranged_min;       /* walks of fewer 32-target chunks use a grid-stride loop, the others per-SM ranges */
+  int32_t moments_blocks_per_sm; /* grid cap, in blocks per SM, of the per-level multipole passes (1-32) */
+  double ms;                     /* hbtg_autotune: measured time of one call with these settings (0 = not measured) */
+} hbtg_tuning;
+
+/* The handle's launch settings (defaults: 8192, 0, 8). */
+int hbtg_get_tuning(const hbtg_handle *handle, hbtg_tuning *tuning);
+int hbtg_set_tuning(hbtg_handle *handle, const hbtg_tuning *tuning);
+
+/* Autotuner: times hbtg_unbind_batch_device on `batch` (device arrays and
+ * host offsets, as for that call) for each candidate setting
+ * (block_sort_max in {0, 2048, 8192} x walk_ranged_min in {0, 1024} x
+ * moments_blocks_per_sm in {4, 8}), two calls each with the second timed,
+ * and keeps the fastest on the handle.  The batch's in/out frame arrays are
+ * restored before every call and on return, so they hold their inputs again;
+ * its outputs hold the results, which every candidate gives alike.  report
+ * (may be NULL) receives up to max_report candidates with their times and
+ * *n_report (may be NULL) their number.  No counterpart in the reference. */
+int hbtg_autotune(hbtg_handle *handle, const hbtg_params *params, hbtg_batch *batch, void *cuda_stream,
+                  hbtg_tuning *report, int max_report, int *n_report);
+
 /* Static description of a return code. */
 const char *hbtg_status_string(int status);
 
