@@ -120,13 +120,21 @@ inline float norm2_f(const float *d) { return d[0] * d[0] + d[1] * d[1] + d[2] *
  * ---------------------------------------------------------------------- */
 class Tree
 {
-  struct Cell
+  /* One cell: its eight sons while the tree is built, then its multipole and
+   * links, in the same 64 bytes, as the reference's TreeCell_t union
+   * (src/oct_tree.h:30-45); finalize copies a cell's sons out before it
+   * writes the multipole over them. */
+  union Cell
   {
     int64_t son[8];
-    float s[3];
-    float len, mass;
-    int64_t sibling, nextnode;
+    struct
+    {
+      float s[3];
+      float len, mass;
+      int64_t sibling, nextnode;
+    };
   };
+  static_assert(sizeof(Cell) == 64, "cell size");
   std::vector<Cell> cells;
   std::vector<int64_t> next_of;
   const float *const *xs = nullptr; /* per source: pointer to float[3] */
