@@ -31,3 +31,18 @@ def test_library_exports_every_declared_symbol():
     assert not missing, missing
     lib.hbtg_status_string.restype = ctypes.c_char_p  # a pure host entry point needs no device
     assert lib.hbtg_status_string(0) == b"ok"
+
+
+def test_launch_setting_entry_points_reject_bad_arguments_without_a_device():
+    """hbtg_get_tuning / hbtg_set_tuning / hbtg_autotune check their arguments
+    before any CUDA call: a null handle is HBTG_ERR_INVALID (1)."""
+    from hbtg.abi import CTuning
+    from hbtg.build import build_library
+    lib = ctypes.CDLL(build_library())
+    t = CTuning(8192, 0, 8, 0.0)
+    lib.hbtg_get_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.hbtg_set_tuning.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.hbtg_autotune.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_int, ctypes.c_void_p]
+    assert lib.hbtg_get_tuning(None, ctypes.byref(t)) == 1
+    assert lib.hbtg_set_tuning(None, ctypes.byref(t)) == 1
+    assert lib.hbtg_autotune(None, None, None, None, None, 0, None) == 1
